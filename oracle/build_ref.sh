@@ -1,0 +1,24 @@
+#!/bin/sh
+# Builds the reference's own C kernels (algn.c with the files it #includes,
+# nonaddCSc.c specialised to 8-bit characters by the reference's sed rule,
+# avl.c and zarr.c to satisfy union.c) straight from the reference sources,
+# plus oracle/ref_driver.c, into oracle/_ref/libporef.so.
+# Test infrastructure only; run where the reference sources are present.
+# Usage: oracle/build_ref.sh [REFERENCE_SRC_DIR]
+set -e
+REF="${1:-${POYD_REFERENCE_SRC:-/root/reference/src}}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+[ -f "$REF/algn.c" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
+mkdir -p "$OUT"
+CF="-O2 -fPIC -w -I$HERE -I$REF"
+gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/algn.c" -o "$OUT/algn.o"
+gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/avl.c" -o "$OUT/avl.o"
+gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/zarr.c" -o "$OUT/zarr.o"
+# myocamlbuild.ml.in:262-269 / 287-289: sed-specialise to CHARSIZE 8
+sed -e 's/nonadd_/nonadd8_/g' -e 's/NONADDSIZE/8/g' "$REF/nonaddCSc.c" | \
+    gcc -std=gnu89 -fgnu89-inline $CF -DCHARSIZE=8 -x c - -c -o "$OUT/nonadd8.o"
+gcc -std=gnu99 $CF -c "$HERE/ref_driver.c" -o "$OUT/ref_driver.o"
+gcc -shared -o "$OUT/libporef.so" "$OUT/algn.o" "$OUT/avl.o" "$OUT/zarr.o" \
+    "$OUT/nonadd8.o" "$OUT/ref_driver.o" -lm
+echo "$OUT/libporef.so"

@@ -1,0 +1,301 @@
+"""ctypes bindings for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries live here:
+
+* ``_build/liboracle.so`` -- the plain-C restatement of the reference's
+  scoring path (``poy_oracle.c``), built by ``build_oracle.sh``;
+* ``_ref/libporef.so`` -- the reference's own ``algn.c`` / ``nonaddCSc.c``
+  compiled from source by ``build_ref.sh`` where the sources are available.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU arms use this
+module, and only as the checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libporef.so")
+
+u8p = C.POINTER(C.c_uint8)
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+
+
+class OrCM(C.Structure):
+    """Mirror of ``or_cm`` (poy_oracle.h)."""
+
+    _fields_ = [
+        ("lcm", C.c_int32), ("gap", C.c_int32), ("a_sz", C.c_int32),
+        ("combinations", C.c_int32), ("cost_model", C.c_int32),
+        ("gap_open", C.c_int32), ("is_metric", C.c_int32),
+        ("all_elements", C.c_int32),
+        ("cost", C.c_int32 * 1024), ("worst", C.c_int32 * 1024),
+        ("prepend", C.c_int32 * 32), ("tail", C.c_int32 * 32),
+        ("median", C.c_uint8 * 1024),
+    ]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")],
+                              stdout=subprocess.DEVNULL)
+    return LIB_PATH
+
+
+def build_ref(src_dir: str | None = None) -> str | None:
+    """Compile the reference C kernels when their sources are present."""
+    src = src_dir or os.environ.get("POYD_REFERENCE_SRC", "/root/reference/src")
+    if not os.path.exists(os.path.join(src, "algn.c")):
+        return None
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), src],
+                          stdout=subprocess.DEVNULL)
+    return REF_PATH
+
+
+_lib = None
+_ref = None
+
+
+def _ptr(a, t=u8p):
+    return a.ctypes.data_as(t)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.or_cm_dna.argtypes = [C.POINTER(OrCM), C.c_int, C.c_int, C.c_int]
+        L.or_cm_of_matrix5.argtypes = [C.POINTER(OrCM), i32p, C.c_int]
+        L.or_cost2_deltaw.argtypes = [u8p, C.c_int, u8p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.or_simple_2.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), C.c_int,
+                                  C.POINTER(C.c_uint16)]
+        L.or_band_cells_linear.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.or_band_cells_linear.restype = C.c_int64
+        L.or_band_cells_affine.argtypes = [C.c_int, C.c_int]
+        L.or_band_cells_affine.restype = C.c_int64
+        L.or_align_2.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), u8p, u8p,
+                                 C.POINTER(C.c_int)]
+        L.or_cost_2.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), C.c_int, C.c_int]
+        for n in ("or_median_2_with_gaps", "or_median_2_no_gaps", "or_ancestor_2"):
+            getattr(L, n).argtypes = [u8p, u8p, C.c_int, C.POINTER(OrCM), u8p]
+        for n in ("or_worst_2", "or_verify_2"):
+            getattr(L, n).argtypes = [u8p, u8p, C.c_int, C.POINTER(OrCM)]
+        L.or_cost_affine_3.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM)]
+        L.or_align_affine_3.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), u8p,
+                                        C.POINTER(C.c_int), u8p, C.POINTER(C.c_int), u8p, u8p,
+                                        C.POINTER(C.c_int)]
+        L.or_dos_median.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), u8p,
+                                    C.POINTER(C.c_int), u8p, u8p, u8p, C.POINTER(C.c_int)]
+        L.or_nonadd_median.argtypes = [u8p, u8p, C.c_int, u8p]
+        L.or_nonadd_median.restype = C.c_int64
+        L.or_nonadd_distance.argtypes = [u8p, u8p, C.c_int]
+        L.or_nonadd_distance.restype = C.c_int64
+        L.or_nonadd_median_3.argtypes = [u8p, u8p, u8p, u8p, C.c_int, u8p]
+        L.or_nonadd_dist_2.argtypes = [u8p, u8p, u8p, C.c_int]
+        L.or_nonadd_dist_2.restype = C.c_int64
+        L.or_sank_elt_median.argtypes = [C.c_int, i64p, i64p, i64p, i64p, i64p, i64p]
+        L.or_sank_elt_distance.argtypes = [C.c_int, i64p, i64p, i64p]
+        L.or_sank_elt_distance.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The compiled reference, or None when it is not built here."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = C.CDLL(REF_PATH)
+        R.ref_cm_new.argtypes = [C.POINTER(OrCM)]
+        R.ref_cm_new.restype = C.c_void_p
+        R.ref_cm_free.argtypes = [C.c_void_p]
+        R.ref_simple_2.argtypes = [u8p, C.c_int, u8p, C.c_int, C.c_void_p, C.c_int]
+        R.ref_align_2.argtypes = [u8p, C.c_int, u8p, C.c_int, C.c_void_p, C.c_int, u8p, u8p,
+                                  C.POINTER(C.c_int)]
+        R.ref_cost_affine_3.argtypes = [u8p, C.c_int, u8p, C.c_int, C.c_void_p]
+        R.ref_align_affine_3.argtypes = [u8p, C.c_int, u8p, C.c_int, C.c_void_p, u8p,
+                                         C.POINTER(C.c_int), u8p, C.POINTER(C.c_int), u8p, u8p,
+                                         C.POINTER(C.c_int)]
+        for n in ("ref_ancestor_2", "ref_median_2_with_gaps", "ref_median_2_no_gaps"):
+            getattr(R, n).argtypes = [u8p, u8p, C.c_int, C.c_void_p, u8p]
+        for n in ("ref_worst_2", "ref_verify_2"):
+            getattr(R, n).argtypes = [u8p, u8p, C.c_int, C.c_void_p]
+        R.ref_nonadd8_median.argtypes = [u8p, u8p, C.c_int, u8p]
+        R.ref_nonadd8_median.restype = C.c_long
+        R.ref_nonadd8_distance.argtypes = [u8p, u8p, C.c_int]
+        R.ref_nonadd8_distance.restype = C.c_long
+        R.ref_nonadd8_median_3.argtypes = [u8p, u8p, u8p, u8p, C.c_int, u8p]
+        _ref = R
+    return _ref
+
+
+# --------------------------------------------------------------------------
+# Pythonic wrappers over the restatement
+# --------------------------------------------------------------------------
+
+def cm_dna(sub: int = 1, indel: int = 2, gap_open: int = -1) -> OrCM:
+    m = OrCM()
+    lib().or_cm_dna(C.byref(m), sub, indel, gap_open)
+    return m
+
+
+def cm_tables(m: OrCM) -> dict:
+    return {
+        "cost": np.ctypeslib.as_array(m.cost).copy(),
+        "worst": np.ctypeslib.as_array(m.worst).copy(),
+        "prepend": np.ctypeslib.as_array(m.prepend).copy(),
+        "tail": np.ctypeslib.as_array(m.tail).copy(),
+        "median": np.ctypeslib.as_array(m.median).copy(),
+        "cost_model": m.cost_model, "gap_open": m.gap_open, "gap": m.gap,
+    }
+
+
+def _u8(x):
+    return np.ascontiguousarray(x, dtype=np.uint8)
+
+
+def deltaw(a, b, m: OrCM, explicit: int | None = None) -> int:
+    a, b = _u8(a), _u8(b)
+    if len(a) >= len(b):
+        s1, s2 = a, b
+    else:
+        s1, s2 = b, a
+    return lib().or_cost2_deltaw(_ptr(s1), len(s1), _ptr(s2), len(s2), m.gap,
+                                 0 if explicit is None else 1, explicit or 0)
+
+
+def cost_2(a, b, m: OrCM, explicit_deltaw: int | None = None) -> int:
+    a, b = _u8(a), _u8(b)
+    return lib().or_cost_2(_ptr(a), len(a), _ptr(b), len(b), C.byref(m),
+                           0 if explicit_deltaw is None else 1, explicit_deltaw or 0)
+
+
+def simple_2(s1, s2, m: OrCM, dw: int, want_dm: bool = False):
+    s1, s2 = _u8(s1), _u8(s2)
+    dm = np.zeros(len(s1) * len(s2), dtype=np.uint16) if want_dm else None
+    c = lib().or_simple_2(_ptr(s1), len(s1), _ptr(s2), len(s2), C.byref(m), dw,
+                          dm.ctypes.data_as(C.POINTER(C.c_uint16)) if want_dm else None)
+    return (c, dm) if want_dm else c
+
+
+def band_cells_linear(l1: int, l2: int, dw: int) -> int:
+    return lib().or_band_cells_linear(max(l1, l2), min(l1, l2), dw)
+
+
+def band_cells_affine(l1: int, l2: int) -> int:
+    return lib().or_band_cells_affine(l1, l2)
+
+
+def align_2(a, b, m: OrCM):
+    a, b = _u8(a), _u8(b)
+    ra = np.zeros(len(a) + len(b) + 2, np.uint8)
+    rb = np.zeros_like(ra)
+    n = C.c_int()
+    c = lib().or_align_2(_ptr(a), len(a), _ptr(b), len(b), C.byref(m), _ptr(ra), _ptr(rb),
+                         C.byref(n))
+    return c, ra[:n.value].copy(), rb[:n.value].copy()
+
+
+def _pair_fn(name, a, b, m, extra=1):
+    a, b = _u8(a), _u8(b)
+    out = np.zeros(len(a) + extra + 1, np.uint8)
+    n = getattr(lib(), name)(_ptr(a), _ptr(b), len(a), C.byref(m), _ptr(out))
+    return out[:n].copy()
+
+
+def median_2_with_gaps(a, b, m):
+    return _pair_fn("or_median_2_with_gaps", a, b, m)
+
+
+def median_2(a, b, m):
+    return _pair_fn("or_median_2_no_gaps", a, b, m)
+
+
+def ancestor_2(a, b, m):
+    return _pair_fn("or_ancestor_2", a, b, m)
+
+
+def worst_2(a, b, m):
+    a, b = _u8(a), _u8(b)
+    return lib().or_worst_2(_ptr(a), _ptr(b), len(a), C.byref(m))
+
+
+def verify_2(a, b, m):
+    a, b = _u8(a), _u8(b)
+    return lib().or_verify_2(_ptr(a), _ptr(b), len(a), C.byref(m))
+
+
+def cost_affine_3(a, b, m):
+    a, b = _u8(a), _u8(b)
+    return lib().or_cost_affine_3(_ptr(a), len(a), _ptr(b), len(b), C.byref(m))
+
+
+def align_affine_3(a, b, m):
+    a, b = _u8(a), _u8(b)
+    cap = len(a) + len(b) + 2
+    med, mwg, ri, rj = (np.zeros(cap + 1, np.uint8) for _ in range(4))
+    lm, lw, lr = C.c_int(), C.c_int(), C.c_int()
+    c = lib().or_align_affine_3(_ptr(a), len(a), _ptr(b), len(b), C.byref(m), _ptr(med),
+                                C.byref(lm), _ptr(mwg), C.byref(lw), _ptr(ri), _ptr(rj),
+                                C.byref(lr))
+    return (c, med[:lm.value].copy(), mwg[:lw.value].copy(), ri[:lr.value].copy(),
+            rj[:lr.value].copy())
+
+
+def dos_median(a, b, m):
+    """DOS.median: (cost, median, aligned a, aligned b, median with gaps)."""
+    a, b = _u8(a), _u8(b)
+    cap = len(a) + len(b) + 2
+    sm, ra, rb, wg = (np.zeros(cap + 1, np.uint8) for _ in range(4))
+    lm, la = C.c_int(), C.c_int()
+    c = lib().or_dos_median(_ptr(a), len(a), _ptr(b), len(b), C.byref(m), _ptr(sm),
+                            C.byref(lm), _ptr(ra), _ptr(rb), _ptr(wg), C.byref(la))
+    return (c, sm[:lm.value].copy(), ra[:la.value].copy(), rb[:la.value].copy(),
+            wg[:la.value].copy())
+
+
+def nonadd_median(a, b):
+    a, b = _u8(a), _u8(b)
+    r = np.zeros(len(a), np.uint8)
+    c = lib().or_nonadd_median(_ptr(a), _ptr(b), len(a), _ptr(r))
+    return c, r
+
+
+def nonadd_distance(a, b):
+    a, b = _u8(a), _u8(b)
+    return lib().or_nonadd_distance(_ptr(a), _ptr(b), len(a))
+
+
+def nonadd_median_3(A, N, D1, D2):
+    A, N, D1, D2 = (_u8(x) for x in (A, N, D1, D2))
+    F = np.zeros(len(A), np.uint8)
+    lib().or_nonadd_median_3(_ptr(A), _ptr(N), _ptr(D1), _ptr(D2), len(A), _ptr(F))
+    return F
+
+
+SANK_INF = ((1 << 62) - 1) // 4
+
+
+def sank_elt_median(tcm, a_s, b_s):
+    tcm = np.ascontiguousarray(tcm, np.int64)
+    a_s = np.ascontiguousarray(a_s, np.int64)
+    b_s = np.ascontiguousarray(b_s, np.int64)
+    k = len(a_s)
+    c, e, beta = (np.zeros(k, np.int64) for _ in range(3))
+    lib().or_sank_elt_median(k, _ptr(tcm, i64p), _ptr(a_s, i64p), _ptr(b_s, i64p),
+                             _ptr(c, i64p), _ptr(e, i64p), _ptr(beta, i64p))
+    return c, e, beta
+
+
+def sank_elt_distance(tcm, a_s, b_s):
+    tcm = np.ascontiguousarray(tcm, np.int64)
+    a_s = np.ascontiguousarray(a_s, np.int64)
+    b_s = np.ascontiguousarray(b_s, np.int64)
+    return lib().or_sank_elt_distance(len(a_s), _ptr(tcm, i64p), _ptr(a_s, i64p),
+                                      _ptr(b_s, i64p))
