@@ -1,0 +1,198 @@
+/*
+ * poyd_gb300 -- C ABI of the GB300 (sm_103a) direct-optimization scoring path.
+ *
+ * Plain pointers and sizes only.  Sequences use POY's bitmask alphabet (DNA:
+ * A=1, C=2, G=4, T=8, gap=16, ambiguity codes are unions) and start with the
+ * leading gap at position 0, exactly like the reference's `struct seq`
+ * contents (seq.h:46-54).  Output sequences are written the way the reference
+ * prepends into a `seq`: right-aligned at the END of a caller-provided slot,
+ * so element i of a result of length n sits at slot[cap - n + i].
+ *
+ * Every entry point returns 0 on success or a negative POYD_E* code; the
+ * reference instead raises an OCaml exception through failwith
+ * (matrices.c:107-113, cm.c:345-358), which an OCaml stub over this ABI
+ * would do on a non-zero return.  poyd_last_error() gives the message.
+ *
+ * Device pointers are CUDA global-memory pointers; `stream` is a
+ * cudaStream_t (NULL = legacy default stream).
+ */
+#ifndef POYD_GB300_H
+#define POYD_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define POYD_OK 0
+#define POYD_EINVAL -1   /* bad argument */
+#define POYD_ECUDA -2    /* CUDA runtime error */
+#define POYD_ERANGE -3   /* costs or lengths outside the supported range */
+#define POYD_ENOMEM -4   /* device allocation failed */
+#define POYD_EUNSUP -5   /* cost matrix form the GPU path does not implement */
+
+/*
+ * Two-dimensional transformation cost matrix over the bitmask alphabet,
+ * restricted to lcm <= 5 (struct cm, cm.h:29-43).  Tables are indexed
+ * (a << 5) + b.  Built by poyd_cm_dna / poyd_cm_of_matrix5, which restate
+ * Cost_matrix.Two_D's constructors (cost_matrix.ml:520-656).
+ */
+typedef struct poyd_cm {
+    int32_t lcm;
+    int32_t gap;
+    int32_t a_sz;
+    int32_t combinations;
+    int32_t cost_model; /* 0 linear, 1 affine (Cost_matrix.cost_model) */
+    int32_t gap_open;
+    int32_t is_metric;
+    int32_t all_elements;
+    int32_t cost[1024];
+    int32_t worst[1024];
+    int32_t prepend[32];
+    int32_t tail[32];
+    uint8_t median[1024];
+} poyd_cm;
+
+const char *poyd_last_error(void);
+int poyd_version(void);
+
+/* Replaces Cost_matrix.Two_D.of_transformations_and_gaps true 5 sub indel 31
+ * (cost_matrix.ml:645-656) followed, for gap_open >= 0, by
+ * Cost_matrix.Two_D.set_affine (cost_matrix.ml:405-416).  gap_open < 0 keeps
+ * the linear model (Cost_matrix.Two_D.default is poyd_cm_dna(m, 1, 2, -1)). */
+int poyd_cm_dna(poyd_cm *m, int32_t sub, int32_t indel, int32_t gap_open);
+/* Replaces Cost_matrix.Two_D.of_list ~use_comb:true over a 5x5 matrix
+ * (A, C, G, T, gap) (cost_matrix.ml:559-563, 520-538), then set_affine as
+ * above. */
+int poyd_cm_of_matrix5(poyd_cm *m, const int32_t *mat25, int32_t gap_open);
+
+/* ---------------------------------------------------------------------
+ * Batched pairwise direct optimization (device-resident inputs).
+ *
+ * `seq` is one device buffer holding every sequence; pair i is
+ * a = seq[a_off[i] .. a_off[i]+a_len[i]) and b likewise, in the caller's
+ * argument order (the order Sequence.Align.cost_2/align_2 receive).  All
+ * per-pair arrays are device arrays of length n.
+ * ------------------------------------------------------------------- */
+
+/* deltaw policies for the linear band (sequence.ml:691-713) */
+#define POYD_DELTAW_DEFAULT 0 /* cost_2 without ?deltaw (align_2, median) */
+#define POYD_DELTAW_EXPLICIT 1 /* cost_2 ~deltaw:deltaw[i] */
+#define POYD_DELTAW_DOS_DISTANCE 2 /* DOS.distance: max(|la-lb|, 8) (seqCS.ml:856-866) */
+
+/* Batched Sequence.Align.cost_2 (sequence.ml:716-723): for each pair the
+ * linear banded cost algn_CAML_simple_2 (algn.c:3409-3427) with the deltaw
+ * policy above, or, for an affine matrix, algn_CAML_cost_affine_3
+ * (algn.c:2628-2680).  cost[i] receives the result.  band_cells, when not
+ * NULL, receives the number of DP cells the reference's band evaluates for
+ * each pair (the unit of the GCUPS metric). */
+int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                      const int64_t *a_off, const int32_t *a_len,
+                      const int64_t *b_off, const int32_t *b_len,
+                      int32_t deltaw_policy, const int32_t *deltaw,
+                      int32_t *cost, int64_t *band_cells, void *stream);
+
+/* Batched DOS.median composition (seqCS.ml:747-776) with its pieces:
+ *   linear: align_2 (cost_2 + backtrack_2d, sequence.ml:849-869,
+ *           algn.c:3551-3666), ancestor_2 (algn.c:4126-4147) and
+ *           median_2_with_gaps (algn.c:4011-4024);
+ *   affine: align_affine_3 (algn.c:2551-2619).
+ * Pair i owns the device slot out + out_off[i] of 4*cap_i bytes,
+ * cap_i = a_len[i] + b_len[i] + 2, split in four right-aligned sequences:
+ *   [0, cap)      aligned a         (align_2's s1p / affine resi)
+ *   [cap, 2cap)   aligned b         (s2p / resj)
+ *   [2cap, 3cap)  median with gaps  (median_2_with_gaps / medianwg)
+ *   [3cap, 4cap)  median            (ancestor_2 / affine median)
+ * out_len[2i] = aligned length, out_len[2i+1] = median length.
+ * With POYD_FLAG_DOS_EMPTY, a pair whose a (or b) is all gaps returns cost 0
+ * and median = the other sequence, as DOS.median does (seqCS.ml:749-752). */
+#define POYD_FLAG_DOS_EMPTY 1
+int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                       const int64_t *a_off, const int32_t *a_len,
+                       const int64_t *b_off, const int32_t *b_len,
+                       int32_t *cost, uint8_t *out, const int64_t *out_off,
+                       int32_t *out_len, int64_t *band_cells, int32_t flags,
+                       void *stream);
+
+/* ---------------------------------------------------------------------
+ * Single-pair drop-ins with the OCaml externals' argument order
+ * (sequence.ml:453-466, 731-758).  Host pointers; each call runs the
+ * device path on one pair and synchronises.  A poyd_matrix plays the role
+ * of Matrix.m: algn_CAML_simple_2 leaves the direction matrix of its pair
+ * in it and algn_CAML_backtrack_2d reads it back (algn.c:3908-3924).
+ * ------------------------------------------------------------------- */
+typedef struct poyd_matrix poyd_matrix;
+poyd_matrix *poyd_matrix_create(void);
+void poyd_matrix_free(poyd_matrix *m);
+
+/* algn_CAML_simple_2(s1, s2, cm, mat, deltawh): s1 is the longer sequence
+ * (algn.c:3281); returns the cost through *cost. */
+int poyd_algn_simple_2(const uint8_t *s1, int32_t l1, const uint8_t *s2,
+                       int32_t l2, const poyd_cm *cm, poyd_matrix *mat,
+                       int32_t deltawh, int32_t *cost);
+/* algn_CAML_backtrack_2d(s1, s2, s1p, s2p, mat, cm, swap): prepends into
+ * s1p/s2p (capacity cap each, right-aligned) and sets their lengths. */
+int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8_t *s2,
+                           int32_t l2, uint8_t *s1p, uint8_t *s2p,
+                           int32_t cap, int32_t *len, poyd_matrix *mat,
+                           const poyd_cm *cm, int32_t swaped);
+/* algn_CAML_cost_affine_3(si, sj, cm, mat). */
+int poyd_algn_cost_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
+                            int32_t lj, const poyd_cm *cm, int32_t *cost);
+/* algn_CAML_align_affine_3(si, sj, cm, mat, resi, resj, median, medianwg):
+ * four right-aligned outputs of capacity cap = li + lj + 2 each. */
+int poyd_algn_align_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
+                             int32_t lj, const poyd_cm *cm, uint8_t *resi,
+                             uint8_t *resj, uint8_t *median, uint8_t *medianwg,
+                             int32_t cap, int32_t *lens /* [3]: res, median, medianwg */,
+                             int32_t *cost);
+
+/* ---------------------------------------------------------------------
+ * Fitch non-additive characters, 8-bit state masks (NonaddCS8).
+ * Batched over candidate pairs: row k of the result uses node rows
+ * a_idx[k] and b_idx[k] of `nodes` (device, n_nodes x len bytes, row
+ * stride `stride` bytes, a multiple of 16).
+ * ------------------------------------------------------------------- */
+/* char_nonadd8_CAML_distance (nonaddCSc.c:1076-1105) per candidate. */
+int poyd_nonadd8_distance_batch(const uint8_t *nodes, int64_t stride,
+                                int32_t len, int32_t n, const int32_t *a_idx,
+                                const int32_t *b_idx, int64_t *dist,
+                                void *stream);
+/* nonadd_median (nonaddCSc.c:422-462) per candidate: median rows into
+ * `out` (n x stride) and added_cost[k]. */
+int poyd_nonadd8_median_batch(const uint8_t *nodes, int64_t stride,
+                              int32_t len, int32_t n, const int32_t *a_idx,
+                              const int32_t *b_idx, uint8_t *out,
+                              int64_t *added_cost, void *stream);
+/* nonadd_median_3 (nonaddCSc.c:472-544) per node: final states. */
+int poyd_nonadd8_median_3_batch(const uint8_t *nodes, int64_t stride,
+                                int32_t len, int32_t n, const int32_t *anc,
+                                const int32_t *prelim, const int32_t *d1,
+                                const int32_t *d2, uint8_t *out, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Sankoff characters (SankCS, sankCS.ml:302-377).  k states per character
+ * (k <= 8), nchar characters per node; per-node data int32
+ * [nchar][k] with the sentinel POYD_SANK_INF standing for OCaml's
+ * max_int/4 (saturating arithmetic, sankCS.ml:34-67).  tcm: device
+ * [k][k].
+ * ------------------------------------------------------------------- */
+#define POYD_SANK_INF (1 << 30)
+/* elt_median over all characters for each candidate (a_idx[i], b_idx[i]):
+ * writes s (c), e and beta rows of the median and, when cost != NULL, the
+ * node's median cost sum_char min_s c (SankCS.median + cost). */
+int poyd_sank_median_batch(const int32_t *nodes, int32_t nchar, int32_t k,
+                           const int32_t *tcm, int32_t n, const int32_t *a_idx,
+                           const int32_t *b_idx, int32_t *out_s,
+                           int32_t *out_e, int32_t *out_beta, void *stream);
+/* SankCS.distance (sankCS.ml:371-377) per candidate as the integer sum of
+ * per-character (min c - min a.s - min b.s); dist[i] is int64. */
+int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int32_t k,
+                             const int32_t *tcm, int32_t n,
+                             const int32_t *a_idx, const int32_t *b_idx,
+                             int64_t *dist, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

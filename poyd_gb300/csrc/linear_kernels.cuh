@@ -1,0 +1,62 @@
+// Argument blocks and launchers of the linear-gap kernels (linear.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "poyd_internal.h"
+
+namespace poyd {
+
+struct LinPlanArgs {
+  int n;
+  const uint8_t *seq;
+  const int64_t *a_off;
+  const int32_t *a_len;
+  const int64_t *b_off;
+  const int32_t *b_len;
+  int policy;
+  const int32_t *deltaw;
+  int gap;
+  int maxc;
+  int with_dm;
+  int dos_empty;
+  LinPlan *plans;
+  int64_t *dm_words;
+  int32_t *wd_out;
+  int64_t *cells;
+  int32_t *err;
+};
+
+struct LinDpArgs {
+  int n;
+  const uint8_t *seq;
+  const LinPlan *plans;
+  const int64_t *dm_off;
+  const int32_t *order;
+  const DevTables *tables;
+  int gap;
+  int *counter;
+  int *scratch;   // per-warp boundary-row slabs
+  int64_t slab;   // ints per slab
+  uint32_t *dm;
+  int32_t *cost;
+};
+
+struct LinTbArgs {
+  int n;
+  const uint8_t *seq;
+  const LinPlan *plans;
+  const int64_t *dm_off;
+  const uint32_t *dm;
+  const DevTables *tables;
+  int gap;
+  uint8_t *out;
+  const int64_t *out_off;
+  int32_t *out_len;
+};
+
+void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
+int lin_dp_blocks(bool dm);
+void launch_lin_dp(const LinDpArgs &A, bool dm, int blocks, cudaStream_t st);
+void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st);
+
+}  // namespace poyd

@@ -1,0 +1,54 @@
+// Internal declarations shared by the host runtime and the kernels.
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include "poyd_gb300.h"
+
+namespace poyd {
+
+// Record a failure message (poyd_last_error) and return the code.
+int fail(int code, const char *fmt, ...);
+int cuda_fail(int err, const char *what);
+
+// Cells outside the band hold this value; every real DP value must stay
+// below kMaxCost so that kInf plus a cost never collides with one.
+constexpr int kInf = 1 << 25;
+constexpr int kMaxCost = 1 << 24;
+constexpr int kLanes = 32;      // rows per strip = lanes per pair
+constexpr int kStepBlock = 32;  // steps per queue block
+
+// Per-pair plan of the linear banded DP, produced on the device.
+struct LinPlan {
+  int64_t s1_off, s2_off;  // rows (longer) and columns sequences
+  int64_t dm_off;          // 32-bit word offset of the direction matrix
+  int32_t l1, l2;          // rows / columns lengths
+  int32_t dlo, wd;         // band diagonals [dlo, dlo + wd)
+  int32_t swap;            // 1: rows are the caller's b
+  int32_t nstrips;         // ceil(l1 / 32)
+  int32_t sblocks;         // 8-step DM words per lane per strip
+  int32_t deltaw;          // width extension used
+  int32_t empty;           // DOS.median empty rule: 1 = a empty, 2 = b empty
+  int32_t pad_;
+};
+static_assert(sizeof(LinPlan) == 64, "LinPlan layout");
+
+// Packed cost table staged in shared memory: entry (a<<5)+b holds
+// cost[a][b] in the low 16 bits and cost[gap][b] in the high 16 bits.
+struct DevTables {
+  uint32_t packed[1024];
+  uint8_t median[1024];
+  int32_t cost[1024];
+};
+
+struct Workspace;
+Workspace *workspace();  // per current device
+// Grow-only device buffer `slot` of at least `bytes`; returns nullptr on failure.
+void *ws_buffer(Workspace *w, int slot, size_t bytes);
+enum WsSlot {
+  WS_TABLES = 0, WS_PLANS, WS_DMWORDS, WS_WD, WS_ORDER, WS_DM, WS_SCRATCH,
+  WS_COUNTER, WS_CELLS, WS_AFF, WS_ERR, WS_NSLOTS
+};
+
+int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);
+
+}  // namespace poyd

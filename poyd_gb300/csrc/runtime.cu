@@ -1,0 +1,253 @@
+// Host runtime: error reporting, per-device grow-only workspace, cost-table
+// upload, and the batched / single-pair C entry points of the linear and
+// affine DO path.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <vector>
+#include "poyd_internal.h"
+#include "linear_kernels.cuh"
+#include "affine_kernels.cuh"
+
+namespace poyd {
+
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(int err, const char *what) {
+  return fail(POYD_ECUDA, "%s: %s", what, cudaGetErrorString((cudaError_t)err));
+}
+
+#define CK(call)                                          \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+  } while (0)
+
+struct Workspace {
+  void *ptr[WS_NSLOTS] = {};
+  size_t size[WS_NSLOTS] = {};
+  poyd_cm last_cm;
+  bool have_cm = false;
+};
+
+static std::mutex g_ws_mu;
+static Workspace *g_ws[64] = {};
+
+Workspace *workspace() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (!g_ws[dev & 63]) g_ws[dev & 63] = new Workspace();
+  return g_ws[dev & 63];
+}
+
+void *ws_buffer(Workspace *w, int slot, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (w->size[slot] >= bytes) return w->ptr[slot];
+  if (w->ptr[slot]) {
+    cudaDeviceSynchronize();
+    cudaFree(w->ptr[slot]);
+    w->ptr[slot] = nullptr;
+    w->size[slot] = 0;
+  }
+  size_t want = bytes + bytes / 4;
+  void *p = nullptr;
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    want = bytes;
+  }
+  w->ptr[slot] = p;
+  w->size[slot] = want;
+  return p;
+}
+
+// Checks the matrix is one the GPU path implements: the combinations
+// alphabet with lcm 5 and gap 16, tail[x] = cost[x][gap] and
+// prepend[x] = cost[gap][x] (fill_default_prepend_tail, cost_matrix.ml:397-403),
+// which lets the kernels fold the first-row, first-column and last-column
+// special cells (algn.c:548-620) into the ordinary cell rule.
+static int check_cm(const poyd_cm *cm, int *maxc) {
+  if (!cm) return fail(POYD_EINVAL, "null cost matrix");
+  if (cm->lcm != 5 || cm->gap != 16 || !cm->combinations)
+    return fail(POYD_EUNSUP, "only the 5-bit combinations alphabet (DNA with ambiguity codes) is supported");
+  int mx = 0;
+  for (int a = 1; a < 32; ++a) {
+    if (cm->tail[a] != cm->cost[(a << 5) | 16] || cm->prepend[a] != cm->cost[(16 << 5) | a])
+      return fail(POYD_EUNSUP, "tail/prepend costs differ from the gap column/row of the cost table");
+    for (int b = 1; b < 32; ++b) {
+      const int c = cm->cost[(a << 5) | b];
+      if (c < 0) return fail(POYD_ERANGE, "negative transformation cost");
+      mx = std::max(mx, c);
+    }
+  }
+  if (mx >= 65536) return fail(POYD_ERANGE, "transformation costs must be below 65536");
+  if (cm->cost_model == 1 && (cm->gap_open < 0 || cm->gap_open >= 65536))
+    return fail(POYD_ERANGE, "gap opening cost out of range");
+  *maxc = mx;
+  return POYD_OK;
+}
+
+int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream) {
+  Workspace *w = workspace();
+  DevTables *d = (DevTables *)ws_buffer(w, WS_TABLES, sizeof(DevTables));
+  if (!d) return fail(POYD_ENOMEM, "table allocation failed");
+  if (!w->have_cm || std::memcmp(&w->last_cm, cm, sizeof(poyd_cm)) != 0) {
+    static thread_local DevTables h;
+    for (int a = 0; a < 32; ++a)
+      for (int b = 0; b < 32; ++b)
+        h.packed[(a << 5) | b] = (uint32_t)(cm->cost[(a << 5) | b] & 0xffff) |
+                                 ((uint32_t)(cm->cost[(16 << 5) | b] & 0xffff) << 16);
+    std::memcpy(h.median, cm->median, sizeof(h.median));
+    std::memcpy(h.cost, cm->cost, sizeof(h.cost));
+    CK(cudaMemcpyAsync(d, &h, sizeof(DevTables), cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    w->last_cm = *cm;
+    w->have_cm = true;
+  }
+  *dev = d;
+  return POYD_OK;
+}
+
+// Shared driver of poyd_cost_2_batch (want_align = false) and
+// poyd_align_2_batch (want_align = true) for the linear model.
+static int linear_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
+                        const int64_t *a_off, const int32_t *a_len, const int64_t *b_off,
+                        const int32_t *b_len, int32_t policy, const int32_t *deltaw,
+                        int32_t *cost, int64_t *cells, bool want_align, int32_t flags,
+                        uint8_t *out, const int64_t *out_off, int32_t *out_len,
+                        cudaStream_t st) {
+  Workspace *w = workspace();
+  DevTables *tabs = nullptr;
+  int rc = upload_tables(cm, &tabs, st);
+  if (rc) return rc;
+  LinPlan *plans = (LinPlan *)ws_buffer(w, WS_PLANS, sizeof(LinPlan) * (size_t)n);
+  int64_t *dmw = (int64_t *)ws_buffer(w, WS_DMWORDS, sizeof(int64_t) * 2 * (size_t)n);
+  int32_t *wdb = (int32_t *)ws_buffer(w, WS_WD, sizeof(int32_t) * 2 * (size_t)n + 16);
+  int32_t *err = (int32_t *)ws_buffer(w, WS_ERR, 64);
+  if (!plans || !dmw || !wdb || !err) return fail(POYD_ENOMEM, "plan allocation failed");
+  CK(cudaMemsetAsync(err, 0, 4, st));
+  LinPlanArgs PA;
+  PA.n = n; PA.seq = seq; PA.a_off = a_off; PA.a_len = a_len; PA.b_off = b_off; PA.b_len = b_len;
+  PA.policy = policy; PA.deltaw = deltaw; PA.gap = cm->gap; PA.maxc = maxc;
+  PA.with_dm = want_align; PA.dos_empty = (flags & POYD_FLAG_DOS_EMPTY) ? 1 : 0;
+  PA.plans = plans; PA.dm_words = dmw; PA.wd_out = wdb; PA.cells = cells; PA.err = err;
+  launch_lin_plan(PA, st);
+  CK(cudaGetLastError());
+
+  // Host: DM offsets, scratch size, and a longest-first pair order.
+  std::vector<int64_t> hw((size_t)n);
+  std::vector<int32_t> hwd((size_t)n + 1);
+  CK(cudaMemcpyAsync(hw.data(), dmw, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hwd.data(), wdb, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(hwd.data() + n, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
+  if (hwd[n] & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
+  std::vector<int64_t> off((size_t)n);
+  int64_t total = 0;
+  int maxwd = 1;
+  for (int32_t i = 0; i < n; ++i) {
+    off[i] = total;
+    if (want_align) total += hw[i];
+    maxwd = std::max(maxwd, hwd[i]);
+  }
+  std::vector<int32_t> order((size_t)n);
+  std::iota(order.begin(), order.end(), 0);
+  // longest first: dm_words ~ strips * (wd + 62) is the band area
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return hw[x] > hw[y]; });
+  int64_t *doff = dmw + n;
+  int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
+  int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
+  if (!dord || !counter) return fail(POYD_ENOMEM, "order allocation failed");
+  CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dord, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(counter, 0, 4, st));
+  uint32_t *dm = nullptr;
+  if (want_align) {
+    dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)std::max<int64_t>(total, 1));
+    if (!dm) return fail(POYD_ENOMEM, "direction matrix allocation (%lld bytes) failed",
+                         (long long)(total * 4));
+  }
+  const int blocks = lin_dp_blocks(want_align);
+  const int64_t slab = maxwd + 64;
+  int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * 8);
+  if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
+  LinDpArgs DA;
+  DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
+  DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
+  DA.cost = cost;
+  launch_lin_dp(DA, want_align, blocks, st);
+  CK(cudaGetLastError());
+  if (want_align) {
+    LinTbArgs TA;
+    TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
+    TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+    launch_lin_traceback(TA, st);
+    CK(cudaGetLastError());
+  }
+  return POYD_OK;
+}
+
+}  // namespace poyd
+
+using namespace poyd;
+
+extern "C" const char *poyd_last_error(void) { return g_err; }
+extern "C" int poyd_version(void) { return 1; }
+
+extern "C" int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                                 const int64_t *a_off, const int32_t *a_len,
+                                 const int64_t *b_off, const int32_t *b_len,
+                                 int32_t deltaw_policy, const int32_t *deltaw, int32_t *cost,
+                                 int64_t *band_cells, void *stream) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!seq || !a_off || !a_len || !b_off || !b_len || !cost)))
+    return fail(POYD_EINVAL, "poyd_cost_2_batch: null argument");
+  if (deltaw_policy == POYD_DELTAW_EXPLICIT && !deltaw)
+    return fail(POYD_EINVAL, "explicit deltaw policy needs the deltaw array");
+  if (n == 0) return POYD_OK;
+  if (cm->cost_model == 1)
+    return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, false,
+                        0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
+  return linear_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, deltaw_policy, deltaw, cost,
+                      band_cells, false, 0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                                  const int64_t *a_off, const int32_t *a_len,
+                                  const int64_t *b_off, const int32_t *b_len, int32_t *cost,
+                                  uint8_t *out, const int64_t *out_off, int32_t *out_len,
+                                  int64_t *band_cells, int32_t flags, void *stream) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!seq || !a_off || !a_len || !b_off || !b_len || !cost || !out ||
+                          !out_off || !out_len)))
+    return fail(POYD_EINVAL, "poyd_align_2_batch: null argument");
+  if (n == 0) return POYD_OK;
+  if (cm->cost_model == 1)
+    return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, true,
+                        flags, out, out_off, out_len, (cudaStream_t)stream);
+  return linear_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
+                      nullptr, cost, band_cells, true, flags, out, out_off, out_len,
+                      (cudaStream_t)stream);
+}

@@ -1,0 +1,81 @@
+"""Loader for the in-tree CUDA library (``lib/libpoyd_gb300.so``).
+
+The library is the product: there is no CPU fallback.  ``lib()`` raises when
+the library has not been built or cannot be loaded, and every wrapper raises
+``PoydError`` when an entry point returns a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libpoyd_gb300.so")
+
+POYD_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ERANGE", -4: "ENOMEM", -5: "EUNSUP"}
+DELTAW_DEFAULT, DELTAW_EXPLICIT, DELTAW_DOS_DISTANCE = 0, 1, 2
+FLAG_DOS_EMPTY = 1
+SANK_INF = 1 << 30
+
+
+class PoydError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"poyd_gb300 error {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PoydCM(C.Structure):
+    """``poyd_cm`` (include/poyd_gb300.h)."""
+
+    _fields_ = [
+        ("lcm", C.c_int32), ("gap", C.c_int32), ("a_sz", C.c_int32),
+        ("combinations", C.c_int32), ("cost_model", C.c_int32),
+        ("gap_open", C.c_int32), ("is_metric", C.c_int32),
+        ("all_elements", C.c_int32),
+        ("cost", C.c_int32 * 1024), ("worst", C.c_int32 * 1024),
+        ("prepend", C.c_int32 * 32), ("tail", C.c_int32 * 32),
+        ("median", C.c_uint8 * 1024),
+    ]
+
+
+# (name, restype, argtypes) of every exported symbol; tests check that the
+# library exports exactly these.
+_vp, _i32, _i64 = C.c_void_p, C.c_int32, C.c_int64
+_cmp = C.POINTER(PoydCM)
+SIGNATURES = [
+    ("poyd_last_error", C.c_char_p, []),
+    ("poyd_version", C.c_int, []),
+    ("poyd_cm_dna", C.c_int, [_cmp, _i32, _i32, _i32]),
+    ("poyd_cm_of_matrix5", C.c_int, [_cmp, _vp, _i32]),
+    ("poyd_cost_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp]),
+    ("poyd_align_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, _i32, _vp]),
+]
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(the GPU path has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != POYD_OK:
+        msg = lib().poyd_last_error()
+        raise PoydError(rc, msg.decode() if msg else "")

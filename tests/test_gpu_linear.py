@@ -1,0 +1,131 @@
+"""Parity of the CUDA linear-gap path with the oracle (bit-exact)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from poyd_gb300 import align, synth
+
+pytestmark = pytest.mark.gpu
+
+MODELS = [(1, 2), (1, 1), (3, 1), (2, 3)]
+
+
+def _edge_pairs(rng):
+    A, B = [], []
+    g = synth.with_gap
+    cases = [(0, 0), (0, 5), (5, 0), (1, 1), (2, 7), (40, 100), (100, 40), (64, 64),
+             (63, 65), (31, 33), (200, 301), (301, 200), (1, 300), (150, 149), (500, 10)]
+    for n1, n2 in cases:
+        A.append(g(synth.random_dna(rng, n1, 0.1)))
+        B.append(g(synth.random_dna(rng, n2, 0.1)))
+    # all-ambiguous and gap-bearing inputs
+    A.append(g(np.full(120, 15, np.uint8)))
+    B.append(g(synth.random_dna(rng, 118)))
+    a = synth.random_dna(rng, 300)
+    b = a.copy()
+    b[::7] = 16
+    b[5:40] = 16
+    A.append(g(a))
+    B.append(g(b))
+    a = synth.random_dna(rng, 257, 0.05)
+    b = a.copy()
+    b[rng.random(len(b)) < 0.3] = 31
+    A.append(g(a))
+    B.append(g(b))
+    return A, B
+
+
+def _random_pairs(seed, n, lmax):
+    A, B = synth.pair_batch(seed, n, lmin=1, lmax=lmax)
+    rng = np.random.default_rng(seed + 1)
+    for _ in range(n // 4):
+        A.append(synth.with_gap(synth.random_dna(rng, int(rng.integers(1, lmax)), 0.05)))
+        B.append(synth.with_gap(synth.random_dna(rng, int(rng.integers(1, lmax)), 0.05)))
+    return A, B
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_cost_2_matches_oracle(model):
+    rng = np.random.default_rng(5)
+    A, B = _random_pairs(100 + model[0], 60, 900)
+    EA, EB = _edge_pairs(rng)
+    A += EA
+    B += EB
+    cm = align.CostMatrix.dna(*model)
+    om = O.cm_dna(model[0], model[1], -1)
+    batch = align.PairBatch.from_host(A, B)
+    for dw in (None, "dos"):
+        cost, cells = align.cost_2(batch, cm, deltaw=dw, band_cells=True)
+        cost = cost.cpu().numpy()
+        cells = cells.cpu().numpy()
+        for i, (a, b) in enumerate(zip(A, B)):
+            explicit = None if dw is None else max(abs(len(a) - len(b)), 8)
+            assert cost[i] == O.cost_2(a, b, om, explicit), (model, dw, i, len(a), len(b))
+            d = O.deltaw(a, b, om, explicit)
+            assert cells[i] == O.band_cells_linear(len(a), len(b), d)
+
+
+def test_cost_2_explicit_deltaw():
+    A, B = _random_pairs(7, 40, 600)
+    cm = align.CostMatrix.default()
+    om = O.cm_dna(1, 2, -1)
+    rng = np.random.default_rng(0)
+    dws = rng.integers(0, 120, len(A)).astype(np.int32)
+    batch = align.PairBatch.from_host(A, B)
+    cost, _ = align.cost_2(batch, cm, deltaw=torch.from_numpy(dws).cuda())
+    cost = cost.cpu().numpy()
+    for i, (a, b) in enumerate(zip(A, B)):
+        assert cost[i] == O.cost_2(a, b, om, int(dws[i])), i
+
+
+@pytest.mark.parametrize("model", MODELS)
+def test_align_2_medians_match_oracle(model):
+    rng = np.random.default_rng(9)
+    A, B = _random_pairs(200 + model[1], 50, 800)
+    EA, EB = _edge_pairs(rng)
+    A += EA
+    B += EB
+    cm = align.CostMatrix.dna(*model)
+    om = O.cm_dna(model[0], model[1], -1)
+    res = align.align_2(align.PairBatch.from_host(A, B), cm).to_host()
+    for i, (a, b) in enumerate(zip(A, B)):
+        c, ra, rb = O.align_2(a, b, om)
+        r = res[i]
+        assert r["cost"] == c, (i, len(a), len(b))
+        assert np.array_equal(r["a"], ra) and np.array_equal(r["b"], rb), (i, len(a), len(b))
+        assert np.array_equal(r["median_wg"], O.median_2_with_gaps(ra, rb, om)), i
+        assert np.array_equal(r["median"], O.ancestor_2(ra, rb, om)), i
+
+
+def test_dos_median_empty_rule():
+    rng = np.random.default_rng(3)
+    g = synth.with_gap
+    A = [g(np.zeros(0, np.uint8)), g(synth.random_dna(rng, 50)), np.array([16, 16, 16], np.uint8)]
+    B = [g(synth.random_dna(rng, 40)), g(np.zeros(0, np.uint8)), g(synth.random_dna(rng, 30))]
+    cm = align.CostMatrix.default()
+    om = O.cm_dna(1, 2, -1)
+    res = align.align_2(align.PairBatch.from_host(A, B), cm, dos_empty=True).to_host()
+    for i, (a, b) in enumerate(zip(A, B)):
+        c, med, ra, rb, wg = O.dos_median(a, b, om)
+        assert res[i]["cost"] == c
+        assert np.array_equal(res[i]["median"], med)
+
+
+def test_full_size_properties():
+    """Config-sized lengths (up to 5,000) through size-independent checks:
+    the aligned pair re-scores to the DP cost (verify_2) and drops back to
+    the inputs when gaps are removed."""
+    A, B = synth.pair_batch(77, 48, lmin=3000, lmax=5000)
+    cm = align.CostMatrix.default()
+    om = O.cm_dna(1, 2, -1)
+    res = align.align_2(align.PairBatch.from_host(A, B), cm).to_host()
+    for i, (a, b) in enumerate(zip(A, B)):
+        r = res[i]
+        assert O.verify_2(r["a"], r["b"], om) == r["cost"]
+        assert np.array_equal(r["a"][r["a"] != 16], a[a != 16])
+        assert np.array_equal(r["b"][r["b"] != 16], b[b != 16])
+    # and full oracle parity on a sample
+    for i in range(0, 48, 12):
+        c, ra, rb = O.align_2(A[i], B[i], om)
+        assert res[i]["cost"] == c and np.array_equal(res[i]["a"], ra)
