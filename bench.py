@@ -1,0 +1,346 @@
+"""Benchmark: batched direct-optimization align_2 (DOS.median pieces) GCUPS.
+
+Workload (one "step"): 65,536 independent DNA pairs, L1 ~ U[100, 5000], each
+partner carrying 10-30 % substitutions and 2-5 % indels (geometric length,
+mean 2), 5 % of positions IUPAC ambiguity masks; TCM substitution 1 / indel 2
+(Cost_matrix.Two_D.default).  Per pair the step runs cost_2 (default deltaw,
+the ``align_2`` path), backtrack_2d, ancestor_2 and median_2_with_gaps on the
+device.  The unit is a DP cell the reference's band evaluates (counted per
+pair by the plan kernel, mirroring algn.c:872-968); GCUPS = cells / s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is device throughput with inputs resident in HBM; ``e2e`` is the
+same metric through the public API with pinned host buffers, the input
+upload and the full result download inside the timed region.  N > 1 runs one
+replica per GPU (the pairs are independent; no collective).  ``--impl
+reference`` times the CPU restatement of the reference (oracle/) on all host
+cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "align_2 GCUPS (bit-exact)"
+UNIT = "GCUPS"
+OPS_PER_CELL = {"linear": 8, "affine": 24}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--pairs", type=int, default=65536)
+    p.add_argument("--model", default="linear", choices=["linear", "affine"])
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--cpu-sample-s", type=float, default=12.0)
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(args):
+    return {
+        "workload": "batched DNA align_2 + ancestor_2 + median_2_with_gaps (DOS.median)",
+        "pairs": args.pairs, "len_range": [100, 5000], "sub": [0.10, 0.30],
+        "indel": [0.02, 0.05], "ambiguity": 0.05,
+        "tcm": "sub 1 / indel 2" + (" / gap_opening 3" if args.model == "affine" else ""),
+        "model": args.model, "seed": args.seed,
+        "l2_policy": "inputs larger than L2 (sequences ~330 MB, direction matrix tens of GB); no flush",
+        "parallelism": "replicas" if args.gpus > 1 else "single",
+    }
+
+
+def cm_for(args, align_mod):
+    if args.model == "affine":
+        return align_mod.CostMatrix.dna(1, 2, 3)
+    return align_mod.CostMatrix.default()
+
+
+def oracle_cm(args, O):
+    return O.cm_dna(1, 2, 3 if args.model == "affine" else -1)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_time_sample(host, idx, cm_o, threads):
+    """Runs the oracle's DOS.median on pairs idx over `threads` host threads;
+    returns (seconds, band cells)."""
+    from oracle import oracle as O
+    L = O.lib()
+    seq, ao, al, bo, bl = host
+    chunks = np.array_split(np.asarray(idx, np.int32), threads)
+    cells = [0] * threads
+
+    def work(t):
+        ch = np.ascontiguousarray(chunks[t])
+        cost = np.zeros(len(ch), np.int32)
+        cells[t] = L.or_dos_median_many(seq.ctypes.data, ao.ctypes.data, al.ctypes.data,
+                                        bo.ctypes.data, bl.ctypes.data, ch.ctypes.data,
+                                        len(ch), cm_o, cost.ctypes.data)
+
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    return time.perf_counter() - t0, int(sum(cells))
+
+
+def cpu_sample_indices(host, budget_s, threads, cm_o, seed):
+    """Picks a random sample of pairs whose CPU time is about budget_s."""
+    rng = np.random.default_rng(seed)
+    n = len(host[2])
+    perm = rng.permutation(n).astype(np.int32)
+    probe = perm[:max(threads * 2, 32)]
+    dt, cells = cpu_time_sample(host, probe, cm_o, threads)
+    per_pair = dt / len(probe)
+    k = int(min(n, max(len(probe), budget_s / max(per_pair, 1e-9))))
+    return perm[:k]
+
+
+def run_reference(args):
+    """CPU arm: the oracle's restatement of the reference on all host cores."""
+    import ctypes as C
+    from oracle import oracle as O
+    from poyd_gb300 import synth
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    O.build()
+    host = synth.pair_batch_fast(args.seed, args.pairs)
+    cm_o = oracle_cm(args, O)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_sample_s / 2)
+    idx = cpu_sample_indices(host, per_step, threads, C.byref(cm_o), args.seed)
+    for _ in range(args.warmup):
+        cpu_time_sample(host, idx[:max(threads, len(idx) // 8)], C.byref(cm_o), threads)
+    tot_t, tot_c = 0.0, 0
+    for s in range(args.steps):
+        dt, cells = cpu_time_sample(host, idx, C.byref(cm_o), threads)
+        tot_t += dt
+        tot_c += cells
+    v = tot_c / tot_t / 1e9
+    sample = "%d of %d pairs per step (random, seeded), DOS.median pieces" % (len(idx), args.pairs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot_t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from poyd_gb300 import align, native, synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    host = synth.pair_batch_fast(args.seed + rank, args.pairs)
+    pinned = [torch.from_numpy(x).pin_memory() for x in host]
+    batch = align.PairBatch.from_packed(pinned, device=dev)
+    cm = cm_for(args, align)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (also sizes the workspace)
+    res = None
+    for _ in range(args.warmup):
+        res = align.align_2(batch, cm, band_cells=True)
+    torch.cuda.synchronize()
+    cells = int(res.band_cells.sum().item())
+    full_cells = int((batch.a_len.to(torch.int64) * batch.b_len.to(torch.int64)).sum().item())
+
+    # ---- device-resident timed region ----
+    native.lib().poyd_profile_enable(1)
+    native.profile_read(clear=True)
+    launches0 = native.lib().poyd_launch_count()
+    barrier()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            res = align.align_2(batch, cm)
+        e1.record(st)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = native.lib().poyd_launch_count() - launches0
+    kname = "lin_dp_dm" if args.model == "linear" else "aff_dp_dm"
+    dp_ms, dp_n = native.profile_read(kname, clear=False)
+    all_ms, all_n = native.profile_read(None, clear=True)
+    native.lib().poyd_profile_enable(0)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = cells * world / (ms_max * 1e-3) / 1e9
+
+    # ---- end-to-end through the public API with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        h2d = sum(int(x.numel() * x.element_size()) for x in pinned)
+
+        def e2e_step(out_host):
+            b = align.PairBatch.from_packed(pinned, device=dev, non_blocking=True)
+            r = align.align_2(b, cm)
+            if out_host is None:
+                out_host = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+                            for x in (r.cost, r.out, r.out_len)]
+            for dst, src in zip(out_host, (r.cost, r.out, r.out_len)):
+                dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            return out_host
+
+        out_host = e2e_step(None)  # untimed: allocates the pinned result buffers
+        barrier()
+        t0 = time.perf_counter()
+        n_e2e = max(1, args.steps // 2)
+        for _ in range(n_e2e):
+            out_host = e2e_step(out_host)
+        dt = (time.perf_counter() - t0) / n_e2e
+        d2h = sum(int(x.numel() * x.element_size()) for x in out_host)
+        tt = torch.tensor([dt], device=dev)
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": cells * world / float(tt.item()) / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    if rank == 0:
+        peak_gops = native.int32_peak()
+        dp_launch_ms = dp_ms / max(dp_n, 1)
+        achieved = cells / (dp_launch_ms * 1e-3) * OPS_PER_CELL[args.model] / 1e9
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            try:
+                traffic = json.load(open(prof)).get(kname)
+            except Exception:
+                traffic = None
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic (seeded generator, poyd_gb300/synth.py)",
+            "config": dict(workload_config(args), band_cells_per_step=cells,
+                           full_matrix_cells_per_step=full_cells),
+            "gpu_launches": int(launches),
+            "kernel_ms_per_step": {"dp": dp_ms / args.steps, "all": all_ms / args.steps},
+            "roofline": {"bound": "int32", "achieved": achieved, "peak": peak_gops,
+                         "unit": "Gop/s", "frac": achieved / peak_gops if peak_gops else None,
+                         "traffic": traffic, "kernel": kname,
+                         "ops_per_cell": OPS_PER_CELL[args.model],
+                         "peak_source": "measured (poyd_int32_peak microbenchmark)"},
+            "clocks": clk.summary(),
+            "e2e": e2e,
+        }
+        # CPU baseline: the oracle port on a bounded sample, all host threads
+        try:
+            import ctypes as C
+            from oracle import oracle as O
+            O.build()
+            cm_o = oracle_cm(args, O)
+            threads = os.cpu_count() or 1
+            idx = cpu_sample_indices(host, args.cpu_sample_s, threads, C.byref(cm_o),
+                                     args.seed)
+            dt, c = cpu_time_sample(host, idx, C.byref(cm_o), threads)
+            line["cpu_baseline"] = {
+                "value": c / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": "%d of %d pairs (random, seeded), %.1f s" % (len(idx), args.pairs, dt)}
+        except Exception as ex:  # the baseline must not hide the GPU line
+            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -192,6 +192,21 @@ int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int32_t k,
                              const int32_t *a_idx, const int32_t *b_idx,
                              int64_t *dist, void *stream);
 
+/* ---------------------------------------------------------------------
+ * Measurement helpers (no counterpart in the reference, which has no
+ * device).  While profiling is on, every kernel the library launches is
+ * bracketed by CUDA events on its own stream; poyd_profile_read sums the
+ * recorded durations of kernels named `name` (NULL = all) in ms and
+ * returns how many launches matched.  poyd_launch_count counts every
+ * kernel launch since load.  poyd_int32_peak measures the device's
+ * achievable INT32 add+min issue rate (Gop/s), the denominator of the DP
+ * roofline.
+ * ------------------------------------------------------------------- */
+int poyd_profile_enable(int on);
+int poyd_profile_read(const char *name, double *ms_total, int clear);
+long long poyd_launch_count(void);
+int poyd_int32_peak(double *gops, double *ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,10 @@ def lib():
                                         C.POINTER(C.c_int)]
         L.or_dos_median.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), u8p,
                                     C.POINTER(C.c_int), u8p, u8p, u8p, C.POINTER(C.c_int)]
+        L.or_dos_median_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OrCM),
+                                         C.c_void_p]
+        L.or_dos_median_many.restype = C.c_int64
         L.or_nonadd_median.argtypes = [u8p, u8p, C.c_int, u8p]
         L.or_nonadd_median.restype = C.c_int64
         L.or_nonadd_distance.argtypes = [u8p, u8p, C.c_int]

@@ -322,18 +322,25 @@ int or_align_2(const uint8_t *a, int la, const uint8_t *b, int lb,
                const or_cm *m, uint8_t *ra, uint8_t *rb, int *alen) {
     /* sequence.ml:849-869 (first_gap = true), linear model:
      * cost_2 then create_edited_2 (sequence.ml:813-823). */
+    /* One grow-only direction matrix per thread, reused across calls like
+     * the reference's Matrix.default arena (matrices.c:77-120); it is not
+     * cleared between calls. */
+    static __thread uint16_t *dm_arena = NULL;
+    static __thread size_t dm_cap = 0;
+    size_t need = (size_t)la * (size_t)lb;
     int dw = or_cost2_deltaw(a, la, b, lb, m->gap, 0, 0);
     int cost;
+    if (need > dm_cap) {
+        free(dm_arena);
+        dm_arena = (uint16_t *)malloc(sizeof(uint16_t) * need);
+        dm_cap = need;
+    }
     if (la >= lb) {
-        uint16_t *dm = (uint16_t *)malloc(sizeof(uint16_t) * (size_t)la * (size_t)lb);
-        cost = or_simple_2(a, la, b, lb, m, dw, dm);
-        *alen = or_backtrack_2d(a, la, b, lb, dm, m, 1, ra, rb);
-        free(dm);
+        cost = or_simple_2(a, la, b, lb, m, dw, dm_arena);
+        *alen = or_backtrack_2d(a, la, b, lb, dm_arena, m, 1, ra, rb);
     } else {
-        uint16_t *dm = (uint16_t *)malloc(sizeof(uint16_t) * (size_t)la * (size_t)lb);
-        cost = or_simple_2(b, lb, a, la, m, dw, dm);
-        *alen = or_backtrack_2d(b, lb, a, la, dm, m, 0, rb, ra);
-        free(dm);
+        cost = or_simple_2(b, lb, a, la, m, dw, dm_arena);
+        *alen = or_backtrack_2d(b, lb, a, la, dm_arena, m, 0, rb, ra);
     }
     return cost;
 }
@@ -861,4 +868,33 @@ double or_sank_elt_distance(int k, const int64_t *tcm, const int64_t *a_s, const
         double fb = s_isinf(mb) ? __builtin_inf() : (double)mb;
         return fm - fa - fb;
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Batch driver for timing the CPU restatement (bench.py's CPU arms): runs   */
+/* DOS.median's linear pieces (align_2, ancestor_2, median_2_with_gaps) or   */
+/* the affine align_affine_3 on pairs idx[0..n) of a packed batch.           */
+/* ------------------------------------------------------------------------ */
+int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,
+                           const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
+                           int n, const or_cm *m, int32_t *cost) {
+    static __thread uint8_t *buf = NULL;
+    static __thread size_t cap = 0;
+    int64_t cells = 0;
+    int t;
+    for (t = 0; t < n; t++) {
+        int i = idx[t];
+        const uint8_t *a = seq + a_off[i], *b = seq + b_off[i];
+        int la = a_len[i], lb = b_len[i], lm, lal;
+        size_t need = (size_t)(la + lb + 4) * 4;
+        if (need > cap) { free(buf); buf = (uint8_t *)malloc(need); cap = need; }
+        {
+            uint8_t *sm = buf, *ra = buf + (la + lb + 4), *rb = ra + (la + lb + 4), *wg = rb + (la + lb + 4);
+            cost[t] = or_dos_median(a, la, b, lb, m, sm, &lm, ra, rb, wg, &lal);
+        }
+        if (m->cost_model == 1) cells += or_band_cells_affine(la, lb);
+        else cells += or_band_cells_linear(la >= lb ? la : lb, la >= lb ? lb : la,
+                                           or_cost2_deltaw(a, la, b, lb, m->gap, 0, 0));
+    }
+    return cells;
 }

@@ -133,6 +133,12 @@ int or_dos_median(const uint8_t *a, int la, const uint8_t *b, int lb,
                   const or_cm *m, uint8_t *seqm, int *lm, uint8_t *ra,
                   uint8_t *rb, uint8_t *medwg, int *lal);
 
+/* DOS.median on pairs idx[0..n) of a packed batch (CPU timing driver);
+ * returns the total band cells, writes each pair's cost. */
+int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,
+                           const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
+                           int n, const or_cm *m, int32_t *cost);
+
 /* ---- Fitch non-additive characters, 8-bit lanes (nonaddCSc.c) ---- */
 int64_t or_nonadd_median(const uint8_t *a, const uint8_t *b, int len, uint8_t *res);
 int64_t or_nonadd_distance(const uint8_t *a, const uint8_t *b, int len);

@@ -1,12 +1,495 @@
-// Affine-gap DO path (placeholder until the affine kernels land).
+// Affine-gap ("3 matrix", 4-state) banded DO on sm_103a.
+//
+// Restates algn_fill_plane_3_aff_nobt / algn_fill_plane_3_aff
+// (algn.c:2287-2548) with the FILL_* cell rules (algn.c:1740-1977) and
+// ASSIGN_MINIMUM (algn.c:2251-2280), initialize_matrices_affine[_nobt]
+// (algn.c:2124-2248) and backtrace_affine (algn.c:1983-2097), as run by
+// algn_CAML_cost_affine_3 / algn_CAML_align_affine_3 (algn.c:2551-2680):
+// rows are the shorter sequence si, columns the longer sj.
+//
+// The band of row i is columns [max(1, i-39), min(e0+i-1, lenj)] with a
+// vertical boundary cell just left of it and, while the band has not
+// reached lenj, a HIGH_NUM boundary cell just right of it.  In diagonal
+// coordinates d = j - i that is d in [-40, e0] for every row, so one warp
+// sweeps it exactly like the linear kernel: lane k owns row 32*strip+k and
+// handles diagonal d at step d + 40 + 2k.  The four states (EH, EV, EB, CB)
+// of row i-1 at column j arrive from lane k-1 by shuffles, with the column
+// characters (sj[j], sj[j-1]); lane 0 reads the previous strip's last row
+// from a per-warp global slab of 16-byte records.  The bt variant packs the
+// bits backtrace_affine reads into one byte per cell (4 cells per word).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <numeric>
+#include <vector>
 #include "affine_kernels.cuh"
 
 namespace poyd {
 
-int affine_batch(const poyd_cm *, int, int32_t, const uint8_t *, const int64_t *,
-                 const int32_t *, const int64_t *, const int32_t *, int32_t *, int64_t *, bool,
-                 int32_t, uint8_t *, const int64_t *, int32_t *, cudaStream_t) {
-  return fail(POYD_EUNSUP, "affine cost model not implemented on the GPU path yet");
+namespace {
+
+constexpr unsigned kFullA = 0xffffffffu;
+constexpr int kHigh = 1000000;  // HIGH_NUM (algn.c:38)
+constexpr int kStart = 40;      // start_v (algn.c:2291)
+constexpr int kDlo = -40;
+
+// One-byte direction code: bits 0-1 the m_todo choice (0 H, 1 A, 2 V, 3 D:
+// DO_HORIZONTAL > DO_ALIGN > DO_VERTICAL > DO_DIAGONAL, algn.c:2005-2012),
+// bit 2 END_VERTICAL, bit 3 END_HORIZONTAL, bit 4 END_BLOCK, bits 5-6 the
+// m_align choice (0 H, 1 D, 2 V, 3 none: ALIGN_TO_HORIZONTAL >
+// ALIGN_TO_DIAGONAL > ALIGN_TO_VERTICAL, algn.c:2049-2051).
+constexpr uint32_t kCodeLeft = 2u | 4u | (3u << 5);   // DO_VERTICAL | END_VERTICAL
+constexpr uint32_t kCodeRight = 0u | 8u | (3u << 5);  // DO_HORIZONTAL | END_HORIZONTAL
+
+struct AffPlan {
+  int64_t si_off, sj_off;
+  int32_t leni, lenj;  // rows 0..leni (si), columns 0..lenj (sj)
+  int32_t e0, wd;
+  int32_t swap;        // 1: rows are the caller's b
+  int32_t nstrips, sblocks;  // sblocks: 4-step DM words per lane per strip
+  int32_t empty;
+  int32_t pad_[4];
+};
+static_assert(sizeof(AffPlan) == 64, "AffPlan layout");
+
+struct AffPlanArgs {
+  int n;
+  const uint8_t *seq;
+  const int64_t *a_off;
+  const int32_t *a_len;
+  const int64_t *b_off;
+  const int32_t *b_len;
+  int gap;
+  int dos_empty;
+  long long maxc;
+  AffPlan *plans;
+  int64_t *dm_words;
+  int32_t *wd_out;
+  int64_t *cells;
+  int32_t *err;
+};
+
+struct AffDpArgs {
+  int n;
+  const uint8_t *seq;
+  const AffPlan *plans;
+  const int64_t *dm_off;
+  const int32_t *order;
+  const DevTables *tables;
+  int go;
+  int *counter;
+  int4 *scratch;
+  int64_t slab;
+  uint32_t *dm;
+  int32_t *cost;
+};
+
+struct AffTbArgs {
+  int n;
+  const uint8_t *seq;
+  const AffPlan *plans;
+  const int64_t *dm_off;
+  const uint32_t *dm;
+  const DevTables *tables;
+  uint8_t *out;
+  const int64_t *out_off;
+  int32_t *out_len;
+};
+
+__global__ void k_aff_plan(AffPlanArgs A) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= A.n) return;
+  const int la = A.a_len[id], lb = A.b_len[id];
+  const int64_t ao = A.a_off[id], bo = A.b_off[id];
+  const int swap = la > lb;  // rows = shorter (algn.c:2595-2617)
+  const int li = swap ? lb : la, lj = swap ? la : lb;
+  const int leni = li - 1, lenj = lj - 1;
+  int e0 = (lenj - leni) + 8;
+  if (e0 < 40) e0 = 40;
+  if (e0 > lenj) e0 = lenj;
+  AffPlan P;
+  P.si_off = swap ? bo : ao;
+  P.sj_off = swap ? ao : bo;
+  P.leni = leni; P.lenj = lenj; P.e0 = e0;
+  P.wd = e0 - kDlo + 1;
+  P.swap = swap;
+  P.nstrips = (leni + 1 + 31) / 32;
+  const int S = P.wd + 62;
+  const int Spad = (S + 31) / 32 * 32;
+  P.sblocks = Spad / 4;
+  P.empty = 0;
+  if (A.dos_empty) {
+    bool ea = true, eb = true;
+    for (int x = 0; x < la && ea; ++x) ea = A.seq[ao + x] == A.gap;
+    for (int x = 0; x < lb && eb; ++x) eb = A.seq[bo + x] == A.gap;
+    P.empty = ea ? 1 : (eb ? 2 : 0);
+  }
+  for (int t = 0; t < 4; ++t) P.pad_[t] = 0;
+  A.plans[id] = P;
+  A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * 32;
+  A.wd_out[id] = P.wd;
+  if (A.cells) {
+    long long c = lenj + 1;
+    for (int i = 1; i <= leni; ++i) {
+      const int s = i > kStart ? i - kStart + 1 : 1;
+      int e = e0 + i - 1;
+      if (e > lenj) e = lenj;
+      c += e - s + 1;
+    }
+    A.cells[id] = c;
+  }
+  if (la < 1 || lb < 1) atomicOr(A.err, 1);
+  // real costs must stay clear of the HIGH_NUM sentinel arithmetic
+  if (A.maxc * (long long)(la + lb + 2) >= (1 << 22)) atomicOr(A.err, 2);
+}
+
+template <bool BT>
+__device__ __forceinline__ void aff_pair(const AffDpArgs &A, const uint32_t *tab,
+                                         const AffPlan &P, int64_t dm_off, int id, int4 *bnd,
+                                         int lane) {
+  const uint8_t *si = A.seq + P.si_off;
+  const uint8_t *sj = A.seq + P.sj_off;
+  const int leni = P.leni, lenj = P.lenj, e0 = P.e0, wd = P.wd, go = A.go;
+  const int Spad = P.sblocks * 4;
+  int result = 0;
+  uint32_t *dm = BT ? A.dm + dm_off : nullptr;
+
+  for (int strip = 0; strip < P.nstrips; ++strip) {
+    const int r0 = strip * 32;
+    const int i = r0 + lane;
+    const bool rowok = i <= leni;
+    const int ic = rowok ? si[i] : 0;
+    const int ip = (rowok && i > 0) ? si[i - 1] : 0;
+    const int si_ext = (int)(tab[(ic << 5) | 16] & 0xffffu);
+    const int si_open = (!(ip & 16) && (ic & 16)) ? 0 : go;
+    const int si_ng = ic & 15;
+    const int si_vext = (i > 1 && (ip & 16) && !(ic & 16)) ? si_open + si_ext : si_ext;
+    const int d_lb = (-i > kDlo) ? -i : kDlo;
+    const bool has_rb = e0 <= lenj - i;
+    const int s_fin = (i == leni) ? (lenj - leni) - kDlo + 2 * lane : -1;
+    const uint32_t *srow = tab + (si_ng << 5);
+
+    int eh_l = kHigh, cb_l = kHigh;
+    int eh_d = kHigh, ev_d = kHigh, eb_d = kHigh, cb_d = kHigh;
+    int m_eh = kHigh, m_ev = kHigh, m_eb = kHigh, m_cb = kHigh, m_col = 0;
+    if (lane == 0 && strip > 0) {
+      const int4 v = bnd[0];
+      eh_d = v.x; ev_d = v.y; eb_d = v.z; cb_d = v.w;
+    }
+    int4 nxt = (strip > 0) ? bnd[1 < wd ? 1 : 0] : make_int4(kHigh, kHigh, kHigh, kHigh);
+    uint32_t word = 0;
+    for (int s = 0; s < Spad; ++s) {
+      int u_eh = __shfl_up_sync(kFullA, m_eh, 1);
+      int u_ev = __shfl_up_sync(kFullA, m_ev, 1);
+      int u_eb = __shfl_up_sync(kFullA, m_eb, 1);
+      int u_cb = __shfl_up_sync(kFullA, m_cb, 1);
+      int col = __shfl_up_sync(kFullA, m_col, 1);
+      const int d = kDlo + s - 2 * lane;
+      const int j = i + d;
+      if (lane == 0) {
+        u_eh = nxt.x; u_ev = nxt.y; u_eb = nxt.z; u_cb = nxt.w;
+        const int x = s + 2;
+        nxt = (strip > 0 && x < wd) ? bnd[x] : make_int4(kHigh, kHigh, kHigh, kHigh);
+        const int jc = (j >= 0 && j <= lenj) ? sj[j] : 0;
+        const int jp = (j >= 1 && j <= lenj + 1) ? sj[j - 1] : 0;
+        col = jc | (jp << 5);
+      }
+      const int jc = col & 31, jp = (col >> 5) & 31;
+      // column quantities (algn.c:2321-2328 / 2451-2457)
+      const int sj_ext = (int)(tab[jc] >> 16);  // prepend[jc] = cost[gap][jc]
+      const int sj_open = (!(jp & 16) && (jc & 16)) ? 0 : go;
+      const int hext = (j == 1) ? sj_ext : (((jp & 16) && !(jc & 16)) ? sj_open + sj_ext : sj_ext);
+      // FILL_EXTEND_HORIZONTAL
+      const int e1 = eh_l + hext, e2 = cb_l + sj_open + sj_ext;
+      int eh = e1 < e2 ? e1 : e2;
+      // FILL_EXTEND_VERTICAL
+      const int v1 = u_ev + si_vext, v2 = u_cb + si_open + si_ext;
+      int ev = v1 < v2 ? v1 : v2;
+      // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]
+      const bool both = (ic & 16) && (jc & 16);
+      const int dg = both ? 0 : kHigh;
+      const int od = BT ? dg : (both ? ((!(ip & 16) && !(jc & 16)) ? 0 : 2 * go) : kHigh);
+      const int b1 = eb_d + dg, b2 = cb_d + od;
+      int eb = b1 < b2 ? b1 : b2;
+      // FILL_CLOSE_BLOCK_DIAGONAL
+      const int cdiag = (int)(srow[jc & 15] & 0xffffu);
+      const int extra = sj_open < si_open ? si_open : sj_open;
+      const int fa = cb_d + cdiag;
+      const int fv = ev_d + cdiag + ((ic & 16) ? sj_open : 0);
+      const int fh = eh_d + cdiag + ((jc & 16) ? si_open : 0);
+      const int fd = eb_d + cdiag + extra;
+      int cb = fa;
+      uint32_t amask = 1;  // ALIGN_TO_ALIGN
+      if (cb >= fv) { if (cb > fv) { cb = fv; amask = 2; } else amask |= 2; }
+      if (cb >= fh) { if (cb > fh) { cb = fh; amask = 4; } else amask |= 4; }
+      if (cb >= fd) { if (cb > fd) { cb = fd; amask = 8; } else amask |= 8; }
+      // ASSIGN_MINIMUM
+      int f = eh;
+      uint32_t dmask = 4;  // DO_HORIZONTAL
+      if (f >= ev) { if (f > ev) { f = ev; dmask = 2; } else dmask |= 2; }
+      if (f >= eb) { if (f > eb) { f = eb; dmask = 8; } else dmask |= 8; }
+      if (f >= cb) { if (f > cb) { f = cb; dmask = 1; } else dmask |= 1; }
+      uint32_t code = 0;
+      if (BT) {
+        // dmask bits: 1 ALIGN, 2 VERTICAL, 4 HORIZONTAL, 8 DIAGONAL
+        const uint32_t todo = (dmask & 4) ? 0u : (dmask & 1) ? 1u : (dmask & 2) ? 2u : 3u;
+        const uint32_t achoice = (amask & 4) ? 0u : (amask & 8) ? 1u : (amask & 2) ? 2u : 3u;
+        code = todo | (v1 < v2 ? 0u : 4u) | (e1 < e2 ? 0u : 8u) | (b1 < b2 ? 0u : 16u) |
+               (achoice << 5);
+      }
+      if (i == 0) {  // initialize_matrices_affine row 0
+        if (j == 0) { eh = go; ev = go; eb = 0; cb = 0; f = 0; }
+        else { eh = eh_l + sj_ext; cb = eh; eb = kHigh; ev = kHigh; f = eh; }
+      } else if (d == d_lb) {  // vertical boundary cell left of the band
+        eh = kHigh; cb = kHigh; eb = kHigh; ev = u_ev + si_vext; f = ev;
+        code = kCodeLeft;
+      } else if (has_rb && d == e0) {  // HIGH_NUM cell right of the band
+        eh = kHigh; ev = kHigh; eb = kHigh; cb = kHigh;
+        code = kCodeRight;
+      }
+      if (s == s_fin) result = f;
+      if (BT) {
+        word = (word << 8) | code;
+        if ((s & 3) == 3) dm[((int64_t)strip * P.sblocks + (s >> 2)) * 32 + lane] = word;
+      }
+      m_eh = eh; m_ev = ev; m_eb = eb; m_cb = cb; m_col = col;
+      if (lane == 31) {
+        const int x = s - 62;
+        if (x >= 0 && x < wd) bnd[x] = make_int4(eh, ev, eb, cb);
+      }
+      eh_d = u_eh; ev_d = u_ev; eb_d = u_eb; cb_d = u_cb;
+      eh_l = eh; cb_l = cb;
+    }
+    __syncwarp();
+  }
+  result = __shfl_sync(kFullA, result, leni & 31);
+  if (lane == 0) A.cost[id] = result;
+}
+
+template <bool BT>
+__global__ void __launch_bounds__(256) k_aff_dp(AffDpArgs A) {
+  __shared__ uint32_t tab[1024];
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) tab[t] = A.tables->packed[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int4 *bnd = A.scratch + gw * A.slab;
+  for (;;) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(A.counter, 1);
+    p = __shfl_sync(kFullA, p, 0);
+    if (p >= A.n) break;
+    const int id = A.order ? A.order[p] : p;
+    const AffPlan P = A.plans[id];
+    if (P.empty) {
+      if (lane == 0) A.cost[id] = 0;
+      continue;
+    }
+    aff_pair<BT>(A, tab, P, BT ? A.dm_off[id] : 0, id, bnd, lane);
+  }
+}
+
+__device__ __forceinline__ void pre(uint8_t *buf, int64_t cap, int64_t &n, int v) {
+  if (n < cap) buf[cap - 1 - n] = (uint8_t)v;
+  ++n;
+}
+
+__global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
+  __shared__ uint8_t med[1024];
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) med[t] = A.tables->median[t];
+  __syncthreads();
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= A.n) return;
+  const AffPlan P = A.plans[id];
+  const int li = P.leni + 1, lj = P.lenj + 1;
+  const int la = P.swap ? lj : li, lb = P.swap ? li : lj;
+  const int64_t cap = (int64_t)la + lb + 2;
+  uint8_t *oa = A.out + A.out_off[id];
+  uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
+  const uint8_t *si = A.seq + P.si_off, *sj = A.seq + P.sj_off;
+  if (P.empty) {
+    const bool a_empty = P.empty == 1;
+    const uint8_t *src = (a_empty != (bool)P.swap) ? sj : si;
+    const int len = a_empty ? lb : la;
+    for (int t = 0; t < len; ++t) om[cap - len + t] = src[t];
+    A.out_len[2 * id] = 0;
+    A.out_len[2 * id + 1] = len;
+    return;
+  }
+  // resi / resj of backtrace_affine in caller order
+  uint8_t *ri = P.swap ? ob : oa, *rj = P.swap ? oa : ob;
+  const uint32_t *dm = A.dm + A.dm_off[id];
+  const int sb = P.sblocks, e0 = P.e0, lenj = P.lenj;
+  int i = P.leni, j = P.lenj;
+  int ic = si[i], jc = sj[j];
+  int64_t nr = 0, nw = 0, nm = 0;
+  int mode = 0;  // 0 todo, 1 vertical, 2 horizontal, 3 diagonal, 4 align
+  bool bad = false;
+  while (i != 0 && j != 0) {
+    const int d = j - i;
+    const int d_lb = (-i > kDlo) ? -i : kDlo;
+    if (d < d_lb || d > e0 || (d == e0 && !(e0 <= lenj - i))) { bad = true; break; }
+    const int k = i & 31, strip = i >> 5;
+    const int s = d - kDlo + 2 * k;
+    const uint32_t w = dm[((int64_t)strip * sb + (s >> 2)) * 32 + k];
+    const uint32_t c = (w >> (8 * (3 - (s & 3)))) & 0xffu;
+    if (mode == 0) {
+      const uint32_t t = c & 3u;
+      mode = t == 0 ? 2 : t == 1 ? 4 : t == 2 ? 1 : 3;
+    } else if (mode == 1) {
+      if (c & 4u) mode = 0;
+      if (!(ic & 16)) { pre(om, cap, nm, ic | 16); pre(ow, cap, nw, ic | 16); }
+      else pre(ow, cap, nw, 16);
+      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, 16);
+      --i; ic = si[i];
+    } else if (mode == 2) {
+      if (c & 8u) mode = 0;
+      if (!(jc & 16)) { pre(om, cap, nm, jc | 16); pre(ow, cap, nw, jc | 16); }
+      else pre(ow, cap, nw, 16);
+      pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, jc);
+      --j; jc = sj[j];
+    } else if (mode == 3) {
+      if (c & 16u) mode = 0;
+      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, jc);
+      pre(ow, cap, nw, 16);
+      --i; --j; jc = sj[j]; ic = si[i];
+    } else {
+      const uint32_t a = (c >> 5) & 3u;
+      if (a == 0) mode = 2;
+      else if (a == 1) mode = 3;
+      else if (a == 2) mode = 1;
+      const int m = med[((ic & 15) << 5) | (jc & 15)];
+      pre(om, cap, nm, m); pre(ow, cap, nw, m);
+      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, jc);
+      --i; --j; jc = sj[j]; ic = si[i];
+    }
+    if (nr + 4 >= cap) { bad = true; break; }
+  }
+  while (!bad && i != 0) {
+    if (!(ic & 16)) { pre(om, cap, nm, ic | 16); pre(ow, cap, nw, ic | 16); }
+    else pre(ow, cap, nw, 16);
+    pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, 16);
+    --i; ic = si[i];
+  }
+  while (!bad && j != 0) {
+    if (!(jc & 16)) { pre(om, cap, nm, jc | 16); pre(ow, cap, nw, jc | 16); }
+    else pre(ow, cap, nw, 16);
+    pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, jc);
+    --j; jc = sj[j];
+  }
+  pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, 16);
+  pre(ow, cap, nw, 16);
+  // an empty median has no position 0 in the reference; treated as not a gap
+  if (nm == 0 || om[cap - nm] != 16) pre(om, cap, nm, 16);
+  A.out_len[2 * id] = bad ? -1 : (int32_t)nr;
+  A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
+}
+
+int aff_blocks(bool bt) {
+  static int cache[2][64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int &c = cache[bt ? 1 : 0][dev & 63];
+  if (!c) {
+    int per_sm = 0, sms = 0;
+    if (bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<false>, 256, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  }
+  return c;
+}
+
+#define CKA(call)                                         \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+  } while (0)
+
+}  // namespace
+
+int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
+                 const int64_t *a_off, const int32_t *a_len, const int64_t *b_off,
+                 const int32_t *b_len, int32_t *cost, int64_t *cells, bool want_align,
+                 int32_t flags, uint8_t *out, const int64_t *out_off, int32_t *out_len,
+                 cudaStream_t st) {
+  Workspace *w = workspace();
+  DevTables *tabs = nullptr;
+  int rc = upload_tables(cm, &tabs, st);
+  if (rc) return rc;
+  AffPlan *plans = (AffPlan *)ws_buffer(w, WS_AFF, sizeof(AffPlan) * (size_t)n);
+  int64_t *dmw = (int64_t *)ws_buffer(w, WS_DMWORDS, sizeof(int64_t) * 2 * (size_t)n);
+  int32_t *wdb = (int32_t *)ws_buffer(w, WS_WD, sizeof(int32_t) * 2 * (size_t)n + 16);
+  int32_t *err = (int32_t *)ws_buffer(w, WS_ERR, 64);
+  if (!plans || !dmw || !wdb || !err) return fail(POYD_ENOMEM, "plan allocation failed");
+  CKA(cudaMemsetAsync(err, 0, 4, st));
+  AffPlanArgs PA;
+  PA.n = n; PA.seq = seq; PA.a_off = a_off; PA.a_len = a_len; PA.b_off = b_off;
+  PA.b_len = b_len; PA.gap = cm->gap; PA.dos_empty = (flags & POYD_FLAG_DOS_EMPTY) ? 1 : 0;
+  PA.maxc = std::max(maxc, cm->gap_open);
+  PA.plans = plans; PA.dm_words = dmw; PA.wd_out = wdb; PA.cells = cells; PA.err = err;
+  {
+    ProfScope ps("aff_plan", st);
+    k_aff_plan<<<(n + 127) / 128, 128, 0, st>>>(PA);
+  }
+  CKA(cudaGetLastError());
+  std::vector<int64_t> hw((size_t)n);
+  std::vector<int32_t> hwd((size_t)n + 1);
+  CKA(cudaMemcpyAsync(hw.data(), dmw, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CKA(cudaMemcpyAsync(hwd.data(), wdb, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CKA(cudaMemcpyAsync(hwd.data() + n, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CKA(cudaStreamSynchronize(st));
+  if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
+  if (hwd[n] & 2) return fail(POYD_ERANGE, "affine costs could reach the HIGH_NUM sentinel range");
+  std::vector<int64_t> off((size_t)n);
+  int64_t total = 0;
+  int maxwd = 1;
+  for (int32_t t = 0; t < n; ++t) {
+    off[t] = total;
+    if (want_align) total += hw[t];
+    maxwd = std::max(maxwd, hwd[t]);
+  }
+  std::vector<int32_t> order((size_t)n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return hw[x] > hw[y]; });
+  int64_t *doff = dmw + n;
+  int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
+  int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
+  if (!dord || !counter) return fail(POYD_ENOMEM, "order allocation failed");
+  CKA(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+  CKA(cudaMemcpyAsync(dord, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+  CKA(cudaMemsetAsync(counter, 0, 4, st));
+  uint32_t *dm = nullptr;
+  if (want_align) {
+    dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)std::max<int64_t>(total, 1));
+    if (!dm) return fail(POYD_ENOMEM, "affine direction matrix allocation failed");
+  }
+  const int blocks = aff_blocks(want_align);
+  const int64_t slab = maxwd + 8;
+  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH, sizeof(int4) * (size_t)slab * (size_t)blocks * 8);
+  if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
+  AffDpArgs DA;
+  DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
+  DA.go = cm->gap_open; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
+  DA.cost = cost;
+  {
+    ProfScope ps(want_align ? "aff_dp_dm" : "aff_dp_cost", st);
+    if (want_align) k_aff_dp<true><<<blocks, 256, 0, st>>>(DA);
+    else k_aff_dp<false><<<blocks, 256, 0, st>>>(DA);
+  }
+  CKA(cudaGetLastError());
+  if (want_align) {
+    AffTbArgs TA;
+    TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
+    TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+    {
+      ProfScope ps("aff_traceback", st);
+      k_aff_traceback<<<(n + 127) / 128, 128, 0, st>>>(TA);
+    }
+    CKA(cudaGetLastError());
+  }
+  return POYD_OK;
 }
 
 }  // namespace poyd

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <cstddef>
+#include <cuda_runtime.h>
 #include "poyd_gb300.h"
 
 namespace poyd {
@@ -50,5 +51,15 @@ enum WsSlot {
 };
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);
+
+// Launch accounting (profile.cu): bracket one kernel launch on `st`.
+void prof_begin(const char *name, cudaStream_t st, void **token);
+void prof_end(void *token, cudaStream_t st);
+struct ProfScope {
+  void *tok;
+  cudaStream_t st;
+  ProfScope(const char *name, cudaStream_t s) : st(s) { prof_begin(name, s, &tok); }
+  ~ProfScope() { prof_end(tok, st); }
+};
 
 }  // namespace poyd

@@ -147,7 +147,7 @@ static int linear_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *s
   PA.policy = policy; PA.deltaw = deltaw; PA.gap = cm->gap; PA.maxc = maxc;
   PA.with_dm = want_align; PA.dos_empty = (flags & POYD_FLAG_DOS_EMPTY) ? 1 : 0;
   PA.plans = plans; PA.dm_words = dmw; PA.wd_out = wdb; PA.cells = cells; PA.err = err;
-  launch_lin_plan(PA, st);
+  { ProfScope ps("lin_plan", st); launch_lin_plan(PA, st); }
   CK(cudaGetLastError());
 
   // Host: DM offsets, scratch size, and a longest-first pair order.
@@ -193,13 +193,13 @@ static int linear_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *s
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
   DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
   DA.cost = cost;
-  launch_lin_dp(DA, want_align, blocks, st);
+  { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, want_align, blocks, st); }
   CK(cudaGetLastError());
   if (want_align) {
     LinTbArgs TA;
     TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
     TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
-    launch_lin_traceback(TA, st);
+    { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
     CK(cudaGetLastError());
   }
   return POYD_OK;

@@ -51,7 +51,25 @@ SIGNATURES = [
     ("poyd_cost_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp]),
     ("poyd_align_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _i32, _vp]),
+    ("poyd_profile_enable", C.c_int, [C.c_int]),
+    ("poyd_profile_read", C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int]),
+    ("poyd_launch_count", C.c_longlong, []),
+    ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
+
+
+def profile_read(name=None, clear=True):
+    """(total ms, launches) of recorded kernels named `name` (None = all)."""
+    ms = C.c_double()
+    n = lib().poyd_profile_read(name.encode() if name else None, C.byref(ms), 1 if clear else 0)
+    return ms.value, n
+
+
+def int32_peak():
+    """Measured INT32 add+min issue rate in Gop/s."""
+    g, ms = C.c_double(), C.c_double()
+    check(lib().poyd_int32_peak(C.byref(g), C.byref(ms)))
+    return g.value
 
 _lib = None
 
