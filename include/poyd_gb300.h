@@ -79,6 +79,7 @@ int poyd_cm_of_matrix5(poyd_cm *m, const int32_t *mat25, int32_t gap_open);
 #define POYD_DELTAW_DEFAULT 0 /* cost_2 without ?deltaw (align_2, median) */
 #define POYD_DELTAW_EXPLICIT 1 /* cost_2 ~deltaw:deltaw[i] */
 #define POYD_DELTAW_DOS_DISTANCE 2 /* DOS.distance: max(|la-lb|, 8) (seqCS.ml:856-866) */
+#define POYD_DELTAW_RAW 3 /* deltaw[i] is algn_CAML_simple_2's deltawh as is */
 
 /* Batched Sequence.Align.cost_2 (sequence.ml:716-723): for each pair the
  * linear banded cost algn_CAML_simple_2 (algn.c:3409-3427) with the deltaw

@@ -502,9 +502,10 @@ static int aff_e0(int leni, int lenj) {
 
 int64_t or_band_cells_affine(int li, int lj) {
     int leni = li - 1, lenj = lj - 1;
-    int64_t n = lenj + 1;
+    int64_t n;
     int i, e0;
     if (leni > lenj) { int t = leni; leni = lenj; lenj = t; }
+    n = lenj + 1; /* row 0 of the rows = shorter orientation */
     e0 = aff_e0(leni, lenj);
     for (i = 1; i <= leni; i++) {
         int s = i > AFF_START_V ? i - AFF_START_V + 1 : 1;

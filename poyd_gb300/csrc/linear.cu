@@ -65,7 +65,9 @@ __global__ void k_lin_plan(LinPlanArgs A) {
   const int dif = l1 - l2;
   const int lower = (int)((double)l1 * 0.10);
   int dwc;
-  if (A.policy == POYD_DELTAW_DEFAULT) {
+  if (A.policy == POYD_DELTAW_RAW) {
+    dwc = A.deltaw[id] - gaps;  // deltawh passed straight to algn_nw
+  } else if (A.policy == POYD_DELTAW_DEFAULT) {
     dwc = (dif < lower) ? lower / 2 : 2;
   } else {
     int v = (A.policy == POYD_DELTAW_EXPLICIT) ? A.deltaw[id] : (dif > 8 ? dif : 8);
@@ -260,7 +262,9 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
   }
   const uint32_t *dm = A.dm + A.dm_off[id];
   const int L2 = P.l2, dlo = P.dlo, sb = P.sblocks;
-  const bool swaped = !P.swap;  // backtrack priority (algn.c:3605-3666)
+  // backtrack priority (algn.c:3605-3666): the caller's first argument is
+  // the rows sequence unless the pair was swapped
+  const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
   int r = P.l1 - 1, j = L2 - 1;
   int64_t n = 0, nm = 0;
   const int spad = sb * 8;

@@ -52,6 +52,7 @@ struct LinTbArgs {
   uint8_t *out;
   const int64_t *out_off;
   int32_t *out_len;
+  int swaped;  // -1: derive from the orientation, else backtrack_2d's flag
 };
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);

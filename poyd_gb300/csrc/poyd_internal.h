@@ -47,10 +47,11 @@ Workspace *workspace();  // per current device
 void *ws_buffer(Workspace *w, int slot, size_t bytes);
 enum WsSlot {
   WS_TABLES = 0, WS_PLANS, WS_DMWORDS, WS_WD, WS_ORDER, WS_DM, WS_SCRATCH,
-  WS_COUNTER, WS_CELLS, WS_AFF, WS_ERR, WS_NSLOTS
+  WS_COUNTER, WS_CELLS, WS_AFF, WS_ERR, WS_SEQ, WS_META, WS_OUT, WS_NSLOTS
 };
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);
+int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *stream);
 
 // Launch accounting (profile.cu): bracket one kernel launch on `st`.
 void prof_begin(const char *name, cudaStream_t st, void **token);

@@ -104,7 +104,10 @@ static int check_cm(const poyd_cm *cm, int *maxc) {
 }
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream) {
-  Workspace *w = workspace();
+  return upload_tables_ws(workspace(), cm, dev, stream);
+}
+
+int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *stream) {
   DevTables *d = (DevTables *)ws_buffer(w, WS_TABLES, sizeof(DevTables));
   if (!d) return fail(POYD_ENOMEM, "table allocation failed");
   if (!w->have_cm || std::memcmp(&w->last_cm, cm, sizeof(poyd_cm)) != 0) {
@@ -126,15 +129,14 @@ int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream) {
 
 // Shared driver of poyd_cost_2_batch (want_align = false) and
 // poyd_align_2_batch (want_align = true) for the linear model.
-static int linear_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
+static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
                         const int64_t *a_off, const int32_t *a_len, const int64_t *b_off,
                         const int32_t *b_len, int32_t policy, const int32_t *deltaw,
                         int32_t *cost, int64_t *cells, bool want_align, int32_t flags,
                         uint8_t *out, const int64_t *out_off, int32_t *out_len,
                         cudaStream_t st) {
-  Workspace *w = workspace();
   DevTables *tabs = nullptr;
-  int rc = upload_tables(cm, &tabs, st);
+  int rc = upload_tables_ws(w, cm, &tabs, st);
   if (rc) return rc;
   LinPlan *plans = (LinPlan *)ws_buffer(w, WS_PLANS, sizeof(LinPlan) * (size_t)n);
   int64_t *dmw = (int64_t *)ws_buffer(w, WS_DMWORDS, sizeof(int64_t) * 2 * (size_t)n);
@@ -195,10 +197,11 @@ static int linear_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *s
   DA.cost = cost;
   { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, want_align, blocks, st); }
   CK(cudaGetLastError());
-  if (want_align) {
+  if (want_align && out) {  // out == nullptr: keep the DM for a later backtrack
     LinTbArgs TA;
     TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
     TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+    TA.swaped = -1;
     { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
     CK(cudaGetLastError());
   }
@@ -228,7 +231,7 @@ extern "C" int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *se
   if (cm->cost_model == 1)
     return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, false,
                         0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
-  return linear_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, deltaw_policy, deltaw, cost,
+  return linear_batch(workspace(), cm, maxc, n, seq, a_off, a_len, b_off, b_len, deltaw_policy, deltaw, cost,
                       band_cells, false, 0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
 }
 
@@ -247,7 +250,197 @@ extern "C" int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *s
   if (cm->cost_model == 1)
     return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, true,
                         flags, out, out_off, out_len, (cudaStream_t)stream);
-  return linear_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
+  return linear_batch(workspace(), cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
                       nullptr, cost, band_cells, true, flags, out, out_off, out_len,
                       (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Single-pair drop-ins.  A poyd_matrix owns its own workspace so that the
+// direction matrix of algn_CAML_simple_2 survives until the matching
+// algn_CAML_backtrack_2d, as Matrix.m does (algn.c:3908-3924).
+// ---------------------------------------------------------------------------
+struct poyd_matrix {
+  Workspace ws;
+  int32_t l1 = -1, l2 = -1;  // pair whose DM is held
+  cudaStream_t st = nullptr;
+};
+
+extern "C" poyd_matrix *poyd_matrix_create(void) { return new poyd_matrix(); }
+
+extern "C" void poyd_matrix_free(poyd_matrix *m) {
+  if (!m) return;
+  for (int s = 0; s < WS_NSLOTS; ++s)
+    if (m->ws.ptr[s]) cudaFree(m->ws.ptr[s]);
+  delete m;
+}
+
+// Copies one pair (a, b) to the device and lays out its batch-of-one
+// metadata: seq, a_off, a_len, b_off, b_len, deltaw, cost.
+struct OnePair {
+  uint8_t *seq;
+  int64_t *off;
+  int32_t *len;
+  int32_t *dw;
+  int32_t *cost;
+};
+
+static int stage_pair(Workspace *w, const uint8_t *a, int32_t la, const uint8_t *b, int32_t lb,
+                      int32_t deltaw, OnePair *P, cudaStream_t st) {
+  uint8_t *seq = (uint8_t *)ws_buffer(w, WS_SEQ, (size_t)la + lb + 64);
+  unsigned char *meta = (unsigned char *)ws_buffer(w, WS_META, 256);
+  if (!seq || !meta) return fail(POYD_ENOMEM, "pair staging allocation failed");
+  struct {
+    int64_t off[2];
+    int32_t len[2];
+    int32_t dw;
+    int32_t cost;
+  } h = {{0, la}, {la, lb}, deltaw, 0};
+  CK(cudaMemcpyAsync(seq, a, (size_t)la, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(seq + la, b, (size_t)lb, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(meta, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  P->seq = seq;
+  P->off = (int64_t *)meta;
+  P->len = (int32_t *)(meta + 16);
+  P->dw = (int32_t *)(meta + 24);
+  P->cost = (int32_t *)(meta + 28);
+  return POYD_OK;
+}
+
+extern "C" int poyd_algn_simple_2(const uint8_t *s1, int32_t l1, const uint8_t *s2, int32_t l2,
+                                  const poyd_cm *cm, poyd_matrix *mat, int32_t deltawh,
+                                  int32_t *cost) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (!s1 || !s2 || !mat || !cost) return fail(POYD_EINVAL, "poyd_algn_simple_2: null argument");
+  if (l2 < 1 || l1 < l2) return fail(POYD_EINVAL, "algn_CAML_simple_2 needs len(s1) >= len(s2) >= 1");
+  if (cm->cost_model != 0) return fail(POYD_EINVAL, "algn_CAML_simple_2 is the linear model");
+  OnePair P;
+  rc = stage_pair(&mat->ws, s1, l1, s2, l2, deltawh, &P, mat->st);
+  if (rc) return rc;
+  // want_align without an output buffer: DP + direction matrix, kept in mat
+  rc = linear_batch(&mat->ws, cm, maxc, 1, P.seq, P.off, P.len, P.off + 1, P.len + 1,
+                    POYD_DELTAW_RAW, P.dw, P.cost, nullptr, true, 0, nullptr, nullptr, nullptr,
+                    mat->st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(cost, P.cost, sizeof(int32_t), cudaMemcpyDeviceToHost, mat->st));
+  CK(cudaStreamSynchronize(mat->st));
+  mat->l1 = l1;
+  mat->l2 = l2;
+  return POYD_OK;
+}
+
+extern "C" int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8_t *s2,
+                                      int32_t l2, uint8_t *s1p, uint8_t *s2p, int32_t cap,
+                                      int32_t *len, poyd_matrix *mat, const poyd_cm *cm,
+                                      int32_t swaped) {
+  (void)s1;
+  (void)s2;
+  if (!mat || !s1p || !s2p || !len || !cm) return fail(POYD_EINVAL, "poyd_algn_backtrack_2d: null argument");
+  if (mat->l1 != l1 || mat->l2 != l2)
+    return fail(POYD_EINVAL, "backtrack_2d needs the direction matrix of the preceding simple_2 on this pair");
+  Workspace *w = &mat->ws;
+  DevTables *tabs = nullptr;
+  int rc = upload_tables_ws(w, cm, &tabs, mat->st);
+  if (rc) return rc;
+  const int64_t slot = (int64_t)l1 + l2 + 2;
+  const size_t tail = ((size_t)4 * slot + 63) & ~(size_t)63;
+  uint8_t *out = (uint8_t *)ws_buffer(w, WS_OUT, tail + 64);
+  if (!out) return fail(POYD_ENOMEM, "backtrack output allocation failed");
+  int32_t *olen = (int32_t *)(out + tail);
+  int64_t *ooff = (int64_t *)(out + tail + 16);
+  const int64_t zero = 0;
+  CK(cudaMemcpyAsync(ooff, &zero, sizeof(zero), cudaMemcpyHostToDevice, mat->st));
+  LinTbArgs TA;
+  TA.n = 1;
+  TA.seq = (const uint8_t *)w->ptr[WS_SEQ];
+  TA.plans = (const LinPlan *)w->ptr[WS_PLANS];
+  TA.dm_off = ((const int64_t *)w->ptr[WS_DMWORDS]) + 1;
+  TA.dm = (const uint32_t *)w->ptr[WS_DM];
+  TA.tables = tabs;
+  TA.gap = cm->gap;
+  TA.out = out;
+  TA.out_off = ooff;
+  TA.out_len = olen;
+  TA.swaped = swaped ? 1 : 0;
+  {
+    ProfScope ps("lin_traceback", mat->st);
+    launch_lin_traceback(TA, mat->st);
+  }
+  CK(cudaGetLastError());
+  int32_t hl[2];
+  CK(cudaMemcpyAsync(hl, olen, sizeof(hl), cudaMemcpyDeviceToHost, mat->st));
+  CK(cudaStreamSynchronize(mat->st));
+  if (hl[0] < 0) return fail(POYD_ERANGE, "traceback left the band");
+  if (hl[0] > cap) return fail(POYD_ERANGE, "output capacity %d below the aligned length %d", cap, hl[0]);
+  CK(cudaMemcpy(s1p + cap - hl[0], out + slot - hl[0], (size_t)hl[0], cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(s2p + cap - hl[0], out + 2 * slot - hl[0], (size_t)hl[0], cudaMemcpyDeviceToHost));
+  *len = hl[0];
+  return POYD_OK;
+}
+
+static int affine_one(const uint8_t *si, int32_t li, const uint8_t *sj, int32_t lj,
+                      const poyd_cm *cm, bool align, uint8_t *resi, uint8_t *resj,
+                      uint8_t *median, uint8_t *medianwg, int32_t cap, int32_t *lens,
+                      int32_t *cost) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (cm->cost_model != 1) return fail(POYD_EINVAL, "the affine entry points need an affine matrix");
+  if (!si || !sj || !cost || li < 1 || lj < 1) return fail(POYD_EINVAL, "affine: bad pair");
+  Workspace *w = workspace();
+  cudaStream_t st = nullptr;
+  OnePair P;
+  rc = stage_pair(w, si, li, sj, lj, 0, &P, st);
+  if (rc) return rc;
+  const int64_t slot = (int64_t)li + lj + 2;
+  uint8_t *out = nullptr;
+  int32_t *olen = nullptr;
+  int64_t *ooff = nullptr;
+  if (align) {
+    if (cap < slot) return fail(POYD_ERANGE, "output capacity below len(si) + len(sj) + 2");
+    const size_t tail = ((size_t)4 * slot + 63) & ~(size_t)63;
+    out = (uint8_t *)ws_buffer(w, WS_OUT, tail + 64);
+    if (!out) return fail(POYD_ENOMEM, "affine output allocation failed");
+    olen = (int32_t *)(out + tail);
+    ooff = (int64_t *)(out + tail + 16);
+    const int64_t zero = 0;
+    CK(cudaMemcpyAsync(ooff, &zero, sizeof(zero), cudaMemcpyHostToDevice, st));
+  }
+  rc = affine_batch(cm, maxc, 1, P.seq, P.off, P.len, P.off + 1, P.len + 1, P.cost, nullptr,
+                    align, 0, out, ooff, olen, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(cost, P.cost, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (!align) return POYD_OK;
+  int32_t hl[2];
+  CK(cudaMemcpy(hl, olen, sizeof(hl), cudaMemcpyDeviceToHost));
+  if (hl[0] < 0) return fail(POYD_ERANGE, "affine traceback left the band");
+  // outputs right-aligned in buffers of capacity cap, like the reference's seq
+  uint8_t *dst[4] = {resi, resj, medianwg, median};
+  const int32_t ln[4] = {hl[0], hl[0], hl[0], hl[1]};
+  for (int k = 0; k < 4; ++k)
+    if (dst[k])
+      CK(cudaMemcpy(dst[k] + cap - ln[k], out + (k + 1) * slot - ln[k], (size_t)ln[k],
+                    cudaMemcpyDeviceToHost));
+  if (lens) {
+    lens[0] = hl[0];
+    lens[1] = hl[1];
+    lens[2] = hl[0];
+  }
+  return POYD_OK;
+}
+
+extern "C" int poyd_algn_cost_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
+                                       int32_t lj, const poyd_cm *cm, int32_t *cost) {
+  return affine_one(si, li, sj, lj, cm, false, nullptr, nullptr, nullptr, nullptr, 0, nullptr,
+                    cost);
+}
+
+extern "C" int poyd_algn_align_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
+                                        int32_t lj, const poyd_cm *cm, uint8_t *resi,
+                                        uint8_t *resj, uint8_t *median, uint8_t *medianwg,
+                                        int32_t cap, int32_t *lens, int32_t *cost) {
+  return affine_one(si, li, sj, lj, cm, true, resi, resj, median, medianwg, cap, lens, cost);
 }

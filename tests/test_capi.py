@@ -1,0 +1,73 @@
+"""The C-ABI library: builds, loads, exports every entry point the public
+header declares, and its cost-matrix constructors match the oracle's
+restatement of cost_matrix.ml.  No GPU needed."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from poyd_gb300 import build, native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "poyd_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(poyd_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.lib()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("model", [(1, 2, -1), (1, 1, -1), (3, 1, -1), (2, 1, 1), (3, 1, 5),
+                                   (1, 2, 3), (1, 1, 0)])
+def test_cost_matrix_matches_oracle(lib, model):
+    m = native.PoydCM()
+    assert lib.poyd_cm_dna(C.byref(m), *model) == 0
+    o = O.cm_dna(*model)
+    for f in ("cost", "worst", "prepend", "tail", "median"):
+        assert np.array_equal(np.ctypeslib.as_array(getattr(m, f)),
+                              np.ctypeslib.as_array(getattr(o, f))), f
+    assert (m.cost_model, m.gap_open, m.is_metric) == (o.cost_model, o.gap_open, o.is_metric)
+
+
+def test_cost_matrix_arbitrary_5x5(lib):
+    rng = np.random.default_rng(3)
+    for t in range(20):
+        mat = rng.integers(0, 6, size=(5, 5)).astype(np.int32)
+        if t % 2 == 0:
+            mat = np.minimum(mat, mat.T)
+            np.fill_diagonal(mat, 0)
+        m = native.PoydCM()
+        assert lib.poyd_cm_of_matrix5(C.byref(m), mat.ctypes.data, -1) == 0
+        o = native.PoydCM()
+        O.lib().or_cm_of_matrix5(C.cast(C.byref(o), C.POINTER(O.OrCM)),
+                                 mat.ctypes.data_as(O.i32p), -1)
+        for f in ("cost", "worst", "median"):
+            assert np.array_equal(np.ctypeslib.as_array(getattr(m, f)),
+                                  np.ctypeslib.as_array(getattr(o, f))), (t, f)
+
+
+def test_errors_are_reported_without_a_gpu(lib):
+    m = native.PoydCM()
+    lib.poyd_cm_dna(C.byref(m), 1, 2, -1)
+    m.lcm = 4  # not the DNA combinations alphabet
+    rc = lib.poyd_cost_2_batch(C.byref(m), 1, None, None, None, None, None, 0, None, None,
+                               None, None)
+    assert rc == -5
+    assert b"alphabet" in lib.poyd_last_error()
