@@ -105,8 +105,8 @@ __global__ void k_lin_plan(LinPlanArgs A) {
     P.l1 = l1; P.l2 = l2;
     P.dlo = dlo; P.wd = wd;
     P.swap = swap;
-    P.nstrips = (l1 + kLanes - 1) / kLanes;
-    const int S = wd + 2 * (kLanes - 1);
+    P.nstrips = (l1 + kRows - 1) / kRows;
+    const int S = wd + kLag * (kLanes - 1) + 1;
     const int Spad = (S + kStepBlock - 1) / kStepBlock * kStepBlock;
     P.sblocks = Spad / 8;
     P.deltaw = dw;
@@ -118,7 +118,7 @@ __global__ void k_lin_plan(LinPlanArgs A) {
     P.pad_ = 0;
     A.plans[id] = P;
     // direction-matrix words; also the work estimate used to order pairs
-    A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * kLanes;
+    A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * kRows;
     A.wd_out[id] = wd;
     if (A.cells) A.cells[id] = cells;
     if (la < 1 || lb < 1) atomicOr(A.err, 1);
@@ -129,8 +129,66 @@ __global__ void k_lin_plan(LinPlanArgs A) {
 // ---------------------------------------------------------------------------
 // Band DP.  DM = true also writes the direction matrix.
 // ---------------------------------------------------------------------------
+struct LinStrip {
+  int HA, HB, diag, Pk, q;
+  uint32_t wA, wB;
+  int result;
+};
+
+// 32 steps of one strip.  Each lane owns two rows: row A = r0 + 2k handles
+// diagonal d at step s = d - dlo + 3k, row B = row A + 1 handles d - 1 in
+// the same step, so row B's delete predecessor is row A's value computed
+// just before and both cells use the same column character.  MASK applies
+// the per-row band/matrix validity (needed only in blocks where some row is
+// outside its band); CAP records the final cell (last strip only).
+template <bool DM, bool MASK, bool CAP>
+__device__ __forceinline__ void lin_block(LinStrip &S, const int2 *trowA, const int2 *trowB,
+                                          int cDA, int cDB, int vbA, int cntA, int vbB, int cntB,
+                                          int finA, int finB, uint2 *dmw, int lane) {
+#pragma unroll
+  for (int u = 0; u < kStepBlock; ++u) {
+    int up = __shfl_up_sync(kFull, S.Pk, 1);
+    if (lane == 0) up = S.q;
+    S.q = __shfl_sync(kFull, S.q, (lane + 1) & 31);
+    const int c = up & 31;
+    const int hup = up >> 5;
+    const int2 TA = trowA[c];  // {cost[a][c], cost[gap][c]}
+    const int2 TB = trowB[c];
+    // row A: delete from the lane above, align from its previous value
+    const int Av = S.diag + TA.x;
+    const int Dv = hup + cDA;
+    const int Iv = S.HA + TA.y;
+    int ha = min(min(Av, Dv), Iv);
+    if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInf;
+    // row B: delete from row A now, align from row A's previous value
+    const int Av2 = S.HA + TB.x;
+    const int Dv2 = ha + cDB;
+    const int Iv2 = S.HB + TB.y;
+    int hb = min(min(Av2, Dv2), Iv2);
+    if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInf;
+    if (DM) {
+      const uint32_t fa = (uint32_t)(Av == ha) | ((uint32_t)(Iv == ha) << 1) |
+                          ((uint32_t)(Dv == ha) << 2);
+      const uint32_t fb = (uint32_t)(Av2 == hb) | ((uint32_t)(Iv2 == hb) << 1) |
+                          ((uint32_t)(Dv2 == hb) << 2);
+      S.wA = (S.wA << 4) | fa;
+      S.wB = (S.wB << 4) | fb;
+      if ((u & 7) == 7) dmw[(u >> 3) * kLanes] = make_uint2(S.wA, S.wB);
+    }
+    if (CAP) {
+      if (u == finA) S.result = ha;
+      if (u == finB) S.result = hb;
+    }
+    S.Pk = (int)(((unsigned)hb << 5) | (unsigned)c);
+    if (lane == 31) S.q = S.Pk;
+    S.diag = hup;
+    S.HA = ha;
+    S.HB = hb;
+  }
+}
+
 template <bool DM>
-__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const uint32_t *tab,
+__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const int2 *tab,
                                          const LinPlan &P, int64_t dm_off, int id,
                                          int *bnd, int lane) {
   const uint8_t *s1 = A.seq + P.s1_off;
@@ -140,28 +198,41 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const uint32_t *tab
 
   for (int x = lane; x < wd; x += 32) bnd[x] = kInf;
   __syncwarp();
-  if (lane == 0) bnd[-dlo] = -(int)(tab[(s1[0] << 5) | s2[0]] & 0xffffu);
+  if (lane == 0) bnd[-dlo] = -tab[(s1[0] << 5) | s2[0]].x;
   __syncwarp();
 
   const int Spad = P.sblocks * 8;
   const int r_last = L1 - 1;
   const int d_last = L2 - L1;
-  int result = 0;
+  LinStrip S;
+  S.result = 0;
   uint32_t *dm = DM ? A.dm + dm_off : nullptr;
 
   for (int strip = 0; strip < P.nstrips; ++strip) {
-    const int r0 = strip * kLanes;
-    const int r = r0 + lane;
-    const bool rowok = r < L1;
-    const int a = rowok ? s1[r] : 0;
-    const uint32_t *trow = tab + (a << 5);
-    const int cD = (int)(tab[(a << 5) | gap] & 0xffffu);
-    const int off = (-dlo - r) > 0 ? (-dlo - r) : 0;
-    const int lower = 2 * lane + off;
-    const int cnt = rowok ? wd - off : 0;
-    const int sfin = (r == r_last) ? (d_last - dlo + 2 * lane) : -1;
-    int H = kInf, diag = kInf;
-    int Pk = (int)((unsigned)kInf << 5);
+    const int r0 = strip * kRows;
+    const int rA = r0 + 2 * lane, rB = rA + 1;
+    const bool okA = rA < L1, okB = rB < L1;
+    const bool last = strip == P.nstrips - 1;
+    const int aA = okA ? s1[rA] : 0, aB = okB ? s1[rB] : 0;
+    const int2 *trowA = tab + (aA << 5), *trowB = tab + (aB << 5);
+    const int cDA = tab[(aA << 5) | gap].x, cDB = tab[(aB << 5) | gap].x;
+    const int offA = (-dlo - rA) > 0 ? (-dlo - rA) : 0;
+    const int offB = (-dlo - rB) > 0 ? (-dlo - rB) : 0;
+    const int lowerA = kLag * lane + offA, lowerB = kLag * lane + 1 + offB;
+    const int cntA = okA ? wd - offA : 0, cntB = okB ? wd - offB : 0;
+    const int sfinA = (rA == r_last) ? (d_last - dlo + kLag * lane) : -1000000;
+    const int sfinB = (rB == r_last) ? (d_last - dlo + kLag * lane + 1) : -1000000;
+    // steps where both rows of every lane are inside their bands
+    const int lo = lowerA > lowerB ? lowerA : lowerB;
+    const int hi = (lowerA + cntA) < (lowerB + cntB) ? (lowerA + cntA) : (lowerB + cntB);
+    const int all_lo = (int)__reduce_max_sync(kFull, (unsigned)lo);
+    const int all_hi = (int)__reduce_min_sync(kFull, (unsigned)hi);
+    S.HA = kInf;
+    S.HB = kInf;
+    S.diag = kInf;
+    S.Pk = (int)((unsigned)kInf << 5);
+    S.wA = 0;
+    S.wB = 0;
     auto qload = [&](int s0) -> int {
       const int x = s0 + lane + 1;
       const int hv = (x < wd) ? bnd[x] : kInf;
@@ -169,52 +240,41 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const uint32_t *tab
       const int c = (j >= 0 && j < L2) ? s2[j] : 0;
       return (int)(((unsigned)hv << 5) | (unsigned)c);
     };
-    int q = qload(0);
-    if (lane == 0) diag = bnd[0];
-    uint32_t word = 0;
+    S.q = qload(0);
+    if (lane == 0) S.diag = bnd[0];
+    uint2 *dmrow = DM ? (uint2 *)(dm + (int64_t)strip * P.sblocks * kRows) + lane : nullptr;
     for (int s0 = 0; s0 < Spad; s0 += kStepBlock) {
       const int qn = (s0 + kStepBlock < Spad) ? qload(s0 + kStepBlock) : 0;
-      const int vb = s0 - lower;
-#pragma unroll
-      for (int u = 0; u < kStepBlock; ++u) {
-        int up = __shfl_up_sync(kFull, Pk, 1);
-        if (lane == 0) up = q;
-        q = __shfl_sync(kFull, q, (lane + 1) & 31);
-        const int c = up & 31;
-        const int hup = up >> 5;
-        const uint32_t T = trow[c];
-        const int Av = diag + (int)(T & 0xffffu);
-        const int Dv = hup + cD;
-        const int Iv = H + (int)(T >> 16);
-        int hn = min(min(Av, Dv), Iv);
-        hn = ((unsigned)(vb + u) < (unsigned)cnt) ? hn : kInf;
-        if (DM) {
-          const uint32_t f = (uint32_t)(Av == hn) | ((uint32_t)(Iv == hn) << 1) |
-                             ((uint32_t)(Dv == hn) << 2);
-          word = (word << 4) | f;
-          if ((u & 7) == 7)
-            dm[((int64_t)strip * P.sblocks + ((s0 + u) >> 3)) * kLanes + lane] = word;
-        }
-        if (s0 + u == sfin) result = hn;
-        Pk = (int)(((unsigned)hn << 5) | (unsigned)c);
-        if (lane == 31) q = Pk;
-        diag = hup;
-        H = hn;
+      uint2 *dmw = DM ? dmrow + (s0 >> 3) * kLanes : nullptr;
+      const int vbA = s0 - lowerA, vbB = s0 - lowerB;
+      if (last) {
+        lin_block<DM, true, true>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
+                                  sfinB - s0, dmw, lane);
+      } else if (s0 >= all_lo && s0 + kStepBlock <= all_hi) {
+        lin_block<DM, false, false>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1, dmw,
+                                    lane);
+      } else {
+        lin_block<DM, true, false>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1, dmw,
+                                   lane);
       }
-      const int x = s0 + lane - 2 * (kLanes - 1);
-      if (x >= 0 && x < wd) bnd[x] = q >> 5;
-      q = qn;
+      const int x = s0 + lane - (kLag * 31 + 1);
+      if (x >= 0 && x < wd) bnd[x] = S.q >> 5;
+      S.q = qn;
     }
     __syncwarp();
   }
-  result = __shfl_sync(kFull, result, r_last & 31);
+  const int src = (r_last % kRows) >> 1;
+  const int result = __shfl_sync(kFull, S.result, src);
   if (lane == 0) A.cost[id] = result;
 }
 
 template <bool DM>
-__global__ void __launch_bounds__(256) k_lin_dp(LinDpArgs A) {
-  __shared__ uint32_t tab[1024];
-  for (int i = threadIdx.x; i < 1024; i += blockDim.x) tab[i] = A.tables->packed[i];
+__global__ void __launch_bounds__(256, 4) k_lin_dp(LinDpArgs A) {
+  __shared__ int2 tab[1024];  // {cost[a][b], cost[gap][b]}
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
+    const uint32_t p = A.tables->packed[i];
+    tab[i] = make_int2((int)(p & 0xffffu), (int)(p >> 16));
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -270,13 +330,13 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
   const int spad = sb * 8;
   bool bad = false;
   while ((int64_t)r * L2 + j >= 0) {
-    const int k = r & 31, strip = r >> 5;
-    const int s = (j - r) - dlo + 2 * k;
+    const int k = (r & (kRows - 1)) >> 1, strip = r / kRows;
+    const int s = (j - r) - dlo + kLag * k + (r & 1);
     if (r < 0 || j < 0 || s < 0 || s >= spad || n + 2 >= cap) {  // left the band: a bug
       bad = true;
       break;
     }
-    const uint32_t w = dm[((int64_t)strip * sb + (s >> 3)) * kLanes + k];
+    const uint32_t w = dm[((int64_t)strip * sb + (s >> 3)) * kRows + (r & (kRows - 1))];
     const uint32_t f = (w >> (4 * (7 - (s & 7)))) & 15u;
     int cr, cc;
     if (f & 1u) { cr = s1[r]; cc = s2[j]; --r; --j; }

@@ -15,7 +15,9 @@ int cuda_fail(int err, const char *what);
 // below kMaxCost so that kInf plus a cost never collides with one.
 constexpr int kInf = 1 << 25;
 constexpr int kMaxCost = 1 << 24;
-constexpr int kLanes = 32;      // rows per strip = lanes per pair
+constexpr int kLanes = 32;      // lanes per pair
+constexpr int kRows = 64;       // rows per strip: two per lane
+constexpr int kLag = 3;         // steps between consecutive lanes
 constexpr int kStepBlock = 32;  // steps per queue block
 
 // Per-pair plan of the linear banded DP, produced on the device.
