@@ -1,0 +1,426 @@
+"""Candidate-pass driver: Wagner build and SPR passes whose every candidate
+join is scored in one batch on the device.
+
+This is the caller side of the hot path (SURVEY 8(f) "search-loop
+integration").  The reference evaluates one candidate per call from
+``single_spr_round`` (ptree.ml:1120-1176) and ``make_wagner_tree``
+(ptree.ml:941-1030) through ``AllDirChar.cost_fn`` -> ``Node.distance``
+(node.ml:914-947); here the candidates of a whole pass are collected and
+scored together, per character type:
+
+* DO sequences: ``DOS.distance`` (cost_2 with deltaw = max(|la-lb|, 8),
+  seqCS.ml:819-867) and ``DOS.median`` (seqCS.ml:747-776) for the downpass;
+* non-additive characters: ``NonaddCS8.distance`` / ``median``
+  (nonaddCS.ml:119-130);
+* Sankoff characters: ``SankCS.distance`` / ``median`` (sankCS.ml:340-377).
+
+The tree is rooted (POY diagnoses from a handle); a node's data is its
+downpass (preliminary) median.  A candidate join of subtree ``s`` on the
+edge above node ``e`` is scored by the distance between s's data and e's
+data -- the quantity ``cost_fn`` adds for a join -- and the exact tree cost
+after a join is recomputed by a full batched downpass, which alone decides
+acceptance.  Batching a pass changes which improving tree is found first
+(the reference accepts sequentially), not the cost of any tree.
+
+Backends: :class:`GpuBackend` runs the CUDA kernels; the oracle backend in
+tests/ implements the same interface on the CPU restatement, so a search
+driven through either yields identical trees, costs and node medians.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import align, native
+from .simulate import Dataset
+
+
+# ---------------------------------------------------------------------------
+# Tree
+# ---------------------------------------------------------------------------
+class Tree:
+    """Rooted binary tree over leaves 0..n-1; internal ids from n upward."""
+
+    def __init__(self, n_leaves: int):
+        self.n = n_leaves
+        cap = 2 * n_leaves
+        self.parent = -np.ones(cap, dtype=np.int64)
+        self.kids = -np.ones((cap, 2), dtype=np.int64)
+        self.root = -1
+        self.free = list(range(2 * n_leaves - 2, n_leaves - 1, -1))
+        self.in_tree = np.zeros(cap, dtype=bool)
+
+    def copy(self) -> "Tree":
+        t = Tree.__new__(Tree)
+        t.n = self.n
+        t.parent = self.parent.copy()
+        t.kids = self.kids.copy()
+        t.root = self.root
+        t.free = list(self.free)
+        t.in_tree = self.in_tree.copy()
+        return t
+
+    def _new_internal(self) -> int:
+        return self.free.pop()
+
+    def start(self, a: int, b: int):
+        w = self._new_internal()
+        self.kids[w] = (a, b)
+        self.parent[a] = self.parent[b] = w
+        self.parent[w] = -1
+        self.root = w
+        self.in_tree[[a, b, w]] = True
+
+    def insert(self, t: int, e: int, w: int | None = None) -> int:
+        """Join node t on the edge above e through a new internal node w."""
+        if w is None:
+            w = self._new_internal()
+        p = self.parent[e]
+        self.kids[w] = (e, t)
+        self.parent[w] = p
+        self.parent[e] = w
+        self.parent[t] = w
+        if p < 0:
+            self.root = w
+        else:
+            k = self.kids[p]
+            k[0 if k[0] == e else 1] = w
+        self.in_tree[[t, w]] = True
+        return w
+
+    def prune(self, s: int) -> int:
+        """Detach the subtree under s; returns its freed parent node."""
+        p = self.parent[s]
+        assert p >= 0, "cannot prune the root"
+        o = self.kids[p][0] if self.kids[p][1] == s else self.kids[p][1]
+        g = self.parent[p]
+        self.parent[o] = g
+        if g < 0:
+            self.root = o
+        else:
+            k = self.kids[g]
+            k[0 if k[0] == p else 1] = o
+        self.parent[p] = -1
+        self.parent[s] = -1
+        self.kids[p] = (-1, -1)
+        self.in_tree[p] = False
+        return p
+
+    def nodes(self):
+        out, stack = [], [self.root]
+        while stack:
+            v = stack.pop()
+            out.append(v)
+            if v >= self.n:
+                stack.extend(self.kids[v])
+        return out
+
+    def subtree(self, s: int):
+        out, stack = [], [s]
+        while stack:
+            v = stack.pop()
+            out.append(v)
+            if v >= self.n:
+                stack.extend(self.kids[v])
+        return out
+
+    def levels(self):
+        """Internal nodes grouped by height (all children before parents)."""
+        h = {}
+        order = self.nodes()[::-1]
+        for v in order:
+            h[v] = 0 if v < self.n else 1 + max(h[self.kids[v][0]], h[self.kids[v][1]])
+        groups = {}
+        for v in order:
+            if v >= self.n:
+                groups.setdefault(h[v], []).append(v)
+        return [sorted(groups[k]) for k in sorted(groups)]
+
+    def newick(self, names=None) -> str:
+        def rec(v):
+            if v < self.n:
+                return names[v] if names else str(v)
+            a, b = self.kids[v]
+            return "(%s,%s)" % (rec(a), rec(b))
+        return rec(self.root) + ";"
+
+
+# ---------------------------------------------------------------------------
+# GPU backend
+# ---------------------------------------------------------------------------
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class GpuBackend:
+    """Node data resident in HBM: DO medians in a byte pool, Fitch rows,
+    Sankoff cost vectors; every batch is a few kernel launches."""
+
+    def __init__(self, data: Dataset, cm: align.CostMatrix, device="cuda"):
+        self.dev = torch.device(device)
+        self.cm = cm
+        self.n = data.n_taxa
+        n_nodes = 2 * self.n
+        self.nf = data.fitch.shape[1]
+        self.stride = max(16, (self.nf + 15) // 16 * 16)
+        self.ns, self.k = data.sank.shape[1], data.sank.shape[2]
+        fit = np.zeros((n_nodes, self.stride), np.uint8)
+        fit[:self.n, :self.nf] = data.fitch
+        self.fitch = torch.from_numpy(fit).to(self.dev)
+        sk = np.zeros((n_nodes, max(self.ns, 1), self.k), np.int32)
+        sk[:self.n, :self.ns] = data.sank
+        self.sank = torch.from_numpy(sk).to(self.dev)
+        self.tcm = torch.from_numpy(np.ascontiguousarray(data.sank_tcm, np.int32)).to(self.dev)
+        total = sum(len(s) for s in data.seqs)
+        self.pool = torch.zeros(max(1 << 20, 16 * total), dtype=torch.uint8, device=self.dev)
+        self.off = np.zeros(n_nodes, np.int64)
+        self.len = np.zeros(n_nodes, np.int32)
+        self.top = 0
+        for v, s in enumerate(data.seqs):
+            self._put(v, torch.from_numpy(np.asarray(s, np.uint8)).to(self.dev))
+        self.stats = {"median_pairs": 0, "distance_pairs": 0, "do_cells": 0}
+
+    # -- sequence pool -------------------------------------------------------
+    def _reserve(self, nbytes: int) -> int:
+        if self.top + nbytes > self.pool.numel():
+            self._compact(extra=nbytes)
+        o = self.top
+        self.top += nbytes
+        return o
+
+    def _compact(self, extra: int = 0):
+        live = [v for v in range(len(self.len)) if self.len[v] > 0]
+        need = sum(int(self.len[v]) for v in live) + extra
+        newpool = torch.zeros(max(2 * need, self.pool.numel()), dtype=torch.uint8, device=self.dev)
+        top = 0
+        for v in live:
+            o, l = int(self.off[v]), int(self.len[v])
+            newpool[top:top + l] = self.pool[o:o + l]
+            self.off[v] = top
+            top += l
+        self.pool, self.top = newpool, top
+
+    def _put(self, v: int, seq: torch.Tensor):
+        o = self._reserve(seq.numel())
+        self.pool[o:o + seq.numel()] = seq
+        self.off[v], self.len[v] = o, seq.numel()
+
+    def _batch(self, a, b) -> align.PairBatch:
+        t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x, dt)).to(self.dev)
+        return align.PairBatch(self.pool, t(self.off[a], np.int64), t(self.len[a], np.int32),
+                               t(self.off[b], np.int64), t(self.len[b], np.int32))
+
+    # -- batched operations -------------------------------------------------
+    def medians(self, a: np.ndarray, b: np.ndarray, out: np.ndarray):
+        """Downpass medians of (a_i, b_i) into nodes out_i; returns the DO
+        and Fitch costs of each median (numpy int64)."""
+        n = len(a)
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L = native.lib()
+        ia = torch.from_numpy(np.asarray(a, np.int32)).to(self.dev)
+        ib = torch.from_numpy(np.asarray(b, np.int32)).to(self.dev)
+        res = align.align_2(self._batch(a, b), self.cm, dos_empty=True)
+        tmp_f = torch.empty((n, self.stride), dtype=torch.uint8, device=self.dev)
+        added = torch.zeros(n, dtype=torch.int64, device=self.dev)
+        if self.nf:
+            native.check(L.poyd_nonadd8_median_batch(_p(self.fitch), C.c_int64(self.stride), self.nf,
+                                                     n, _p(ia), _p(ib), _p(tmp_f), _p(added), st))
+        if self.ns:
+            tmp_s = torch.empty((n, self.ns, self.k), dtype=torch.int32, device=self.dev)
+            native.check(L.poyd_sank_median_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
+                                                  _p(ia), _p(ib), _p(tmp_s), None, None, st))
+        # move the medians into the pool
+        ln = res.out_len.view(-1, 2)[:, 1].to(torch.int64)
+        lens = ln.cpu().numpy()
+        if lens.min() < 0:
+            raise native.PoydError(-3, "median traceback failed")
+        src = res.out_off + 4 * res.cap - ln
+        dst_off = np.array([self._reserve(int(x)) for x in lens], np.int64)
+        total = int(lens.sum())
+        seg = torch.repeat_interleave(torch.arange(n, device=self.dev), ln)
+        starts = torch.cumsum(ln, 0) - ln
+        pos = torch.arange(total, device=self.dev) - starts[seg]
+        dst = torch.from_numpy(dst_off).to(self.dev)
+        self.pool[dst[seg] + pos] = res.out[src[seg] + pos]
+        self.off[out], self.len[out] = dst_off, lens.astype(np.int32)
+        oi = torch.from_numpy(np.asarray(out, np.int64)).to(self.dev)
+        if self.nf:
+            self.fitch[oi] = tmp_f
+        if self.ns:
+            self.sank[oi] = tmp_s
+        self.stats["median_pairs"] += n
+        return res.cost.cpu().numpy().astype(np.int64), added.cpu().numpy()
+
+    def distances(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        """Candidate-join distance d(a_i, b_i) = DOS.distance + Fitch + Sankoff."""
+        n = len(a)
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L = native.lib()
+        ia = torch.from_numpy(np.asarray(a, np.int32)).to(self.dev)
+        ib = torch.from_numpy(np.asarray(b, np.int32)).to(self.dev)
+        do, cells = align.cost_2(self._batch(a, b), self.cm, deltaw="dos", band_cells=True)
+        tot = do.to(torch.int64)
+        if self.nf:
+            fd = torch.empty(n, dtype=torch.int64, device=self.dev)
+            native.check(L.poyd_nonadd8_distance_batch(_p(self.fitch), C.c_int64(self.stride), self.nf,
+                                                       n, _p(ia), _p(ib), _p(fd), st))
+            tot = tot + fd
+        if self.ns:
+            sd = torch.empty(n, dtype=torch.int64, device=self.dev)
+            native.check(L.poyd_sank_distance_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
+                                                    _p(ia), _p(ib), _p(sd), st))
+            tot = tot + sd
+        self.stats["distance_pairs"] += n
+        self.stats["do_cells"] += int(cells.sum().item())
+        return tot.cpu().numpy()
+
+    def sank_cost(self, v: int) -> int:
+        if not self.ns:
+            return 0
+        s = self.sank[v]
+        return int(torch.clamp(s.min(dim=1).values, max=native.SANK_INF).to(torch.int64).sum().item())
+
+    def node_seq(self, v: int) -> np.ndarray:
+        o, l = int(self.off[v]), int(self.len[v])
+        return self.pool[o:o + l].cpu().numpy()
+
+    def node_fitch(self, v: int) -> np.ndarray:
+        return self.fitch[v, :self.nf].cpu().numpy()
+
+    def node_sank(self, v: int) -> np.ndarray:
+        return self.sank[v, :self.ns].cpu().numpy()
+
+
+# ---------------------------------------------------------------------------
+# Diagnosis and search
+# ---------------------------------------------------------------------------
+@dataclass
+class Diagnosis:
+    do_cost: dict = field(default_factory=dict)
+    fitch_cost: dict = field(default_factory=dict)
+    total: int = 0
+
+
+def downpass(tree: Tree, be, nodes=None) -> Diagnosis:
+    """Preliminary medians of every internal node, one batch per height."""
+    d = Diagnosis()
+    for level in tree.levels():
+        lv = np.array(level, np.int64)
+        a = tree.kids[lv, 0]
+        b = tree.kids[lv, 1]
+        do, fi = be.medians(a, b, lv)
+        for i, v in enumerate(level):
+            d.do_cost[v] = int(do[i])
+            d.fitch_cost[v] = int(fi[i])
+    d.total = sum(d.do_cost.values()) + sum(d.fitch_cost.values()) + be.sank_cost(tree.root)
+    return d
+
+
+def wagner(n: int, be, order=None, log=None):
+    """make_wagner_tree (ptree.ml:941-1030): add taxa one at a time at the
+    edge whose join distance is smallest (ties: lowest node id)."""
+    order = list(range(n)) if order is None else list(order)
+    t = Tree(n)
+    t.start(order[0], order[1])
+    downpass(t, be)
+    for x in order[2:]:
+        cand = np.array(sorted(t.nodes()), np.int64)
+        d = be.distances(np.full(len(cand), x, np.int64), cand)
+        if log is not None:
+            log.append((x, cand, d))
+        e = int(cand[int(np.argmin(d))])
+        t.insert(x, e)
+        downpass(t, be)
+    return t, downpass(t, be)
+
+
+@dataclass
+class PassStats:
+    candidates: int = 0
+    moves_tried: int = 0
+    moves_accepted: int = 0
+    cost_before: int = 0
+    cost_after: int = 0
+    seconds_scoring: float = 0.0
+    seconds_total: float = 0.0
+
+
+def spr_candidates(t: Tree):
+    """Every (pruned subtree s, join edge e) of one SPR pass: s ranges over
+    non-root nodes whose parent is not the root, e over the nodes left after
+    pruning s, except s's old sibling (the unchanged tree)."""
+    S, E = [], []
+    all_nodes = t.nodes()
+    for s in all_nodes:
+        p = t.parent[s]
+        if p < 0 or t.parent[p] < 0:
+            continue
+        sub = set(t.subtree(s))
+        sib = t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1]
+        for e in all_nodes:
+            if e in sub or e == p or e == sib:
+                continue
+            S.append(s)
+            E.append(e)
+    return np.array(S, np.int64), np.array(E, np.int64)
+
+
+def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None):
+    """One SPR pass: score every candidate join in one batch (or through
+    `scorer`, which may score a subset), then try the best-scoring moves in
+    order; a move is kept only if the exact re-diagnosed tree cost drops."""
+    t0 = time.perf_counter()
+    st = PassStats()
+    diag = downpass(t, be)
+    st.cost_before = diag.total
+    S, E = spr_candidates(t)
+    st.candidates = len(S)
+    t1 = time.perf_counter()
+    if scorer is None:
+        score = be.distances(S, E)
+    else:
+        score = scorer(t, S, E)
+    # the cost of each subtree where it is now: distance to its sibling
+    subs = np.unique(S)
+    cur = {}
+    if len(subs):
+        sib = np.array([t.kids[t.parent[s]][0] if t.kids[t.parent[s]][1] == s
+                        else t.kids[t.parent[s]][1] for s in subs], np.int64)
+        dcur = be.distances(subs, sib)
+        cur = dict(zip(subs.tolist(), dcur.tolist()))
+    st.seconds_scoring = time.perf_counter() - t1
+    if log is not None:
+        log.append((t.copy(), S, E, score))
+    gain = np.array([cur[s] - sc for s, sc in zip(S.tolist(), score.tolist())], np.int64)
+    order = np.lexsort((E, S, -gain))  # largest predicted gain first, ties by ids
+    best = diag.total
+    tried = set()
+    for i in order:
+        if st.moves_tried >= max_moves or gain[i] <= 0:
+            break
+        s, e = int(S[i]), int(E[i])
+        if s in tried:
+            continue
+        tried.add(s)
+        if not (t.in_tree[s] and t.in_tree[e]) or e in set(t.subtree(s)):
+            continue
+        st.moves_tried += 1
+        trial = t.copy()
+        w = trial.prune(s)
+        if trial.parent[e] < 0 and e != trial.root:
+            continue
+        trial.insert(s, e, w)
+        d = downpass(trial, be)
+        if d.total < best:
+            best = d.total
+            t.parent, t.kids, t.root, t.free, t.in_tree = (trial.parent, trial.kids, trial.root,
+                                                          trial.free, trial.in_tree)
+            st.moves_accepted += 1
+    downpass(t, be)
+    st.cost_after = best
+    st.seconds_total = time.perf_counter() - t0
+    return st

@@ -1,0 +1,73 @@
+"""The candidate-pass backend interface of poyd_gb300.search implemented on
+the CPU oracle (test infrastructure): DOS.median / DOS.distance, NonaddCS8
+and SankCS from oracle/, one pair at a time as the reference does."""
+import numpy as np
+
+from oracle import oracle as O
+from poyd_gb300.simulate import SANK_INF
+
+
+class OracleBackend:
+    def __init__(self, data, om):
+        self.om = om
+        self.n = data.n_taxa
+        self.seq = {v: np.asarray(s, np.uint8) for v, s in enumerate(data.seqs)}
+        self.fitch = {v: data.fitch[v].copy() for v in range(self.n)}
+        big = O.SANK_INF
+        self.sank = {}
+        for v in range(self.n):
+            s = data.sank[v].astype(np.int64)
+            s[s >= SANK_INF] = big
+            self.sank[v] = s
+        self.tcm = data.sank_tcm.astype(np.int64)
+        self.nf = data.fitch.shape[1]
+        self.ns = data.sank.shape[1]
+
+    def medians(self, a, b, out):
+        do, fi = [], []
+        for x, y, v in zip(a, b, out):
+            c, med, _, _, _ = O.dos_median(self.seq[int(x)], self.seq[int(y)], self.om)
+            self.seq[int(v)] = med
+            do.append(c)
+            if self.nf:
+                fc, fm = O.nonadd_median(self.fitch[int(x)], self.fitch[int(y)])
+            else:
+                fc, fm = 0, np.zeros(0, np.uint8)
+            self.fitch[int(v)] = fm
+            fi.append(fc)
+            rows = []
+            for ch in range(self.ns):
+                c_, _, _ = O.sank_elt_median(self.tcm, self.sank[int(x)][ch], self.sank[int(y)][ch])
+                rows.append(c_)
+            self.sank[int(v)] = np.array(rows, np.int64).reshape(self.ns, -1) if self.ns else \
+                np.zeros((0, self.tcm.shape[0]), np.int64)
+        return np.array(do, np.int64), np.array(fi, np.int64)
+
+    def distances(self, a, b):
+        out = []
+        for x, y in zip(a, b):
+            s1, s2 = self.seq[int(x)], self.seq[int(y)]
+            d = O.cost_2(s1, s2, self.om, max(abs(len(s1) - len(s2)), 8))
+            if self.nf:
+                d += O.nonadd_distance(self.fitch[int(x)], self.fitch[int(y)])
+            tot = 0.0
+            for ch in range(self.ns):
+                tot += O.sank_elt_distance(self.tcm, self.sank[int(x)][ch], self.sank[int(y)][ch])
+            out.append(d + int(tot))
+        return np.array(out, np.int64)
+
+    def sank_cost(self, v):
+        if not self.ns:
+            return 0
+        return int(sum(int(min(r)) for r in self.sank[int(v)]))
+
+    def node_seq(self, v):
+        return self.seq[int(v)]
+
+    def node_fitch(self, v):
+        return self.fitch[int(v)]
+
+    def node_sank(self, v):
+        s = self.sank[int(v)].copy()
+        s[s >= O.SANK_INF] = SANK_INF
+        return s.astype(np.int32)
