@@ -213,6 +213,35 @@ int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int32_t k,
                              int64_t *dist, void *stream);
 
 /* ---------------------------------------------------------------------
+ * Learned join proposal (no counterpart in the reference): building blocks
+ * of the 32-256-256-128-1 ReLU MLP with BF16 weights/activations and FP32
+ * accumulation on tensor cores.  Matrices are row-major bf16 (uint16
+ * storage); op(A)[m,k] = tA ? A[k*lda+m] : A[m*lda+k], likewise B.
+ * ------------------------------------------------------------------- */
+/* C[M,N] = op(A) op(B) (+ bias[n]) (ReLU) -> C32 (fp32, optional, added to
+ * when accumulate) and/or C16 (bf16), row stride ldc. */
+int poyd_gemm_bf16(const void *A, int32_t lda, int32_t tA, const void *B, int32_t ldb,
+                   int32_t tB, int32_t M, int32_t N, int32_t K, const float *bias,
+                   int32_t relu, float *C32, void *C16, int32_t ldc, int32_t accumulate,
+                   void *stream);
+/* dZ = dH * (H > 0) over n bf16 elements */
+int poyd_relu_grad_bf16(const void *dH, const void *H, void *dZ, int64_t n, void *stream);
+/* out[n] = sum_m X[m, n] */
+int poyd_colsum_bf16(const void *X, int32_t M, int32_t N, float *out, void *stream);
+/* y[m] = H[m,:] . w + b[0] (the 128 -> 1 output layer) */
+int poyd_mlp_head_forward(const void *H, const void *w, const float *b, int32_t M, int32_t K,
+                          float *y, void *stream);
+/* mean-squared-error head: dZ = (2(y-t)/M) w masked by H > 0, dw = H^T dy,
+ * db = sum dy, loss = mean (y-t)^2 */
+int poyd_mlp_head_backward(const void *H, const void *w, const float *y, const float *target,
+                           int32_t M, int32_t K, void *dZ, float *dw, float *db, float *loss,
+                           void *stream);
+/* Adam on fp32 master weights (step >= 1), refreshing the bf16 copy w16 */
+int poyd_adam_step(float *w, void *w16, const float *g, float *m, float *v, int64_t n, float lr,
+                   float b1, float b2, float eps, int32_t step, void *stream);
+int poyd_to_bf16(const float *x, void *y, int64_t n, void *stream);
+
+/* ---------------------------------------------------------------------
  * Measurement helpers (no counterpart in the reference, which has no
  * device).  While profiling is on, every kernel the library launches is
  * bracketed by CUDA events on its own stream; poyd_profile_read sums the
