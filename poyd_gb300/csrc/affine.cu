@@ -413,9 +413,9 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
                  const int32_t *b_len, int32_t *cost, int64_t *cells, bool want_align,
                  int32_t flags, uint8_t *out, const int64_t *out_off, int32_t *out_len,
                  cudaStream_t st) {
-  Workspace *w = workspace();
+  Workspace *w = workspace(st);
   DevTables *tabs = nullptr;
-  int rc = upload_tables(cm, &tabs, st);
+  int rc = upload_tables_ws(w, cm, &tabs, st);
   if (rc) return rc;
   AffPlan *plans = (AffPlan *)ws_buffer(w, WS_AFF, sizeof(AffPlan) * (size_t)n);
   int64_t *dmw = (int64_t *)ws_buffer(w, WS_DMWORDS, sizeof(int64_t) * 2 * (size_t)n);

@@ -44,7 +44,7 @@ struct DevTables {
 };
 
 struct Workspace;
-Workspace *workspace();  // per current device
+Workspace *workspace(cudaStream_t st = nullptr);  // per (current device, stream)
 // Grow-only device buffer `slot` of at least `bytes`; returns nullptr on failure.
 void *ws_buffer(Workspace *w, int slot, size_t bytes);
 enum WsSlot {

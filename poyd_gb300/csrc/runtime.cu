@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -43,14 +44,17 @@ struct Workspace {
 };
 
 static std::mutex g_ws_mu;
-static Workspace *g_ws[64] = {};
+static std::map<std::pair<int, cudaStream_t>, Workspace *> g_ws;
 
-Workspace *workspace() {
+// One workspace per (device, stream): batches issued on different streams
+// may be in flight together without sharing scratch.
+Workspace *workspace(cudaStream_t st) {
   int dev = 0;
   cudaGetDevice(&dev);
   std::lock_guard<std::mutex> lk(g_ws_mu);
-  if (!g_ws[dev & 63]) g_ws[dev & 63] = new Workspace();
-  return g_ws[dev & 63];
+  Workspace *&w = g_ws[std::make_pair(dev, st)];
+  if (!w) w = new Workspace();
+  return w;
 }
 
 void *ws_buffer(Workspace *w, int slot, size_t bytes) {
@@ -104,7 +108,7 @@ static int check_cm(const poyd_cm *cm, int *maxc) {
 }
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream) {
-  return upload_tables_ws(workspace(), cm, dev, stream);
+  return upload_tables_ws(workspace((cudaStream_t)stream), cm, dev, stream);
 }
 
 int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *stream) {
@@ -231,7 +235,7 @@ extern "C" int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *se
   if (cm->cost_model == 1)
     return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, false,
                         0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
-  return linear_batch(workspace(), cm, maxc, n, seq, a_off, a_len, b_off, b_len, deltaw_policy, deltaw, cost,
+  return linear_batch(workspace((cudaStream_t)stream), cm, maxc, n, seq, a_off, a_len, b_off, b_len, deltaw_policy, deltaw, cost,
                       band_cells, false, 0, nullptr, nullptr, nullptr, (cudaStream_t)stream);
 }
 
@@ -250,7 +254,7 @@ extern "C" int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *s
   if (cm->cost_model == 1)
     return affine_batch(cm, maxc, n, seq, a_off, a_len, b_off, b_len, cost, band_cells, true,
                         flags, out, out_off, out_len, (cudaStream_t)stream);
-  return linear_batch(workspace(), cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
+  return linear_batch(workspace((cudaStream_t)stream), cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
                       nullptr, cost, band_cells, true, flags, out, out_off, out_len,
                       (cudaStream_t)stream);
 }
