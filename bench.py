@@ -49,6 +49,11 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-s", type=float, default=12.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", default="align", choices=["align", "spr", "learned", "serving"],
+                   help="align (default, the headline line) or one of the other configs")
+    p.add_argument("--train-trees", type=int, default=2)
+    p.add_argument("--max-passes", type=int, default=8)
+    p.add_argument("--serve-s", type=float, default=10.0)
     return p.parse_args()
 
 
@@ -200,6 +205,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def aggregate(cells: int, seconds: float, dev, world: int):
+    """Replica aggregation: (sum of band cells over ranks, max step time over
+    ranks).  Each rank runs its own independent pairs; no data-path
+    collective, only these two reductions of the timing."""
+    import torch
+    import torch.distributed as dist
+    c = torch.tensor([float(cells)], dtype=torch.float64, device=dev)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(c.item()), float(t.item())
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -250,11 +269,8 @@ def run_ours(args):
     dp_ms, dp_n = native.profile_read(kname, clear=False)
     all_ms, all_n = native.profile_read(None, clear=True)
     native.lib().poyd_profile_enable(0)
-    t = torch.tensor([ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = cells * world / (ms_max * 1e-3) / 1e9
+    total_cells, ms_max = aggregate(cells, ms, dev, world)
+    value = total_cells / (ms_max * 1e-3) / 1e9
 
     # ---- end-to-end through the public API with host buffers ----
     e2e = None
@@ -280,10 +296,8 @@ def run_ours(args):
             out_host = e2e_step(out_host)
         dt = (time.perf_counter() - t0) / n_e2e
         d2h = sum(int(x.numel() * x.element_size()) for x in out_host)
-        tt = torch.tensor([dt], device=dev)
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": cells * world / float(tt.item()) / 1e9, "unit": UNIT,
+        _, dt_max = aggregate(cells, dt, dev, world)
+        e2e = {"value": total_cells / dt_max / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     if rank == 0:
@@ -334,10 +348,207 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _emit(line):
+    print(json.dumps(line))
+
+
+def _snapshot(be):
+    """Host copies of a GpuBackend's node data, in the oracle's layout."""
+    from oracle import oracle as O
+    seqs = [be.node_seq(v) for v in range(len(be.len))]
+    lens = np.array([len(s) for s in seqs], np.int32)
+    off = np.zeros(len(seqs), np.int64)
+    off[1:] = np.cumsum(lens.astype(np.int64))[:-1]
+    buf = np.concatenate(seqs + [np.zeros(64, np.uint8)])
+    fitch = np.ascontiguousarray(be.fitch[:, :be.nf].cpu().numpy()) if be.nf else np.zeros(1, np.uint8)
+    sank = be.sank[:, :be.ns].cpu().numpy().astype(np.int64)
+    sank[sank >= (1 << 30)] = O.SANK_INF
+    return buf, off, lens, fitch, np.ascontiguousarray(sank)
+
+
+def cpu_candidate_rate(be, S, E, budget_s, threads):
+    """Candidates/s of the oracle's C scoring on all host threads (sample)."""
+    import ctypes as C
+    from oracle import oracle as O
+    L = O.lib()
+    buf, off, lens, fitch, sank = _snapshot(be)
+    tcm = np.ascontiguousarray(be.tcm.cpu().numpy().astype(np.int64))
+    om = O.cm_dna(1, 2, -1)
+    rng = np.random.default_rng(0)
+
+    def run(idx):
+        chunks = np.array_split(idx, threads)
+        outs = [np.zeros(len(c), np.int64) for c in chunks]
+
+        def work(i):
+            a = np.ascontiguousarray(S[chunks[i]], np.int32)
+            b = np.ascontiguousarray(E[chunks[i]], np.int32)
+            L.or_candidate_scores(buf.ctypes.data, off.ctypes.data, lens.ctypes.data, fitch.ctypes.data,
+                                  be.nf, sank.ctypes.data, be.ns, be.k, tcm.ctypes.data, a.ctypes.data,
+                                  b.ctypes.data, len(a), C.byref(om), outs[i].ctypes.data)
+        ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+        t0 = time.perf_counter()
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        return time.perf_counter() - t0, np.concatenate(outs)
+
+    probe = rng.choice(len(S), size=min(len(S), threads * 4), replace=False)
+    dt, _ = run(probe)
+    k = int(min(len(S), max(len(probe), budget_s / max(dt / len(probe), 1e-9))))
+    idx = rng.choice(len(S), size=k, replace=False)
+    dt, out = run(idx)
+    return k / dt, k, idx, out
+
+
+def run_spr(args):
+    """Config 2: one SPR pass, 200 taxa x ~1,500 bp + 2,000 Fitch (2-8 states)
+    + 200 Sankoff (4 states); every candidate join scored in one batch."""
+    import torch
+    from poyd_gb300 import align, learned, native, search, simulate
+    data = simulate.simulate(args.seed, 200, 1500, n_fitch=2000, n_sank=200)
+    be = search.GpuBackend(data, align.CostMatrix.default())
+    t = learned.random_tree(data.n_taxa, args.seed)
+    search.downpass(t, be)
+    S, E = search.spr_candidates(t)
+    for _ in range(2):  # warm-up
+        be.distances(S[:4096], E[:4096])
+    native.lib().poyd_profile_enable(1)
+    native.profile_read(clear=True)
+    be.stats["do_cells"] = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    score = be.distances(S, E)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    k = {}
+    for name in ("lin_dp_cost", "lin_plan", "fitch_distance", "sank_distance"):
+        k[name] = native.profile_read(name, clear=False)[0]
+    native.profile_read(clear=True)
+    native.lib().poyd_profile_enable(0)
+    threads = os.cpu_count() or 1
+    rate, k_cpu, idx, out = cpu_candidate_rate(be, S, E, args.cpu_sample_s, threads)
+    st = search.spr_pass(t, be, max_moves=16)
+    n = len(S)
+    fitch_bytes = 2.0 * n * be.nf
+    sank_bytes = 2.0 * n * be.ns * be.k * 4
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs") \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6774.9
+    line = {
+        "workload": "config 2: SPR pass, 200 taxa x 1500 bp + 2000 Fitch + 200 Sankoff",
+        "metric": "candidate joins scored per second", "value": n / dt, "unit": "joins/s",
+        "candidates": n, "seconds_scoring": dt,
+        "kernel_ms": k,
+        "do_gcups_cost_only": be.stats["do_cells"] / 1e9 / (k["lin_dp_cost"] * 1e-3)
+        if k["lin_dp_cost"] else None,
+        "fitch_gbs": fitch_bytes / (k["fitch_distance"] * 1e-3) / 1e9 if k["fitch_distance"] else None,
+        "sank_gbs": sank_bytes / (k["sank_distance"] * 1e-3) / 1e9 if k["sank_distance"] else None,
+        "hbm_peak_gbs": peak,
+        "pass": {"moves_tried": st.moves_tried, "moves_accepted": st.moves_accepted,
+                 "cost_before": st.cost_before, "cost_after": st.cost_after,
+                 "seconds": st.seconds_total},
+    }
+    line["cpu_baseline"] = {"value": rate, "unit": "joins/s", "cores": threads, "kind": "port",
+                            "sample": "%d of %d candidates" % (k_cpu, n),
+                            "bit_exact_on_sample": bool(np.array_equal(out, score[idx]))}
+    _emit(line)
+
+
+def run_learned(args):
+    """Config 3: learned proposal vs plain exhaustive SPR, time to the same
+    exact tree cost (500 taxa x ~1,000 bp)."""
+    import torch
+    from poyd_gb300 import align, learned, search, simulate
+    data = simulate.simulate(args.seed, 500, 1000, n_fitch=400, n_sank=40)
+    be = search.GpuBackend(data, align.CostMatrix.default())
+    Xs, ys = [], []
+    t0 = time.perf_counter()
+    for s in range(args.train_trees):
+        t = learned.random_tree(data.n_taxa, 1000 + s)
+        search.downpass(t, be)
+        X, y = learned.log_pass(t, be)
+        Xs.append(X)
+        ys.append(y)
+    X, y = torch.cat(Xs), torch.cat(ys)
+    t_log = time.perf_counter() - t0
+    prop = learned.Proposal(seed=0)
+    t0 = time.perf_counter()
+    prop.fit(X, y, epochs=4, batch=4096, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    tp = learned.random_tree(data.n_taxa, args.seed + 7)
+    hist_p, sec_p = learned.run_search(tp, be, None, max_passes=args.max_passes)
+    target = hist_p[-1]
+    tl = learned.random_tree(data.n_taxa, args.seed + 7)
+    stats = {}
+    sc = learned.learned_scorer(prop, be, frac=0.03, stats=stats)
+    t0 = time.perf_counter()
+    hist_l = []
+    for _ in range(3 * args.max_passes):
+        st = search.spr_pass(tl, be, max_moves=16, scorer=sc)
+        hist_l.append(st.cost_after)
+        if st.cost_after <= target:
+            break
+        if st.moves_accepted == 0:
+            st = search.spr_pass(tl, be, max_moves=16)  # exhaustive fallback
+            hist_l.append(st.cost_after)
+            if st.moves_accepted == 0 or st.cost_after <= target:
+                break
+    torch.cuda.synchronize()
+    sec_l = time.perf_counter() - t0
+    _emit({
+        "workload": "config 3: learned join proposal vs plain exhaustive SPR, 500 taxa x 1000 bp",
+        "metric": "SPR time to equal tree cost, learned vs plain GPU",
+        "plain_seconds": sec_p, "plain_cost": target, "plain_passes": len(hist_p),
+        "learned_seconds": sec_l, "learned_cost": hist_l[-1], "learned_passes": len(hist_l),
+        "speedup": sec_p / sec_l if sec_l else None,
+        "reached_same_cost": hist_l[-1] <= target,
+        "training_pairs": int(X.shape[0]), "log_seconds": t_log, "train_seconds": t_train,
+        "exact_evaluated_fraction": stats.get("exact", 0) / max(stats.get("candidates", 1), 1),
+    })
+
+
+def run_serving(args):
+    """Config 4: Poisson stream (2,000 req/s) from 16 simulated searches."""
+    import torch
+    from poyd_gb300 import align, serve
+    seqs, jobs = serve.make_workload(args.seed, n_clients=16, rate=2000.0, seconds=args.serve_s)
+    pool = serve.SequencePool(seqs)
+    cm = align.CostMatrix.default()
+    warm = serve.Server(pool, cm, n_streams=3)
+    warm.run([serve.Job(-1 - i, j.kind, j.a, j.b, 0.0) for i, j in enumerate(jobs[:256])])
+    srv = serve.Server(pool, cm, budget_bytes=120 << 30, n_streams=3)
+    t0 = time.perf_counter()
+    done = srv.run(jobs)
+    wall = time.perf_counter() - t0
+    st = serve.latency_stats(done)
+    rng = np.random.default_rng(1)
+    ok = True
+    for j in rng.choice(done, size=min(64, len(done)), replace=False):
+        b = pool.batch([j.a], [j.b], torch.device("cuda"))
+        if j.kind == "cost":
+            ok &= int(align.cost_2(b, cm, deltaw="dos")[0].item()) == j.cost
+        else:
+            r = align.align_2(b, cm, dos_empty=True).to_host()[0]
+            ok &= r["cost"] == j.cost and np.array_equal(r["median"], j.median)
+    _emit({"workload": "config 4: serving loop, 16 searches, Poisson 2000 req/s, 120 GB budget",
+           "metric": "served requests/s", "value": len(done) / wall, "unit": "req/s",
+           "offered_rate": 2000.0, "seconds": wall, "batches": srv.batches,
+           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+           "jobs": st["n"], "sample_identical_alone": bool(ok)})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "spr":
+        run_spr(args)
+    elif args.workload == "learned":
+        run_learned(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

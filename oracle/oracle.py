@@ -97,6 +97,9 @@ def lib():
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OrCM),
                                          C.c_void_p]
         L.or_dos_median_many.restype = C.c_int64
+        L.or_candidate_scores.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                                             C.c_void_p, C.c_void_p, C.c_void_p,
+                                                             C.c_int, C.POINTER(OrCM), C.c_void_p]
         L.or_nonadd_median.argtypes = [u8p, u8p, C.c_int, u8p]
         L.or_nonadd_median.restype = C.c_int64
         L.or_nonadd_distance.argtypes = [u8p, u8p, C.c_int]

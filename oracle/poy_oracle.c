@@ -899,3 +899,29 @@ int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32
     }
     return cells;
 }
+
+/* Candidate-join scores for the CPU timing of a search pass: for pairs
+ * (a[t], b[t]) of nodes, DOS.distance (seqCS.ml:819-867) + Fitch distance
+ * (nonaddCSc.c:1076-1105) + Sankoff distance (sankCS.ml:371-377).  Node
+ * data: sequences in a packed buffer, Fitch rows [node][nf], Sankoff cost
+ * vectors [node][ns][k] (int64, OR_SANK_INF = infinity). */
+void or_candidate_scores(const uint8_t *seq, const int64_t *off, const int32_t *len,
+                         const uint8_t *fitch, int nf, const int64_t *sank, int ns, int k,
+                         const int64_t *tcm, const int32_t *a, const int32_t *b, int n,
+                         const or_cm *m, int64_t *out) {
+    int t, ch;
+    for (t = 0; t < n; t++) {
+        const uint8_t *x = seq + off[a[t]], *y = seq + off[b[t]];
+        int lx = len[a[t]], ly = len[b[t]];
+        int64_t s = or_cost_2(x, lx, y, ly, m, 1, or_dos_distance_deltaw(lx, ly));
+        if (nf) s += or_nonadd_distance(fitch + (int64_t)a[t] * nf, fitch + (int64_t)b[t] * nf, nf);
+        {
+            double tot = 0.0;
+            for (ch = 0; ch < ns; ch++)
+                tot += or_sank_elt_distance(k, tcm, sank + ((int64_t)a[t] * ns + ch) * k,
+                                            sank + ((int64_t)b[t] * ns + ch) * k);
+            s += (int64_t)tot;
+        }
+        out[t] = s;
+    }
+}

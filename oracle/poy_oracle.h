@@ -139,6 +139,12 @@ int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32
                            const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
                            int n, const or_cm *m, int32_t *cost);
 
+/* Candidate-join scores DOS.distance + Fitch + Sankoff (CPU timing driver). */
+void or_candidate_scores(const uint8_t *seq, const int64_t *off, const int32_t *len,
+                         const uint8_t *fitch, int nf, const int64_t *sank, int ns, int k,
+                         const int64_t *tcm, const int32_t *a, const int32_t *b, int n,
+                         const or_cm *m, int64_t *out);
+
 /* ---- Fitch non-additive characters, 8-bit lanes (nonaddCSc.c) ---- */
 int64_t or_nonadd_median(const uint8_t *a, const uint8_t *b, int len, uint8_t *res);
 int64_t or_nonadd_distance(const uint8_t *a, const uint8_t *b, int len);

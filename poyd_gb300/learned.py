@@ -95,7 +95,7 @@ def features(t: search.Tree, be, S: np.ndarray, E: np.ndarray, cur: dict) -> tor
     fsib = _fitch_dist(be, S, sb) / nf * 10
     sse = _sank_dist(be, S, E) / ns
     ssib = _sank_dist(be, S, sb) / ns
-    curs = T(np.array([cur[int(x)] for x in S], np.float32))
+    curs = T(cur[S].astype(np.float32))
     size_t, depth_t = T(size), T(depth)
     f = [
         torch.log1p(size_t[s]), torch.log1p(size_t[e]),
@@ -116,13 +116,14 @@ def features(t: search.Tree, be, S: np.ndarray, E: np.ndarray, cur: dict) -> tor
     return X
 
 
-def current_attachment(t: search.Tree, be, S: np.ndarray) -> dict:
+def current_attachment(t: search.Tree, be, S: np.ndarray) -> np.ndarray:
+    """Exact distance of every pruned subtree to its current sibling, indexed by node id."""
+    cur = np.zeros(len(t.parent), np.int64)
     subs = np.unique(S)
-    if len(subs) == 0:
-        return {}
-    _, _, _, sib = node_info(t, be)
-    d = be.distances(subs, sib[subs])
-    return dict(zip(subs.tolist(), d.tolist()))
+    if len(subs):
+        _, _, _, sib = node_info(t, be)
+        cur[subs] = be.distances(subs, sib[subs])
+    return cur
 
 
 class Proposal:
@@ -151,7 +152,7 @@ def log_pass(t: search.Tree, be):
     X = features(t, be, S, E, cur)
     score = be.distances(S, E)
     delta = torch.from_numpy(
-        (score - np.array([cur[int(x)] for x in S], np.int64)).astype(np.float32) / 100.0
+        (score - cur[S]).astype(np.float32) / 100.0
     ).to(be.dev)
     return X, delta
 

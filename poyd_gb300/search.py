@@ -278,6 +278,25 @@ class GpuBackend:
         self.stats["do_cells"] += int(cells.sum().item())
         return tot.cpu().numpy()
 
+    def ensure_nodes(self, n_nodes: int):
+        """Room for node ids < n_nodes (scratch ids of move evaluation)."""
+        have = self.fitch.shape[0]
+        if n_nodes <= have:
+            return
+        grow = max(n_nodes, 2 * have)
+        f = torch.zeros((grow, self.stride), dtype=torch.uint8, device=self.dev)
+        f[:have] = self.fitch
+        sk = torch.zeros((grow,) + tuple(self.sank.shape[1:]), dtype=torch.int32, device=self.dev)
+        sk[:have] = self.sank
+        self.fitch, self.sank = f, sk
+        self.off = np.concatenate([self.off, np.zeros(grow - have, np.int64)])
+        self.len = np.concatenate([self.len, np.zeros(grow - have, np.int32)])
+
+    def release_nodes(self, first: int):
+        """Forget scratch node ids >= first (their pool bytes are reclaimed
+        at the next compaction)."""
+        self.len[first:] = 0
+
     def sank_cost(self, v: int) -> int:
         if not self.ns:
             return 0
@@ -349,24 +368,46 @@ class PassStats:
     seconds_total: float = 0.0
 
 
+def euler(t: Tree):
+    """Preorder entry / exit times: u is in subtree(v) iff tin[v] <= tin[u] < tout[v]."""
+    cap = len(t.parent)
+    tin = np.zeros(cap, np.int64)
+    tout = np.zeros(cap, np.int64)
+    clock = 0
+    stack = [(t.root, 0)]
+    while stack:
+        v, state = stack.pop()
+        if state == 0:
+            tin[v] = clock
+            clock += 1
+            stack.append((v, 1))
+            if v >= t.n:
+                stack.append((int(t.kids[v][1]), 0))
+                stack.append((int(t.kids[v][0]), 0))
+        else:
+            tout[v] = clock
+    return tin, tout
+
+
 def spr_candidates(t: Tree):
     """Every (pruned subtree s, join edge e) of one SPR pass: s ranges over
     non-root nodes whose parent is not the root, e over the nodes left after
-    pruning s, except s's old sibling (the unchanged tree)."""
-    S, E = [], []
-    all_nodes = t.nodes()
-    for s in all_nodes:
-        p = t.parent[s]
-        if p < 0 or t.parent[p] < 0:
-            continue
-        sub = set(t.subtree(s))
-        sib = t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1]
-        for e in all_nodes:
-            if e in sub or e == p or e == sib:
-                continue
-            S.append(s)
-            E.append(e)
-    return np.array(S, np.int64), np.array(E, np.int64)
+    pruning s, except s's old parent and sibling (the unchanged tree)."""
+    nodes = np.array(sorted(t.nodes()), np.int64)
+    par = t.parent
+    ok = np.array([par[v] >= 0 and par[par[v]] >= 0 for v in nodes], bool)
+    subs = nodes[ok]
+    if len(subs) == 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    tin, tout = euler(t)
+    p = par[subs]
+    sib = np.where(t.kids[p, 0] == subs, t.kids[p, 1], t.kids[p, 0])
+    S = np.repeat(subs, len(nodes))
+    E = np.tile(nodes, len(subs))
+    ps, ss = np.repeat(p, len(nodes)), np.repeat(sib, len(nodes))
+    inside = (tin[E] >= tin[S]) & (tin[E] < tout[S])
+    keep = ~inside & (E != ps) & (E != ss)
+    return S[keep], E[keep]
 
 
 def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None):
@@ -386,41 +427,110 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None):
         score = scorer(t, S, E)
     # the cost of each subtree where it is now: distance to its sibling
     subs = np.unique(S)
-    cur = {}
+    cur = np.zeros(len(t.parent), np.int64)
     if len(subs):
-        sib = np.array([t.kids[t.parent[s]][0] if t.kids[t.parent[s]][1] == s
-                        else t.kids[t.parent[s]][1] for s in subs], np.int64)
-        dcur = be.distances(subs, sib)
-        cur = dict(zip(subs.tolist(), dcur.tolist()))
+        p = t.parent[subs]
+        sib = np.where(t.kids[p, 0] == subs, t.kids[p, 1], t.kids[p, 0])
+        cur[subs] = be.distances(subs, sib)
     st.seconds_scoring = time.perf_counter() - t1
     if log is not None:
         log.append((t.copy(), S, E, score))
-    gain = np.array([cur[s] - sc for s, sc in zip(S.tolist(), score.tolist())], np.int64)
+    gain = cur[S] - score
     order = np.lexsort((E, S, -gain))  # largest predicted gain first, ties by ids
-    best = diag.total
-    tried = set()
+    moves, seen = [], set()
     for i in order:
-        if st.moves_tried >= max_moves or gain[i] <= 0:
+        if len(moves) >= max_moves or gain[i] <= 0:
             break
         s, e = int(S[i]), int(E[i])
-        if s in tried:
-            continue
-        tried.add(s)
-        if not (t.in_tree[s] and t.in_tree[e]) or e in set(t.subtree(s)):
-            continue
-        st.moves_tried += 1
-        trial = t.copy()
-        w = trial.prune(s)
-        if trial.parent[e] < 0 and e != trial.root:
-            continue
-        trial.insert(s, e, w)
-        d = downpass(trial, be)
-        if d.total < best:
-            best = d.total
-            t.parent, t.kids, t.root, t.free, t.in_tree = (trial.parent, trial.kids, trial.root,
-                                                          trial.free, trial.in_tree)
-            st.moves_accepted += 1
-    downpass(t, be)
+        if s not in seen:
+            seen.add(s)
+            moves.append((s, e))
+    # Rounds: the exact cost of every remaining move is computed in one
+    # batched incremental diagnosis; the best improving move is applied and
+    # the tree re-diagnosed; moves no longer valid are dropped.
+    best = diag.total
+    while moves:
+        st.moves_tried += len(moves)
+        totals = evaluate_moves(t, be, diag, moves)
+        k = int(np.argmin(totals))
+        if totals[k] >= best:
+            break
+        s, e = moves.pop(k)
+        w = t.prune(s)
+        t.insert(s, e, w)
+        diag = downpass(t, be)
+        assert diag.total == totals[k], (diag.total, totals[k])
+        best = diag.total
+        st.moves_accepted += 1
+        moves = [(a, b) for a, b in moves if _valid_move(t, a, b)]
     st.cost_after = best
     st.seconds_total = time.perf_counter() - t0
     return st
+
+
+def _valid_move(t: Tree, s: int, e: int) -> bool:
+    p = t.parent[s]
+    if p < 0 or t.parent[p] < 0 or not t.in_tree[e]:
+        return False
+    sib = t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1]
+    return e != p and e != sib and e not in set(t.subtree(s))
+
+
+def _heights(t: Tree) -> dict:
+    h = {}
+    for v in t.nodes()[::-1]:
+        h[v] = 0 if v < t.n else 1 + max(h[t.kids[v][0]], h[t.kids[v][1]])
+    return h
+
+
+def evaluate_moves(t: Tree, be, diag: Diagnosis, moves) -> np.ndarray:
+    """Exact total cost of the tree after each SPR move (s onto the edge above
+    e), computed together: a move changes only the ancestors of the prune
+    point and of the regraft point, so each trial recomputes just those nodes
+    (into scratch node slots), and the dirty nodes of every trial at one
+    height form one batch of medians."""
+    h_base = _heights(t)
+    base_sank = be.sank_cost(t.root)
+    tid_next = 2 * t.n
+    recs = {}      # level -> list of (trial, a_ref, b_ref, out_tid)
+    old = np.zeros(len(moves), np.int64)
+    roots = []
+    for m, (s, e) in enumerate(moves):
+        T = t.copy()
+        p = T.parent[s]
+        g = T.parent[p]
+        w = T.prune(s)
+        T.insert(s, e, w)
+        dirty = set()
+        for v in (g, w):
+            while v >= 0 and v not in dirty:
+                dirty.add(v)
+                v = T.parent[v]
+        h, tid = {}, {}
+
+        def height(v):
+            if v not in dirty:
+                return h_base[v]
+            if v not in h:
+                h[v] = 1 + max(height(T.kids[v][0]), height(T.kids[v][1]))
+            return h[v]
+
+        for v in sorted(dirty, key=height):
+            tid[v] = tid_next
+            tid_next += 1
+            a, b = T.kids[v]
+            ref = lambda c: tid[c] if c in dirty else c
+            recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v]))
+            old[m] += diag.do_cost[v] + diag.fitch_cost[v]
+        roots.append(tid[T.root])
+    be.ensure_nodes(tid_next)
+    new = np.zeros(len(moves), np.int64)
+    for lvl in sorted(recs):
+        r = np.array(recs[lvl], np.int64)
+        do, fi = be.medians(r[:, 1], r[:, 2], r[:, 3])
+        np.add.at(new, r[:, 0], do + fi)
+    totals = np.array([diag.total - old[m] + new[m] - base_sank + be.sank_cost(roots[m])
+                       for m in range(len(moves))], np.int64)
+    be.release_nodes(2 * t.n)
+    return totals
+

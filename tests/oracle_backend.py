@@ -71,3 +71,11 @@ class OracleBackend:
         s = self.sank[int(v)].copy()
         s[s >= O.SANK_INF] = SANK_INF
         return s.astype(np.int32)
+
+    def ensure_nodes(self, n_nodes):
+        pass
+
+    def release_nodes(self, first):
+        for d in (self.seq, self.fitch, self.sank):
+            for v in [v for v in d if v >= first]:
+                del d[v]
