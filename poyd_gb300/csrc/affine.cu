@@ -139,6 +139,10 @@ __global__ void k_aff_plan(AffPlanArgs A) {
     A.cells[id] = c;
   }
   if (la < 1 || lb < 1) atomicOr(A.err, 1);
+  unsigned wide = 0;  // codes index 32-entry table rows
+  for (int x = 0; x < la; ++x) wide |= A.seq[ao + x];
+  for (int x = 0; x < lb; ++x) wide |= A.seq[bo + x];
+  if (wide >> 5) atomicOr(A.err, 4);
   // real costs must stay clear of the HIGH_NUM sentinel arithmetic
   if (A.maxc * (long long)(la + lb + 2) >= (1 << 22)) atomicOr(A.err, 2);
 }
@@ -441,6 +445,7 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
   CKA(cudaStreamSynchronize(st));
   if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
   if (hwd[n] & 2) return fail(POYD_ERANGE, "affine costs could reach the HIGH_NUM sentinel range");
+  if (hwd[n] & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
   std::vector<int64_t> off((size_t)n);
   int64_t total = 0;
   int maxwd = 1;

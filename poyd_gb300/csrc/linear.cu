@@ -41,17 +41,20 @@ __global__ void k_lin_plan(LinPlanArgs A) {
   const int la = A.a_len[id], lb = A.b_len[id];
   const int64_t ao = A.a_off[id], bo = A.b_off[id];
   const int gap = A.gap;
-  unsigned ga = 0, gb = 0, na = 0, nb = 0;
+  unsigned ga = 0, gb = 0, na = 0, nb = 0, wide = 0;
   for (int x = lane; x < la; x += 32) {
     const int c = A.seq[ao + x];
     ga += (c & gap) != 0;
     na += c != gap;
+    wide |= (unsigned)c >> 5;
   }
   for (int x = lane; x < lb; x += 32) {
     const int c = A.seq[bo + x];
     gb += (c & gap) != 0;
     nb += c != gap;
+    wide |= (unsigned)c >> 5;
   }
+  wide = __reduce_or_sync(kFull, wide);
   ga = __reduce_add_sync(kFull, ga);
   gb = __reduce_add_sync(kFull, gb);
   na = __reduce_add_sync(kFull, na);
@@ -108,7 +111,7 @@ __global__ void k_lin_plan(LinPlanArgs A) {
     P.nstrips = (l1 + kRows - 1) / kRows;
     const int S = wd + kLag * (kLanes - 1) + 1;
     const int Spad = (S + kStepBlock - 1) / kStepBlock * kStepBlock;
-    P.sblocks = Spad / 8;
+    P.sblocks = Spad / kStepBlock;
     P.deltaw = dw;
     P.empty = 0;
     if (A.dos_empty) {
@@ -118,22 +121,60 @@ __global__ void k_lin_plan(LinPlanArgs A) {
     P.pad_ = 0;
     A.plans[id] = P;
     // direction-matrix words; also the work estimate used to order pairs
-    A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * kRows;
+    A.dm_words[id] = (int64_t)P.nstrips * P.sblocks *
+                     lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
     A.wd_out[id] = wd;
     if (A.cells) A.cells[id] = cells;
     if (la < 1 || lb < 1) atomicOr(A.err, 1);
+    if (wide) atomicOr(A.err, 4);  // codes index 32-entry table rows
     if ((long long)A.maxc * (l1 + l2 + 2) >= kMaxCost) atomicOr(A.err, 2);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Band DP.  DM = true also writes the direction matrix.
+// Band DP.
+//
+// Three modes share one sweep:
+//   kDpCost    costs only;
+//   kDpSets    also the full direction set of every cell, three bit planes
+//              (align, insert, delete), for the single-pair simple_2 /
+//              backtrack_2d protocol where the backtrack priority is chosen
+//              after the fill;
+//   kDpChoice  the move backtrack_2d will take from every cell, two bits,
+//              when the priority is known before the fill (batched align_2).
+//              Values are kept times four with the move's rank in the low two
+//              bits (align 0; then insert 1, delete 2 when swaped, else
+//              delete 1, insert 2), so one add-min chain yields the minimum
+//              and, among tied moves, the one of highest priority.
+// Every value is biased by cost[s1[0]][s2[0]] (cell (0,0) holds it instead
+// of 0) so that all values stay non-negative; the bias is removed from the
+// result.
 // ---------------------------------------------------------------------------
 struct LinStrip {
   int HA, HB, diag, Pk, q;
-  uint32_t wA, wB;
+  uint32_t a0, a1, a2;  // row A direction words
+  uint32_t b0, b1, b2;  // row B
   int result;
 };
+
+// Shared memory of one k_lin_dp block.
+struct LinSmem {
+  uint32_t ctab[32 * 33];               // cost[a][b] at a*33 + b (rows padded one bank)
+  int gcost[3][32];                     // cost[gap][b]; 4*cost[gap][b] + 1; ... + 2
+  uint32_t prof[kDpWarps][32][kLanes];  // per lane: cost[aA][c] | cost[aB][c] << 16 (x4 in kDpChoice)
+};
+
+template <int MODE>
+struct DpMode {
+  static constexpr int kScale = MODE == kDpChoice ? 4 : 1;
+  static constexpr int kInfV = MODE == kDpChoice ? kInfChoice : kInf;
+};
+
+// Appends one direction bit: (plane << 1) | [cand == h].  h is the minimum
+// of the candidates, so cand - h - 1 is negative exactly when cand == h.
+__device__ __forceinline__ uint32_t dir_bit(uint32_t plane, int cand, int h) {
+  return __funnelshift_l((uint32_t)(cand - h - 1), plane, 1);
+}
 
 // 32 steps of one strip.  Each lane owns two rows: row A = r0 + 2k handles
 // diagonal d at step s = d - dlo + 3k, row B = row A + 1 handles d - 1 in
@@ -141,39 +182,55 @@ struct LinStrip {
 // just before and both cells use the same column character.  MASK applies
 // the per-row band/matrix validity (needed only in blocks where some row is
 // outside its band); CAP records the final cell (last strip only).
-template <bool DM, bool MASK, bool CAP>
-__device__ __forceinline__ void lin_block(LinStrip &S, const int2 *trowA, const int2 *trowB,
+template <int MODE, bool MASK, bool CAP>
+__device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, const int *gcost,
                                           int cDA, int cDB, int vbA, int cntA, int vbB, int cntB,
-                                          int finA, int finB, uint2 *dmw, int lane) {
+                                          int finA, int finB, uint32_t *dmw, int lane) {
+  constexpr int kInfV = DpMode<MODE>::kInfV;
 #pragma unroll
   for (int u = 0; u < kStepBlock; ++u) {
     int up = __shfl_up_sync(kFull, S.Pk, 1);
     if (lane == 0) up = S.q;
     S.q = __shfl_sync(kFull, S.q, (lane + 1) & 31);
     const int c = up & 31;
-    const int hup = up >> 5;
-    const int2 TA = trowA[c];  // {cost[a][c], cost[gap][c]}
-    const int2 TB = trowB[c];
-    // row A: delete from the lane above, align from its previous value
-    const int Av = S.diag + TA.x;
-    const int Dv = hup + cDA;
-    const int Iv = S.HA + TA.y;
-    int ha = min(min(Av, Dv), Iv);
-    if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInf;
-    // row B: delete from row A now, align from row A's previous value
-    const int Av2 = S.HA + TB.x;
-    const int Dv2 = ha + cDB;
-    const int Iv2 = S.HB + TB.y;
-    int hb = min(min(Av2, Dv2), Iv2);
-    if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInf;
-    if (DM) {
-      const uint32_t fa = (uint32_t)(Av == ha) | ((uint32_t)(Iv == ha) << 1) |
-                          ((uint32_t)(Dv == ha) << 2);
-      const uint32_t fb = (uint32_t)(Av2 == hb) | ((uint32_t)(Iv2 == hb) << 1) |
-                          ((uint32_t)(Dv2 == hb) << 2);
-      S.wA = (S.wA << 4) | fa;
-      S.wB = (S.wB << 4) | fb;
-      if ((u & 7) == 7) dmw[(u >> 3) * kLanes] = make_uint2(S.wA, S.wB);
+    const int hup = (int)((unsigned)up >> 5);
+    const uint32_t pr = prof[c * kLanes];  // {cost[aA][c], cost[aB][c]}
+    const int g = gcost[c];                // cost[gap][c] (+ rank)
+    int ha, hb;
+    if (MODE == kDpSets) {
+      // row A: delete from the lane above, align from its previous value
+      const int Av = S.diag + (int)(pr & 0xffffu);
+      const int Dv = hup + cDA;
+      const int Iv = S.HA + g;
+      ha = min(min(Av, Dv), Iv);
+      if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
+      // row B: delete from row A now, align from row A's previous value
+      const int Av2 = S.HA + (int)(pr >> 16);
+      const int Dv2 = ha + cDB;
+      const int Iv2 = S.HB + g;
+      hb = min(min(Av2, Dv2), Iv2);
+      if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
+      S.a0 = dir_bit(S.a0, Av, ha);
+      S.a1 = dir_bit(S.a1, Iv, ha);
+      S.a2 = dir_bit(S.a2, Dv, ha);
+      S.b0 = dir_bit(S.b0, Av2, hb);
+      S.b1 = dir_bit(S.b1, Iv2, hb);
+      S.b2 = dir_bit(S.b2, Dv2, hb);
+    } else {
+      ha = __viaddmin_s32(hup, cDA, __viaddmin_s32(S.HA, g, S.diag + (int)(pr & 0xffffu)));
+      if (MODE == kDpChoice) {
+        if (u < 16) S.a0 = (S.a0 << 2) | ((uint32_t)ha & 3u);
+        else S.a1 = (S.a1 << 2) | ((uint32_t)ha & 3u);
+        ha &= ~3;
+      }
+      if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
+      hb = __viaddmin_s32(ha, cDB, __viaddmin_s32(S.HB, g, S.HA + (int)(pr >> 16)));
+      if (MODE == kDpChoice) {
+        if (u < 16) S.b0 = (S.b0 << 2) | ((uint32_t)hb & 3u);
+        else S.b1 = (S.b1 << 2) | ((uint32_t)hb & 3u);
+        hb &= ~3;
+      }
+      if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
     }
     if (CAP) {
       if (u == finA) S.result = ha;
@@ -185,28 +242,42 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const int2 *trowA, const 
     S.HA = ha;
     S.HB = hb;
   }
+  if (MODE == kDpSets) {
+    uint2 *w = (uint2 *)dmw;
+    w[0] = make_uint2(S.a0, S.b0);
+    w[kLanes] = make_uint2(S.a1, S.b1);
+    w[2 * kLanes] = make_uint2(S.a2, S.b2);
+  } else if (MODE == kDpChoice) {
+    *(uint4 *)dmw = make_uint4(S.a0, S.a1, S.b0, S.b1);
+  }
 }
 
-template <bool DM>
-__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const int2 *tab,
-                                         const LinPlan &P, int64_t dm_off, int id,
-                                         int *bnd, int lane) {
+template <int MODE>
+__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const LinSmem &sm, uint32_t *prof,
+                                         const LinPlan &P, int64_t dm_off, int id, int *bnd,
+                                         int lane) {
+  constexpr int kScale = DpMode<MODE>::kScale, kInfV = DpMode<MODE>::kInfV;
+  constexpr int kWords = lin_dm_words(MODE);  // DM words per (strip, 32-step block)
   const uint8_t *s1 = A.seq + P.s1_off;
   const uint8_t *s2 = A.seq + P.s2_off;
   const int L1 = P.l1, L2 = P.l2, dlo = P.dlo, wd = P.wd;
   const int gap = A.gap;
+  // backtrack priority (algn.c:3605-3666): insert before delete when swaped
+  const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
+  const int rank_i = MODE == kDpChoice ? (swaped ? 1 : 2) : 0;
+  const int rank_d = MODE == kDpChoice ? 3 - rank_i : 0;
+  const int *gcost = sm.gcost[rank_i];
+  const int bias = kScale * (int)sm.ctab[s1[0] * 33 + s2[0]];
 
-  for (int x = lane; x < wd; x += 32) bnd[x] = kInf;
-  __syncwarp();
-  if (lane == 0) bnd[-dlo] = -tab[(s1[0] << 5) | s2[0]].x;
+  for (int x = lane; x < wd; x += 32) bnd[x] = (x == -dlo) ? 0 : kInfV;
   __syncwarp();
 
-  const int Spad = P.sblocks * 8;
+  const int Spad = P.sblocks * kStepBlock;
   const int r_last = L1 - 1;
   const int d_last = L2 - L1;
   LinStrip S;
   S.result = 0;
-  uint32_t *dm = DM ? A.dm + dm_off : nullptr;
+  uint32_t *dm = MODE != kDpCost ? A.dm + dm_off : nullptr;
 
   for (int strip = 0; strip < P.nstrips; ++strip) {
     const int r0 = strip * kRows;
@@ -214,8 +285,13 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const int2 *tab,
     const bool okA = rA < L1, okB = rB < L1;
     const bool last = strip == P.nstrips - 1;
     const int aA = okA ? s1[rA] : 0, aB = okB ? s1[rB] : 0;
-    const int2 *trowA = tab + (aA << 5), *trowB = tab + (aB << 5);
-    const int cDA = tab[(aA << 5) | gap].x, cDB = tab[(aB << 5) | gap].x;
+    // this lane's profile of its two row characters (read back only by the
+    // same lane: no warp synchronisation needed)
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c)
+      prof[c * kLanes] = kScale * (sm.ctab[aA * 33 + c] | (sm.ctab[aB * 33 + c] << 16));
+    const int cDA = kScale * (int)sm.ctab[aA * 33 + gap] + rank_d;
+    const int cDB = kScale * (int)sm.ctab[aB * 33 + gap] + rank_d;
     const int offA = (-dlo - rA) > 0 ? (-dlo - rA) : 0;
     const int offB = (-dlo - rB) > 0 ? (-dlo - rB) : 0;
     const int lowerA = kLag * lane + offA, lowerB = kLag * lane + 1 + offB;
@@ -227,56 +303,66 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const int2 *tab,
     const int hi = (lowerA + cntA) < (lowerB + cntB) ? (lowerA + cntA) : (lowerB + cntB);
     const int all_lo = (int)__reduce_max_sync(kFull, (unsigned)lo);
     const int all_hi = (int)__reduce_min_sync(kFull, (unsigned)hi);
-    S.HA = kInf;
-    S.HB = kInf;
-    S.diag = kInf;
-    S.Pk = (int)((unsigned)kInf << 5);
-    S.wA = 0;
-    S.wB = 0;
+    S.HA = kInfV;
+    S.HB = kInfV;
+    S.diag = kInfV;
+    S.Pk = (int)((unsigned)kInfV << 5);
     auto qload = [&](int s0) -> int {
       const int x = s0 + lane + 1;
-      const int hv = (x < wd) ? bnd[x] : kInf;
+      const int hv = (x < wd) ? bnd[x] : kInfV;
       const int j = r0 + dlo + s0 + lane;
       const int c = (j >= 0 && j < L2) ? s2[j] : 0;
       return (int)(((unsigned)hv << 5) | (unsigned)c);
     };
     S.q = qload(0);
     if (lane == 0) S.diag = bnd[0];
-    uint2 *dmrow = DM ? (uint2 *)(dm + (int64_t)strip * P.sblocks * kRows) + lane : nullptr;
+    // kDpSets word (strip, block b, plane p, lane k, row half h):
+    //   (strip * sblocks + b) * 192 + p * 64 + 2k + h
+    // kDpChoice word (strip, block b, lane k, row half h, step half e):
+    //   (strip * sblocks + b) * 128 + 4k + 2h + e
+    uint32_t *dmrow = MODE == kDpCost ? nullptr
+                    : dm + (int64_t)strip * P.sblocks * kWords +
+                          (MODE == kDpSets ? 2 * lane : 4 * lane);
     for (int s0 = 0; s0 < Spad; s0 += kStepBlock) {
       const int qn = (s0 + kStepBlock < Spad) ? qload(s0 + kStepBlock) : 0;
-      uint2 *dmw = DM ? dmrow + (s0 >> 3) * kLanes : nullptr;
+      uint32_t *dmw = MODE == kDpCost ? nullptr : dmrow + (s0 / kStepBlock) * kWords;
       const int vbA = s0 - lowerA, vbB = s0 - lowerB;
       if (last) {
-        lin_block<DM, true, true>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
-                                  sfinB - s0, dmw, lane);
+        lin_block<MODE, true, true>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
+                                    sfinB - s0, dmw, lane);
       } else if (s0 >= all_lo && s0 + kStepBlock <= all_hi) {
-        lin_block<DM, false, false>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1, dmw,
-                                    lane);
+        lin_block<MODE, false, false>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
+                                      dmw, lane);
       } else {
-        lin_block<DM, true, false>(S, trowA, trowB, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1, dmw,
-                                   lane);
+        lin_block<MODE, true, false>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
+                                     dmw, lane);
       }
       const int x = s0 + lane - (kLag * 31 + 1);
-      if (x >= 0 && x < wd) bnd[x] = S.q >> 5;
+      if (x >= 0 && x < wd) bnd[x] = (int)((unsigned)S.q >> 5);
       S.q = qn;
     }
     __syncwarp();
   }
   const int src = (r_last % kRows) >> 1;
   const int result = __shfl_sync(kFull, S.result, src);
-  if (lane == 0) A.cost[id] = result;
+  if (lane == 0) A.cost[id] = (result - bias) / kScale;
 }
 
-template <bool DM>
-__global__ void __launch_bounds__(256, 4) k_lin_dp(LinDpArgs A) {
-  __shared__ int2 tab[1024];  // {cost[a][b], cost[gap][b]}
-  for (int i = threadIdx.x; i < 1024; i += blockDim.x) {
-    const uint32_t p = A.tables->packed[i];
-    tab[i] = make_int2((int)(p & 0xffffu), (int)(p >> 16));
+template <int MODE>
+__global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
+  __shared__ LinSmem sm;
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x)
+    sm.ctab[(i >> 5) * 33 + (i & 31)] = A.tables->packed[i] & 0xffffu;
+  if (threadIdx.x < 32) {
+    const int g = (int)(A.tables->packed[threadIdx.x] >> 16);
+    sm.gcost[0][threadIdx.x] = g;
+    sm.gcost[1][threadIdx.x] = 4 * g + 1;
+    sm.gcost[2][threadIdx.x] = 4 * g + 2;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t *prof = &sm.prof[warp][0][lane];
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int *bnd = A.scratch + gw * A.slab;
   for (;;) {
@@ -290,7 +376,7 @@ __global__ void __launch_bounds__(256, 4) k_lin_dp(LinDpArgs A) {
       if (lane == 0) A.cost[id] = 0;
       continue;
     }
-    lin_pair<DM>(A, tab, P, DM ? A.dm_off[id] : 0, id, bnd, lane);
+    lin_pair<MODE>(A, sm, prof, P, MODE != kDpCost ? A.dm_off[id] : 0, id, bnd, lane);
   }
 }
 
@@ -325,9 +411,10 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
   // backtrack priority (algn.c:3605-3666): the caller's first argument is
   // the rows sequence unless the pair was swapped
   const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
+  const int mode = A.mode;
   int r = P.l1 - 1, j = L2 - 1;
   int64_t n = 0, nm = 0;
-  const int spad = sb * 8;
+  const int spad = sb * kStepBlock;
   bool bad = false;
   while ((int64_t)r * L2 + j >= 0) {
     const int k = (r & (kRows - 1)) >> 1, strip = r / kRows;
@@ -336,11 +423,25 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
       bad = true;
       break;
     }
-    const uint32_t w = dm[((int64_t)strip * sb + (s >> 3)) * kRows + (r & (kRows - 1))];
-    const uint32_t f = (w >> (4 * (7 - (s & 7)))) & 15u;
+    const int64_t blk = (int64_t)strip * sb + s / kStepBlock;
+    int move;  // 0 align, 1 insert (s2 against a gap), 2 delete
+    if (mode == kDpChoice) {
+      // 2-bit rank per step, 16 steps per word; step s of a word is bits
+      // 2*(15 - s%16); rank 1 is insert when swaped, else delete
+      const uint32_t w = dm[blk * (2 * kRows) + 2 * (r & (kRows - 1)) + ((s & 31) >> 4)];
+      const uint32_t code = (w >> (2 * (15 - (s & 15)))) & 3u;
+      move = code == 0 ? 0 : (((code == 1u) == swaped) ? 1 : 2);
+    } else {
+      // three bit planes (align, insert, delete); step s of a block is bit 31 - s%32
+      const uint32_t *w = dm + blk * (3 * kRows) + (r & (kRows - 1));
+      const int sh = 31 - (s & 31);
+      const uint32_t f = ((w[0] >> sh) & 1u) | (((w[kRows] >> sh) & 1u) << 1) |
+                         (((w[2 * kRows] >> sh) & 1u) << 2);
+      move = (f & 1u) ? 0 : ((swaped ? (f & 2u) : !(f & 4u)) ? 1 : 2);
+    }
     int cr, cc;
-    if (f & 1u) { cr = s1[r]; cc = s2[j]; --r; --j; }
-    else if (swaped ? (f & 2u) : !(f & 4u)) { cr = gap; cc = s2[j]; --j; }
+    if (move == 0) { cr = s1[r]; cc = s2[j]; --r; --j; }
+    else if (move == 1) { cr = gap; cc = s2[j]; --j; }
     else { cr = s1[r]; cc = gap; --r; }
     const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
     const int m = med[(ca << 5) | cb];
@@ -365,24 +466,27 @@ void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st) {
   k_lin_plan<<<(unsigned)blocks, threads, 0, st>>>(A);
 }
 
-int lin_dp_blocks(bool dm) {
-  static int cache[2][64] = {};
+int lin_dp_blocks(int mode) {
+  static int cache[3][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  int &c = cache[dm ? 1 : 0][dev & 63];
+  int &c = cache[mode][dev & 63];
   if (!c) {
     int per_sm = 0, sms = 0;
-    if (dm) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<true>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<false>, 256, 0);
+    const int t = kDpWarps * 32;
+    if (mode == kDpSets) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpSets>, t, 0);
+    else if (mode == kDpChoice) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpChoice>, t, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpCost>, t, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
   return c;
 }
 
-void launch_lin_dp(const LinDpArgs &A, bool dm, int blocks, cudaStream_t st) {
-  if (dm) k_lin_dp<true><<<blocks, 256, 0, st>>>(A);
-  else k_lin_dp<false><<<blocks, 256, 0, st>>>(A);
+void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st) {
+  if (mode == kDpSets) k_lin_dp<kDpSets><<<blocks, kDpWarps * 32, 0, st>>>(A);
+  else if (mode == kDpChoice) k_lin_dp<kDpChoice><<<blocks, kDpWarps * 32, 0, st>>>(A);
+  else k_lin_dp<kDpCost><<<blocks, kDpWarps * 32, 0, st>>>(A);
 }
 
 void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st) {

@@ -17,7 +17,7 @@ struct LinPlanArgs {
   const int32_t *deltaw;
   int gap;
   int maxc;
-  int with_dm;
+  int with_dm;  // kDpCost, kDpSets or kDpChoice: sizes the direction matrix
   int dos_empty;
   LinPlan *plans;
   int64_t *dm_words;
@@ -39,6 +39,7 @@ struct LinDpArgs {
   int64_t slab;   // ints per slab
   uint32_t *dm;
   int32_t *cost;
+  int swaped;  // kDpChoice priority: -1 derives it from the orientation
 };
 
 struct LinTbArgs {
@@ -53,11 +54,12 @@ struct LinTbArgs {
   const int64_t *out_off;
   int32_t *out_len;
   int swaped;  // -1: derive from the orientation, else backtrack_2d's flag
+  int mode;    // kDpSets or kDpChoice: how the direction matrix was written
 };
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
-int lin_dp_blocks(bool dm);
-void launch_lin_dp(const LinDpArgs &A, bool dm, int blocks, cudaStream_t st);
+int lin_dp_blocks(int mode);
+void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st);
 void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st);
 
 }  // namespace poyd

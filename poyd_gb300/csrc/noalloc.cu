@@ -35,7 +35,7 @@ namespace {
 
 constexpr int kNaMaxPairs = 65536;
 constexpr int kNaSlabInts = 2048;   // per-warp boundary row: wd <= 1984
-constexpr int kNaWarps = 2432;      // persistent warps (304 blocks of 8)
+constexpr int kNaWarps = 2432;      // persistent warps (304 blocks of kDpWarps = 8)
 constexpr size_t kNaHeader = 256;   // counter + error flags
 constexpr size_t kNaTables = (sizeof(DevTables) + 255) / 256 * 256;
 constexpr size_t kNaPlans = sizeof(LinPlan) * (size_t)kNaMaxPairs;
@@ -71,7 +71,7 @@ int na_scratch(unsigned char **out) {
 // Rejects plans whose band would overflow a fixed per-warp slab.
 __global__ void k_na_check(const int32_t *wd, int n, int limit, int32_t *err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && wd[i] > limit) atomicOr(err, 4);
+  if (i < n && wd[i] > limit) atomicOr(err, 8);
 }
 
 int na_check_cm(const poyd_cm *cm, int *maxc) {
@@ -158,15 +158,16 @@ extern "C" int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uin
   NA_CK(cudaStreamSynchronize(st));
   if (herr & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
   if (herr & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
-  if (herr & 4)
+  if (herr & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
+  if (herr & 8)
     return fail(POYD_ERANGE, "a band is wider than the %d diagonals the fixed scratch holds",
                 kNaSlabInts - 64);
 
   LinDpArgs DA;
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = nullptr; DA.order = nullptr;
   DA.tables = tabs; DA.gap = cm->gap; DA.counter = counter; DA.scratch = slabs;
-  DA.slab = kNaSlabInts; DA.dm = nullptr; DA.cost = cost;
-  launch_lin_dp(DA, false, kNaWarps / 8, st);
+  DA.slab = kNaSlabInts; DA.dm = nullptr; DA.cost = cost; DA.swaped = -1;
+  launch_lin_dp(DA, kDpCost, kNaWarps / kDpWarps, st);
   NA_CK(cudaGetLastError());
   return POYD_OK;
 }

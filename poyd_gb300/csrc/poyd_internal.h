@@ -18,7 +18,15 @@ constexpr int kMaxCost = 1 << 24;
 constexpr int kLanes = 32;      // lanes per pair
 constexpr int kRows = 64;       // rows per strip: two per lane
 constexpr int kLag = 3;         // steps between consecutive lanes
-constexpr int kStepBlock = 32;  // steps per queue block
+constexpr int kStepBlock = 32;  // steps per queue block and per direction word
+constexpr int kDpWarps = 8;     // warps per k_lin_dp block
+// k_lin_dp modes: costs only; full direction sets; backtrack moves (values x4)
+constexpr int kDpCost = 0, kDpSets = 1, kDpChoice = 2;
+constexpr int kInfChoice = 3 << 25;  // out-of-band value of kDpChoice (x4 scale)
+// direction-matrix words per (strip, 32-step block) of each mode
+__host__ __device__ constexpr int lin_dm_words(int mode) {
+  return mode == kDpSets ? 3 * kRows : (mode == kDpChoice ? 2 * kRows : 0);
+}
 
 // Per-pair plan of the linear banded DP, produced on the device.
 struct LinPlan {
@@ -27,8 +35,8 @@ struct LinPlan {
   int32_t l1, l2;          // rows / columns lengths
   int32_t dlo, wd;         // band diagonals [dlo, dlo + wd)
   int32_t swap;            // 1: rows are the caller's b
-  int32_t nstrips;         // ceil(l1 / 32)
-  int32_t sblocks;         // 8-step DM words per lane per strip
+  int32_t nstrips;         // ceil(l1 / 64)
+  int32_t sblocks;         // 32-step blocks per strip
   int32_t deltaw;          // width extension used
   int32_t empty;           // DOS.median empty rule: 1 = a empty, 2 = b empty
   int32_t pad_;

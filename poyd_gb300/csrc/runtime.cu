@@ -151,7 +151,11 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   LinPlanArgs PA;
   PA.n = n; PA.seq = seq; PA.a_off = a_off; PA.a_len = a_len; PA.b_off = b_off; PA.b_len = b_len;
   PA.policy = policy; PA.deltaw = deltaw; PA.gap = cm->gap; PA.maxc = maxc;
-  PA.with_dm = want_align; PA.dos_empty = (flags & POYD_FLAG_DOS_EMPTY) ? 1 : 0;
+  // The batched align_2 knows backtrack_2d's priority before the fill and
+  // keeps only the chosen moves (values x4 must fit the 16-bit profile); the
+  // single-pair protocol (out == nullptr) keeps the full direction sets.
+  const int mode = !want_align ? kDpCost : ((out && maxc < 16384) ? kDpChoice : kDpSets);
+  PA.with_dm = mode; PA.dos_empty = (flags & POYD_FLAG_DOS_EMPTY) ? 1 : 0;
   PA.plans = plans; PA.dm_words = dmw; PA.wd_out = wdb; PA.cells = cells; PA.err = err;
   { ProfScope ps("lin_plan", st); launch_lin_plan(PA, st); }
   CK(cudaGetLastError());
@@ -165,6 +169,7 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   CK(cudaStreamSynchronize(st));
   if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
   if (hwd[n] & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
+  if (hwd[n] & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
   std::vector<int64_t> off((size_t)n);
   int64_t total = 0;
   int maxwd = 1;
@@ -191,21 +196,21 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     if (!dm) return fail(POYD_ENOMEM, "direction matrix allocation (%lld bytes) failed",
                          (long long)(total * 4));
   }
-  const int blocks = lin_dp_blocks(want_align);
+  const int blocks = lin_dp_blocks(mode);
   const int64_t slab = maxwd + 64;
-  int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * 8);
+  int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * kDpWarps);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
   LinDpArgs DA;
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
   DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
-  DA.cost = cost;
-  { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, want_align, blocks, st); }
+  DA.cost = cost; DA.swaped = -1;
+  { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
   CK(cudaGetLastError());
   if (want_align && out) {  // out == nullptr: keep the DM for a later backtrack
     LinTbArgs TA;
     TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
     TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
-    TA.swaped = -1;
+    TA.swaped = -1; TA.mode = mode;
     { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
     CK(cudaGetLastError());
   }
@@ -368,6 +373,7 @@ extern "C" int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8
   TA.out_off = ooff;
   TA.out_len = olen;
   TA.swaped = swaped ? 1 : 0;
+  TA.mode = kDpSets;
   {
     ProfScope ps("lin_traceback", mat->st);
     launch_lin_traceback(TA, mat->st);

@@ -129,3 +129,21 @@ def test_full_size_properties():
     for i in range(0, 48, 12):
         c, ra, rb = O.align_2(A[i], B[i], om)
         assert res[i]["cost"] == c and np.array_equal(res[i]["a"], ra)
+
+
+def test_codes_above_31_rejected():
+    """Element codes index 32-entry table rows: wider codes are refused before
+    any DP launch (linear and affine)."""
+    from poyd_gb300 import native
+    rng = np.random.default_rng(9)
+    a = synth.with_gap(synth.random_dna(rng, 50))
+    b = synth.with_gap(synth.random_dna(rng, 50))
+    b[10] = 40
+    batch = align.PairBatch.from_host([a], [b])
+    for cm in (align.CostMatrix.dna(1, 2), align.CostMatrix.dna(1, 2, gap_opening=3)):
+        with pytest.raises(native.PoydError):
+            align.cost_2(batch, cm)
+        with pytest.raises(native.PoydError):
+            align.align_2(batch, cm)
+    ok = align.PairBatch.from_host([a], [synth.with_gap(synth.random_dna(rng, 50))])
+    assert int(align.cost_2(ok, align.CostMatrix.dna(1, 2))[0].item()) >= 0
