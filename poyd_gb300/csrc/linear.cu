@@ -5,23 +5,26 @@
 // algn.c:461-620, plus backtrack_2d (algn.c:3551-3666), ancestor_2
 // (algn.c:4126-4147) and median_2_with_gaps (algn.c:4011-4024).
 //
-// Layout on the GPU.  One warp owns one pair.  Lane k owns DP row
-// r = 32*strip + k of a 32-row strip; the warp sweeps the band in diagonal
-// coordinates d = j - r, which makes the band edges of every row the same
-// two diagonals [dlo, dlo+wd) (the reference's ukk left/right cells).  Lane
-// k handles diagonal d at step s = d - dlo + 2k: the value of row r-1 at
-// (d+1) -- the "delete" predecessor -- arrives from lane k-1 by one shuffle
-// that also carries the column character s2[r+d]; the previous shuffle's
-// value is the "align" predecessor and the lane's own previous value is the
-// "insert" predecessor.  Lane 0 is fed the previous strip's last row from a
-// register queue that rotates one lane per step and is refilled / flushed
-// with one coalesced 128-byte load / store every 32 steps (the boundary row
-// lives in a per-warp global scratch slab of wd ints).  Cells outside the
-// band or the matrix hold kInf, which removes exactly the moves the
-// reference's edge cells omit.  The direction set of every cell (ALIGN 1,
-// INSERT 2, DELETE 4; matrices.h:22-27) is packed 8 cells per 32-bit word
-// and stored with one coalesced store per 8 steps; the traceback addresses
-// it by (strip, step/8, lane).
+// Layout on the GPU.  One warp owns one pair (persistent grid, pairs taken
+// longest-first).  Lane k owns DP rows r0 + 2k and r0 + 2k + 1 of a 64-row
+// strip; the warp sweeps the band in diagonal coordinates d = j - r, which
+// makes the band edges of every row the same two diagonals [dlo, dlo+wd)
+// (the reference's ukk left/right cells).  Lane k handles diagonal d of its
+// first row at step s = d - dlo + 3k and d - 1 of its second row in the same
+// step: the value of the row above at (d+1) -- the "delete" predecessor --
+// arrives from lane k-1 by one shuffle that also carries the column
+// character; the previous shuffle's value is the "align" predecessor and the
+// lane's own previous value the "insert" predecessor.  Lane 0 is fed the
+// previous strip's last row from a register queue that rotates one lane per
+// step and is refilled / flushed with one coalesced 128-byte load / store
+// every 32 steps (the boundary row lives in a per-warp global slab of wd
+// ints).  Cells outside the band or the matrix hold an out-of-band value
+// that removes exactly the moves the reference's edge cells omit.  Costs come
+// from a per-lane profile in shared memory (both row characters' costs
+// against every column character in one word, laid out [char][lane] so a
+// step's 32 lookups hit 32 banks).  Direction information is written per
+// 32-step block with one coalesced store (see the mode notes below); the
+// traceback addresses it by (strip, block, lane).
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "poyd_internal.h"
@@ -132,6 +135,139 @@ __global__ void k_lin_plan(LinPlanArgs A) {
 }
 
 // ---------------------------------------------------------------------------
+// Writes a sequence backwards (the reference's seq_prepend order), collecting
+// bytes in a register and storing whole aligned 4-byte words; only a word
+// that the sequence covers in part (its two ends) is written byte by byte.
+// ---------------------------------------------------------------------------
+struct BackWriter {
+  uint8_t *p;     // next position (moves down)
+  uint32_t buf;   // pending bytes; the last one written in the low byte
+  int pend;
+  __device__ explicit BackWriter(uint8_t *top) : p(top), buf(0), pend(0) {}
+  __device__ __forceinline__ void put(uint32_t v) {
+    buf = (buf << 8) | v;
+    ++pend;
+    if (((uintptr_t)p & 3u) == 0) {  // p is the lowest byte of its word
+      if (pend == 4) *(uint32_t *)p = buf;
+      else
+        for (int i = 0; i < pend; ++i) p[i] = (uint8_t)(buf >> (8 * i));
+      pend = 0;
+    }
+    --p;
+  }
+  __device__ __forceinline__ void flush() {  // bytes at p+1 .. p+pend
+    for (int i = 0; i < pend; ++i) p[1 + i] = (uint8_t)(buf >> (8 * i));
+    pend = 0;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Traceback + medians of one pair by one thread.  Run by k_lin_traceback
+// (one thread per pair) or, for batched align_2, inside k_lin_dp by the warp
+// that finishes the last DP of a 32-pair batch (one lane per pair).
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int id) {
+  const LinPlan P = A.plans[id];
+  const int gap = A.gap;
+  const int la = P.swap ? P.l2 : P.l1, lb = P.swap ? P.l1 : P.l2;
+  const int64_t cap = (int64_t)la + lb + 2;
+  uint8_t *oa = A.out + A.out_off[id];
+  uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
+  const uint8_t *s1 = A.seq + P.s1_off, *s2 = A.seq + P.s2_off;
+  if (P.empty) {
+    // DOS.median: the non-empty (or second) sequence is the median.
+    const bool a_empty = P.empty == 1;
+    const uint8_t *src = (a_empty != (bool)P.swap) ? s2 : s1;  // caller's b if a empty
+    const int len = a_empty ? lb : la;
+    for (int i = 0; i < len; ++i) om[cap - len + i] = src[i];
+    A.out_len[2 * id] = 0;
+    A.out_len[2 * id + 1] = len;
+    return;
+  }
+  const uint32_t *dm = A.dm + A.dm_off[id];
+  const int L2 = P.l2, dlo = P.dlo, sb = P.sblocks;
+  // backtrack priority (algn.c:3605-3666): the caller's first argument is
+  // the rows sequence unless the pair was swapped
+  const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
+  const int mode = A.mode;
+  int r = P.l1 - 1, j = L2 - 1;
+  int n = 0, nm = 0;
+  const int spad = sb * kStepBlock;
+  bool bad = false;
+  // kDpChoice: the four words of one (block, lane) -- both rows of the lane,
+  // 32 steps -- form one 16-byte group; the walk keeps the current group
+  // (eight lanes' groups share a 128-byte line, so the next ones are
+  // usually L1 hits).
+  const uint4 *dm4 = (const uint4 *)dm;
+  uint4 cur = make_uint4(0, 0, 0, 0);
+  int cur_key = -1;
+  BackWriter wa(oa + cap - 1), wb(ob + cap - 1), ww(ow + cap - 1), wm(om + cap - 1);
+  // cell (r, j) ends the walk once r * L2 + j < 0
+  while (r > 0 || (r == 0 && j >= 0)) {
+    const int k = (r & (kRows - 1)) >> 1, strip = r >> 6;
+    const int s = (j - r) - dlo + kLag * k + (r & 1);
+    if (j < 0 || s < 0 || s >= spad || n + 2 >= cap) {  // left the band: a bug
+      bad = true;
+      break;
+    }
+    const int blk = strip * sb + (s >> 5);
+    int move;  // 0 align, 1 insert (s2 against a gap), 2 delete
+    if (mode == kDpChoice) {
+      const int key = blk * kLanes + k;
+      if (key != cur_key) {
+        cur = dm4[key];
+        cur_key = key;
+      }
+      // 2-bit rank per step, 16 steps per word (row A: x, y; row B: z, w);
+      // step s of a word is bits 2*(15 - s%16); rank 1 is insert when
+      // swaped, else delete
+      const uint32_t lo = (r & 1) ? cur.z : cur.x, hi = (r & 1) ? cur.w : cur.y;
+      const uint32_t w = (s & 16) ? hi : lo;
+      const uint32_t code = (w >> (30 - 2 * (s & 15))) & 3u;
+      move = code == 0 ? 0 : (((code == 1u) == swaped) ? 1 : 2);
+    } else {
+      // three bit planes (align, insert, delete); step s of a block is bit 31 - s%32
+      const uint32_t *w = dm + (int64_t)blk * (3 * kRows) + (r & (kRows - 1));
+      const int sh = 31 - (s & 31);
+      const uint32_t f = ((w[0] >> sh) & 1u) | (((w[kRows] >> sh) & 1u) << 1) |
+                         (((w[2 * kRows] >> sh) & 1u) << 2);
+      move = (f & 1u) ? 0 : ((swaped ? (f & 2u) : !(f & 4u)) ? 1 : 2);
+    }
+    const bool dr = move != 1, dj = move != 2;  // consumes a row / a column
+    const int cr = dr ? (int)s1[r] : gap, cc = dj ? (int)s2[j] : gap;
+    r -= dr;
+    j -= dj;
+    const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
+    const int m = med[(ca << 5) | cb];
+    wa.put((uint32_t)ca);
+    wb.put((uint32_t)cb);
+    ww.put((uint32_t)m);
+    if (m != gap) {
+      wm.put((uint32_t)m);
+      ++nm;
+    }
+    ++n;
+  }
+  // ancestor_2 ends with the leading gap (algn.c:4140-4141)
+  wm.put((uint32_t)gap);
+  ++nm;
+  wa.flush();
+  wb.flush();
+  ww.flush();
+  wm.flush();
+  A.out_len[2 * id] = bad ? -1 : (int32_t)n;
+  A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
+}
+
+__global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
+  __shared__ uint8_t med[1024];
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) med[i] = A.tables->median[i];
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < A.n) tb_pair(A, med, A.order ? A.order[t] : t);
+}
+
+// ---------------------------------------------------------------------------
 // Band DP.
 //
 // Three modes share one sweep:
@@ -162,6 +298,7 @@ struct LinSmem {
   uint32_t ctab[32 * 33];               // cost[a][b] at a*33 + b (rows padded one bank)
   int gcost[3][32];                     // cost[gap][b]; 4*cost[gap][b] + 1; ... + 2
   uint32_t prof[kDpWarps][32][kLanes];  // per lane: cost[aA][c] | cost[aB][c] << 16 (x4 in kDpChoice)
+  uint8_t med[1024];                    // median table (fused traceback)
 };
 
 template <int MODE>
@@ -353,6 +490,8 @@ __global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
   __shared__ LinSmem sm;
   for (int i = threadIdx.x; i < 1024; i += blockDim.x)
     sm.ctab[(i >> 5) * 33 + (i & 31)] = A.tables->packed[i] & 0xffffu;
+  if (MODE == kDpChoice && A.fuse_tb)
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) sm.med[i] = A.tables->median[i];
   if (threadIdx.x < 32) {
     const int g = (int)(A.tables->packed[threadIdx.x] >> 16);
     sm.gcost[0][threadIdx.x] = g;
@@ -374,87 +513,27 @@ __global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
     const LinPlan P = A.plans[id];
     if (P.empty) {
       if (lane == 0) A.cost[id] = 0;
-      continue;
-    }
-    lin_pair<MODE>(A, sm, prof, P, MODE != kDpCost ? A.dm_off[id] : 0, id, bnd, lane);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Traceback + medians: one thread per pair.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
-  __shared__ uint8_t med[1024];
-  for (int i = threadIdx.x; i < 1024; i += blockDim.x) med[i] = A.tables->median[i];
-  __syncthreads();
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= A.n) return;
-  const LinPlan P = A.plans[id];
-  const int gap = A.gap;
-  const int la = P.swap ? P.l2 : P.l1, lb = P.swap ? P.l1 : P.l2;
-  const int64_t cap = (int64_t)la + lb + 2;
-  uint8_t *oa = A.out + A.out_off[id];
-  uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
-  const uint8_t *s1 = A.seq + P.s1_off, *s2 = A.seq + P.s2_off;
-  if (P.empty) {
-    // DOS.median: the non-empty (or second) sequence is the median.
-    const bool a_empty = P.empty == 1;
-    const uint8_t *src = (a_empty != (bool)P.swap) ? s2 : s1;  // caller's b if a empty
-    const int len = a_empty ? lb : la;
-    for (int i = 0; i < len; ++i) om[cap - len + i] = src[i];
-    A.out_len[2 * id] = 0;
-    A.out_len[2 * id + 1] = len;
-    return;
-  }
-  const uint32_t *dm = A.dm + A.dm_off[id];
-  const int L2 = P.l2, dlo = P.dlo, sb = P.sblocks;
-  // backtrack priority (algn.c:3605-3666): the caller's first argument is
-  // the rows sequence unless the pair was swapped
-  const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
-  const int mode = A.mode;
-  int r = P.l1 - 1, j = L2 - 1;
-  int64_t n = 0, nm = 0;
-  const int spad = sb * kStepBlock;
-  bool bad = false;
-  while ((int64_t)r * L2 + j >= 0) {
-    const int k = (r & (kRows - 1)) >> 1, strip = r / kRows;
-    const int s = (j - r) - dlo + kLag * k + (r & 1);
-    if (r < 0 || j < 0 || s < 0 || s >= spad || n + 2 >= cap) {  // left the band: a bug
-      bad = true;
-      break;
-    }
-    const int64_t blk = (int64_t)strip * sb + s / kStepBlock;
-    int move;  // 0 align, 1 insert (s2 against a gap), 2 delete
-    if (mode == kDpChoice) {
-      // 2-bit rank per step, 16 steps per word; step s of a word is bits
-      // 2*(15 - s%16); rank 1 is insert when swaped, else delete
-      const uint32_t w = dm[blk * (2 * kRows) + 2 * (r & (kRows - 1)) + ((s & 31) >> 4)];
-      const uint32_t code = (w >> (2 * (15 - (s & 15)))) & 3u;
-      move = code == 0 ? 0 : (((code == 1u) == swaped) ? 1 : 2);
     } else {
-      // three bit planes (align, insert, delete); step s of a block is bit 31 - s%32
-      const uint32_t *w = dm + blk * (3 * kRows) + (r & (kRows - 1));
-      const int sh = 31 - (s & 31);
-      const uint32_t f = ((w[0] >> sh) & 1u) | (((w[kRows] >> sh) & 1u) << 1) |
-                         (((w[2 * kRows] >> sh) & 1u) << 2);
-      move = (f & 1u) ? 0 : ((swaped ? (f & 2u) : !(f & 4u)) ? 1 : 2);
+      lin_pair<MODE>(A, sm, prof, P, MODE != kDpCost ? A.dm_off[id] : 0, id, bnd, lane);
     }
-    int cr, cc;
-    if (move == 0) { cr = s1[r]; cc = s2[j]; --r; --j; }
-    else if (move == 1) { cr = gap; cc = s2[j]; --j; }
-    else { cr = s1[r]; cc = gap; --r; }
-    const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
-    const int m = med[(ca << 5) | cb];
-    oa[cap - 1 - n] = (uint8_t)ca;
-    ob[cap - 1 - n] = (uint8_t)cb;
-    ow[cap - 1 - n] = (uint8_t)m;
-    if (m != gap) om[cap - 1 - nm++] = (uint8_t)m;
-    ++n;
+    if (MODE == kDpChoice && A.fuse_tb) {
+      // Publish this pair's direction matrix; the warp completing the batch
+      // (no waiting: the count tells) walks all of its pairs, one per lane.
+      __syncwarp();
+      const int b = p / kLanes;
+      const int size = min(kLanes, A.n - b * kLanes);
+      int last = 0;
+      if (lane == 0) {
+        __threadfence();
+        last = atomicAdd(A.batch_done + b, 1) == size - 1;
+      }
+      if (__shfl_sync(kFull, last, 0)) {
+        __threadfence();
+        if (lane < size) tb_pair(A.tb, sm.med, A.order ? A.order[b * kLanes + lane] : b * kLanes + lane);
+        __syncwarp();
+      }
+    }
   }
-  // ancestor_2 ends with the leading gap (algn.c:4140-4141)
-  om[cap - 1 - nm++] = (uint8_t)gap;
-  A.out_len[2 * id] = bad ? -1 : (int32_t)n;
-  A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
 }
 
 // ---------------------------------------------------------------------------

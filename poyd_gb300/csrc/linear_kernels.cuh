@@ -26,6 +26,22 @@ struct LinPlanArgs {
   int32_t *err;
 };
 
+struct LinTbArgs {
+  int n;
+  const uint8_t *seq;
+  const LinPlan *plans;
+  const int64_t *dm_off;
+  const uint32_t *dm;
+  const DevTables *tables;
+  int gap;
+  uint8_t *out;
+  const int64_t *out_off;
+  int32_t *out_len;
+  int swaped;  // -1: derive from the orientation, else backtrack_2d's flag
+  int mode;    // kDpSets or kDpChoice: how the direction matrix was written
+  const int32_t *order;  // k_lin_traceback: thread t walks pair order[t] (nullable)
+};
+
 struct LinDpArgs {
   int n;
   const uint8_t *seq;
@@ -40,21 +56,12 @@ struct LinDpArgs {
   uint32_t *dm;
   int32_t *cost;
   int swaped;  // kDpChoice priority: -1 derives it from the orientation
-};
-
-struct LinTbArgs {
-  int n;
-  const uint8_t *seq;
-  const LinPlan *plans;
-  const int64_t *dm_off;
-  const uint32_t *dm;
-  const DevTables *tables;
-  int gap;
-  uint8_t *out;
-  const int64_t *out_off;
-  int32_t *out_len;
-  int swaped;  // -1: derive from the orientation, else backtrack_2d's flag
-  int mode;    // kDpSets or kDpChoice: how the direction matrix was written
+  // kDpChoice with fuse_tb: the warp finishing the last DP of 32 consecutive
+  // pairs (order positions 32b..32b+31, counted in batch_done[b]) runs their
+  // traceback with `tb`
+  int fuse_tb;
+  int *batch_done;
+  LinTbArgs tb;
 };
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);

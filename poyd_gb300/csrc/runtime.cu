@@ -200,17 +200,28 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   const int64_t slab = maxwd + 64;
   int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * kDpWarps);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
+  LinTbArgs TA;
+  TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
+  TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+  TA.swaped = -1; TA.mode = mode; TA.order = dord;
+  // Batched align_2 with backtrack moves: the traceback runs inside the DP
+  // kernel, batch by batch as their fills complete.
+  const bool fuse = want_align && out && mode == kDpChoice;
+  int *batch_done = nullptr;
+  if (fuse) {
+    const size_t nb = ((size_t)n + kLanes - 1) / kLanes;
+    batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * nb);
+    if (!batch_done) return fail(POYD_ENOMEM, "batch counter allocation failed");
+    CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * nb, st));
+  }
   LinDpArgs DA;
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
   DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
   DA.cost = cost; DA.swaped = -1;
+  DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA;
   { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
   CK(cudaGetLastError());
-  if (want_align && out) {  // out == nullptr: keep the DM for a later backtrack
-    LinTbArgs TA;
-    TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
-    TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
-    TA.swaped = -1; TA.mode = mode;
+  if (want_align && out && !fuse) {  // out == nullptr: keep the DM for a later backtrack
     { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
     CK(cudaGetLastError());
   }
@@ -374,6 +385,7 @@ extern "C" int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8
   TA.out_len = olen;
   TA.swaped = swaped ? 1 : 0;
   TA.mode = kDpSets;
+  TA.order = nullptr;
   {
     ProfScope ps("lin_traceback", mat->st);
     launch_lin_traceback(TA, mat->st);
