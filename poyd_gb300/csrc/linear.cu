@@ -307,6 +307,23 @@ struct DpMode {
   static constexpr int kInfV = MODE == kDpChoice ? kInfChoice : kInf;
 };
 
+// Integer work of the DP splits over two pipes that issue side by side, each
+// at half a warp instruction per clock: min / select / logic / shifts run on
+// the ALU pipe, while the adds, the field extraction and the packing are
+// issued as multiply-adds (IMAD on the FMA pipe) through imad().  The
+// multipliers are kernel arguments (DpK: 1, 4, 32, 128, -65536), so the
+// compiler cannot fold them back into ALU adds and shifts.
+__device__ __forceinline__ int imad(int a, int b, int c) {
+  int d;
+  asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+
 // Appends one direction bit: (plane << 1) | [cand == h].  h is the minimum
 // of the candidates, so cand - h - 1 is negative exactly when cand == h.
 __device__ __forceinline__ uint32_t dir_bit(uint32_t plane, int cand, int h) {
@@ -321,6 +338,7 @@ __device__ __forceinline__ uint32_t dir_bit(uint32_t plane, int cand, int h) {
 // outside its band); CAP records the final cell (last strip only).
 template <int MODE, bool MASK, bool CAP>
 __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, const int *gcost,
+                                          uint32_t ps, uint32_t gs, const DpK &K,
                                           int cDA, int cDB, int vbA, int cntA, int vbB, int cntB,
                                           int finA, int finB, uint32_t *dmw, int lane) {
   constexpr int kInfV = DpMode<MODE>::kInfV;
@@ -330,11 +348,11 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, con
     if (lane == 0) up = S.q;
     S.q = __shfl_sync(kFull, S.q, (lane + 1) & 31);
     const int c = up & 31;
-    const int hup = (int)((unsigned)up >> 5);
-    const uint32_t pr = prof[c * kLanes];  // {cost[aA][c], cost[aB][c]}
-    const int g = gcost[c];                // cost[gap][c] (+ rank)
     int ha, hb;
     if (MODE == kDpSets) {
+      const int hup = (int)((unsigned)up >> 5);
+      const uint32_t pr = prof[c * kLanes];  // {cost[aA][c], cost[aB][c]}
+      const int g = gcost[c];                // cost[gap][c]
       // row A: delete from the lane above, align from its previous value
       const int Av = S.diag + (int)(pr & 0xffffu);
       const int Dv = hup + cDA;
@@ -353,29 +371,45 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, con
       S.b0 = dir_bit(S.b0, Av2, hb);
       S.b1 = dir_bit(S.b1, Iv2, hb);
       S.b2 = dir_bit(S.b2, Dv2, hb);
+      if (CAP) {
+        if (u == finA) S.result = ha;
+        if (u == finB) S.result = hb;
+      }
+      S.Pk = (int)(((unsigned)hb << 5) | (unsigned)c);
+      S.diag = hup;
     } else {
-      ha = __viaddmin_s32(hup, cDA, __viaddmin_s32(S.HA, g, S.diag + (int)(pr & 0xffffu)));
+      const int hup = (int)((unsigned)up >> 5);
+      const uint32_t pr = lds32((uint32_t)imad(c, K.k128, (int)ps));  // {cost[aA][c], cost[aB][c]}
+      const int g = (int)lds32((uint32_t)imad(c, K.four, (int)gs));  // cost[gap][c] (+ rank)
+      const int hi = (int)(pr >> 16);                             // cost[aB][c]
+      // row A: delete from the lane above, align from its previous value
+      const int Av = imad(hi, K.m64k, imad((int)pr, K.one, S.diag));
+      const int Iv = imad(g, K.one, S.HA);
+      ha = __viaddmin_s32(hup, cDA, min(Av, Iv));
       if (MODE == kDpChoice) {
-        if (u < 16) S.a0 = (S.a0 << 2) | ((uint32_t)ha & 3u);
-        else S.a1 = (S.a1 << 2) | ((uint32_t)ha & 3u);
+        if (u < 16) S.a0 = (uint32_t)imad((int)S.a0, K.four, ha & 3);
+        else S.a1 = (uint32_t)imad((int)S.a1, K.four, ha & 3);
         ha &= ~3;
       }
       if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
-      hb = __viaddmin_s32(ha, cDB, __viaddmin_s32(S.HB, g, S.HA + (int)(pr >> 16)));
+      // row B: delete from row A now, align from row A's previous value
+      const int Av2 = imad(hi, K.one, S.HA);
+      const int Iv2 = imad(g, K.one, S.HB);
+      hb = __viaddmin_s32(ha, cDB, min(Av2, Iv2));
       if (MODE == kDpChoice) {
-        if (u < 16) S.b0 = (S.b0 << 2) | ((uint32_t)hb & 3u);
-        else S.b1 = (S.b1 << 2) | ((uint32_t)hb & 3u);
+        if (u < 16) S.b0 = (uint32_t)imad((int)S.b0, K.four, hb & 3);
+        else S.b1 = (uint32_t)imad((int)S.b1, K.four, hb & 3);
         hb &= ~3;
       }
       if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
+      if (CAP) {
+        if (u == finA) S.result = ha;
+        if (u == finB) S.result = hb;
+      }
+      S.Pk = imad(hb, K.k32, c);
+      S.diag = hup;
     }
-    if (CAP) {
-      if (u == finA) S.result = ha;
-      if (u == finB) S.result = hb;
-    }
-    S.Pk = (int)(((unsigned)hb << 5) | (unsigned)c);
     if (lane == 31) S.q = S.Pk;
-    S.diag = hup;
     S.HA = ha;
     S.HB = hb;
   }
@@ -404,6 +438,9 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const LinSmem &sm, 
   const int rank_i = MODE == kDpChoice ? (swaped ? 1 : 2) : 0;
   const int rank_d = MODE == kDpChoice ? 3 - rank_i : 0;
   const int *gcost = sm.gcost[rank_i];
+  // shared-memory byte addresses of this lane's profile column and of gcost
+  const uint32_t ps = (uint32_t)__cvta_generic_to_shared(prof);
+  const uint32_t gs = (uint32_t)__cvta_generic_to_shared(gcost);
   const int bias = kScale * (int)sm.ctab[s1[0] * 33 + s2[0]];
 
   for (int x = lane; x < wd; x += 32) bnd[x] = (x == -dlo) ? 0 : kInfV;
@@ -465,13 +502,13 @@ __device__ __forceinline__ void lin_pair(const LinDpArgs &A, const LinSmem &sm, 
       uint32_t *dmw = MODE == kDpCost ? nullptr : dmrow + (s0 / kStepBlock) * kWords;
       const int vbA = s0 - lowerA, vbB = s0 - lowerB;
       if (last) {
-        lin_block<MODE, true, true>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
+        lin_block<MODE, true, true>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
                                     sfinB - s0, dmw, lane);
       } else if (s0 >= all_lo && s0 + kStepBlock <= all_hi) {
-        lin_block<MODE, false, false>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
+        lin_block<MODE, false, false>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
                                       dmw, lane);
       } else {
-        lin_block<MODE, true, false>(S, prof, gcost, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
+        lin_block<MODE, true, false>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
                                      dmw, lane);
       }
       const int x = s0 + lane - (kLag * 31 + 1);

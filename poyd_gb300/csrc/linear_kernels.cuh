@@ -42,6 +42,12 @@ struct LinTbArgs {
   const int32_t *order;  // k_lin_traceback: thread t walks pair order[t] (nullable)
 };
 
+// Runtime multipliers of the DP's multiply-add arithmetic (see linear.cu).
+struct DpK {
+  int one, four, k32, k128, m64k;
+};
+inline DpK dp_constants() { return DpK{1, 4, 32, 128, -65536}; }
+
 struct LinDpArgs {
   int n;
   const uint8_t *seq;
@@ -62,6 +68,7 @@ struct LinDpArgs {
   int fuse_tb;
   int *batch_done;
   LinTbArgs tb;
+  DpK k;  // multiplier constants (1, 4, 32, 128, -65536)
 };
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);

@@ -178,11 +178,23 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     if (want_align) total += hw[i];
     maxwd = std::max(maxwd, hwd[i]);
   }
-  std::vector<int32_t> order((size_t)n);
-  std::iota(order.begin(), order.end(), 0);
-  // longest first: dm_words ~ strips * (wd + 62) is the band area
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t x, int32_t y) { return hw[x] > hw[y]; });
+  // Longest first (dm_words ~ strips x band steps is the band area): a
+  // stable two-pass radix sort on a descending 24-bit key, linear in n.
+  std::vector<int32_t> order((size_t)n), tmp((size_t)n);
+  std::vector<uint32_t> key((size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    const int64_t q = std::min<int64_t>(hw[i] >> 7, (1 << 24) - 1);  // multiples of 128
+    key[i] = (uint32_t)((1 << 24) - 1 - q);
+    tmp[i] = i;
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    const int sh = 12 * pass;
+    std::vector<int32_t> cnt((1 << 12) + 1, 0);
+    for (int32_t i = 0; i < n; ++i) ++cnt[((key[tmp[i]] >> sh) & 4095) + 1];
+    for (int b = 0; b < (1 << 12); ++b) cnt[b + 1] += cnt[b];
+    for (int32_t i = 0; i < n; ++i) order[cnt[(key[tmp[i]] >> sh) & 4095]++] = tmp[i];
+    if (pass == 0) std::swap(order, tmp);
+  }
   int64_t *doff = dmw + n;
   int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
   int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
@@ -218,7 +230,7 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
   DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
   DA.cost = cost; DA.swaped = -1;
-  DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA;
+  DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
   { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
   CK(cudaGetLastError());
   if (want_align && out && !fuse) {  // out == nullptr: keep the DM for a later backtrack
