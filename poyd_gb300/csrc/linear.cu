@@ -311,7 +311,7 @@ struct DpMode {
 // at half a warp instruction per clock: min / select / logic / shifts run on
 // the ALU pipe, while the adds, the field extraction and the packing are
 // issued as multiply-adds (IMAD on the FMA pipe) through imad().  The
-// multipliers are kernel arguments (DpK: 1, 4, 32, 128, -65536), so the
+// multipliers are kernel arguments (DpK: 1, -1, 4, 32, 128, -65536), so the
 // compiler cannot fold them back into ALU adds and shifts.
 __device__ __forceinline__ int imad(int a, int b, int c) {
   int d;
@@ -387,9 +387,11 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, con
       const int Iv = imad(g, K.one, S.HA);
       ha = __viaddmin_s32(hup, cDA, min(Av, Iv));
       if (MODE == kDpChoice) {
-        if (u < 16) S.a0 = (uint32_t)imad((int)S.a0, K.four, ha & 3);
-        else S.a1 = (uint32_t)imad((int)S.a1, K.four, ha & 3);
-        ha &= ~3;
+        // acc * 4 + (ha & 3) as acc * 4 + ha - (ha & ~3), exact mod 2^32
+        const int hc = ha & ~3;
+        if (u < 16) S.a0 = (uint32_t)imad(hc, K.m1, imad((int)S.a0, K.four, ha));
+        else S.a1 = (uint32_t)imad(hc, K.m1, imad((int)S.a1, K.four, ha));
+        ha = hc;
       }
       if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
       // row B: delete from row A now, align from row A's previous value
@@ -397,9 +399,10 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, con
       const int Iv2 = imad(g, K.one, S.HB);
       hb = __viaddmin_s32(ha, cDB, min(Av2, Iv2));
       if (MODE == kDpChoice) {
-        if (u < 16) S.b0 = (uint32_t)imad((int)S.b0, K.four, hb & 3);
-        else S.b1 = (uint32_t)imad((int)S.b1, K.four, hb & 3);
-        hb &= ~3;
+        const int hc = hb & ~3;
+        if (u < 16) S.b0 = (uint32_t)imad(hc, K.m1, imad((int)S.b0, K.four, hb));
+        else S.b1 = (uint32_t)imad(hc, K.m1, imad((int)S.b1, K.four, hb));
+        hb = hc;
       }
       if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
       if (CAP) {
