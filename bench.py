@@ -35,7 +35,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "align_2 GCUPS (bit-exact)"
 UNIT = "GCUPS"
-OPS_PER_CELL = {"linear": 8, "affine": 24}  # see DESIGN.md "Roofline"
+# Algorithmic integer ops per band cell: linear 3 adds + 2 mins + 3 direction
+# compares; affine 24 for its four-state recurrence (algn.c:1740-1977).
+OPS_PER_CELL = {"linear": 8, "affine": 24}
 
 
 def parse():
@@ -324,7 +326,9 @@ def run_ours(args):
                          "unit": "Gop/s", "frac": achieved / peak_gops if peak_gops else None,
                          "traffic": traffic, "kernel": kname,
                          "ops_per_cell": OPS_PER_CELL[args.model],
-                         "peak_source": "measured (poyd_int32_peak microbenchmark)"},
+                         "peak_source": "measured (poyd_int32_peak: fused add-min on the ALU "
+                                        "pipe interleaved with multiply-add adds on the FMA pipe)",
+                         "peak_alu_pipe_only": native.int_pipe_rate(0)},
             "clocks": clk.summary(),
             "e2e": e2e,
         }

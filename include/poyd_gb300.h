@@ -247,13 +247,17 @@ int poyd_to_bf16(const float *x, void *y, int64_t n, void *stream);
  * bracketed by CUDA events on its own stream; poyd_profile_read sums the
  * recorded durations of kernels named `name` (NULL = all) in ms and
  * returns how many launches matched.  poyd_launch_count counts every
- * kernel launch since load.  poyd_int32_peak measures the device's
- * achievable INT32 add+min issue rate (Gop/s), the denominator of the DP
- * roofline.
+ * kernel launch since load.  poyd_int_pipe_rate measures integer issue
+ * (Gop/s) with independent chains: mode 0 fused add-min (2 ops per
+ * instruction, ALU pipe), mode 1 adds issued as multiply-adds (1 op, FMA
+ * pipe), mode 2 the two interleaved (both pipes).  poyd_int32_peak is
+ * mode 2, the denominator of the DP roofline: the DP issues its mins and
+ * logic on the ALU pipe and its adds on the FMA pipe.
  * ------------------------------------------------------------------- */
 int poyd_profile_enable(int on);
 int poyd_profile_read(const char *name, double *ms_total, int clear);
 long long poyd_launch_count(void);
+int poyd_int_pipe_rate(int mode, double *gops, double *ms);
 int poyd_int32_peak(double *gops, double *ms);
 
 #ifdef __cplusplus

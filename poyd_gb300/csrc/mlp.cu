@@ -1,6 +1,6 @@
 // Kernels of the learned join proposal: a 32-256-256-128-1 ReLU MLP with
 // BF16 weights and activations and FP32 accumulation (no counterpart in the
-// reference).
+// reference; it orders the candidate joins of a search pass).
 //
 // k_gemm: C = op(A) op(B) (+ bias, ReLU) on tensor cores through inline PTX
 // mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32.  A warp owns a 16x32

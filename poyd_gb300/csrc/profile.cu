@@ -1,8 +1,8 @@
 // Launch accounting for the benchmark: while enabled, every kernel the
 // library launches is bracketed by CUDA events recorded on its own stream,
 // so per-kernel device time inside a timed region can be read back without
-// a profiler.  Also an INT32-issue microbenchmark that measures the
-// achievable integer add/min rate used as the DP roofline denominator.
+// a profiler.  Also integer-issue microbenchmarks; the two-pipe one is the
+// DP roofline denominator.
 #include <cuda_runtime.h>
 #include <cstring>
 #include <mutex>
@@ -45,21 +45,68 @@ void prof_end(void *token, cudaStream_t st) {
   delete e;
 }
 
-// INT32 issue benchmark: independent add+min chains, 8 per thread.
-__global__ void k_int32_peak(int *out, int iters, int seed) {
-  int a0 = threadIdx.x + seed, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
-  int a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+// Integer issue benchmarks, 8 independent chains per thread.  The DP issues
+// on two integer pipes: min / logic / fused add-min on the ALU pipe and
+// multiply-adds on the FMA pipe, each at half a warp instruction per clock.
+//   MODE 0: fused add-min,            2 ops per instruction (ALU pipe);
+//   MODE 1: add as a multiply-add,    1 op per instruction (FMA pipe);
+//   MODE 2: the two interleaved 1:1,  1.5 ops per instruction (both pipes).
+template <int MODE>
+__global__ void k_int_rate(int *out, int iters, int seed, int one) {
+  int a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = threadIdx.x + seed + i;
   const int b = seed | 1, c = 1 << 29;
 #pragma unroll 1
-  for (int i = 0; i < iters; ++i) {
+  for (int it = 0; it < iters; ++it) {
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      a0 = min(a0 + b, c); a1 = min(a1 + b, c); a2 = min(a2 + b, c); a3 = min(a3 + b, c);
-      a4 = min(a4 + b, c); a5 = min(a5 + b, c); a6 = min(a6 + b, c); a7 = min(a7 + b, c);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const bool fma = MODE == 1 || (MODE == 2 && (i & 1));
+        if (fma) {
+          int d;
+          asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a[i]), "r"(one), "r"(b));
+          a[i] = d;
+        } else {
+          a[i] = __viaddmin_s32(a[i], b, c);
+        }
+      }
     }
   }
-  const int r = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+  int r = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) r ^= a[i];
   if (r == 0x7fffffff) out[0] = r;  // keeps the chains live
+}
+
+template <int MODE>
+static int int_rate(double *gops, double *ms) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int *out = nullptr;
+  if (cudaMalloc(&out, 16) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaMalloc");
+  const int threads = 1024, blocks = sms * 2, iters = 2048;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  k_int_rate<MODE><<<blocks, threads>>>(out, 32, 3, 1);
+  cudaEventRecord(a);
+  k_int_rate<MODE><<<blocks, threads>>>(out, iters, 5, 1);
+  cudaEventRecord(b);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "integer rate kernel");
+  const double per_instr = MODE == 0 ? 2.0 : (MODE == 1 ? 1.0 : 1.5);
+  const double ops = (double)blocks * threads * iters * 16.0 * 8.0 * per_instr;
+  if (gops) *gops = ops / (t * 1e-3) / 1e9;
+  if (ms) *ms = t;
+  return POYD_OK;
 }
 
 }  // namespace poyd
@@ -109,30 +156,11 @@ extern "C" int poyd_profile_read(const char *name, double *ms_total, int clear) 
   return cnt;
 }
 
-extern "C" int poyd_int32_peak(double *gops, double *ms) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int *out = nullptr;
-  if (cudaMalloc(&out, 16) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaMalloc");
-  const int threads = 1024, blocks = sms * 2, iters = 4096;
-  cudaEvent_t a, b;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
-  k_int32_peak<<<blocks, threads>>>(out, 64, 3);
-  cudaEventRecord(a);
-  k_int32_peak<<<blocks, threads>>>(out, iters, 5);
-  cudaEventRecord(b);
-  cudaError_t e = cudaEventSynchronize(b);
-  float t = 0;
-  cudaEventElapsedTime(&t, a, b);
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  cudaFree(out);
-  if (e != cudaSuccess) return cuda_fail(e, "int32 peak kernel");
-  // 16 unrolled x 8 chains x 2 ops (add, min) per iteration per thread
-  const double ops = (double)blocks * threads * iters * 16.0 * 8.0 * 2.0;
-  if (gops) *gops = ops / (t * 1e-3) / 1e9;
-  if (ms) *ms = t;
-  return POYD_OK;
+extern "C" int poyd_int_pipe_rate(int mode, double *gops, double *ms) {
+  if (mode == 0) return int_rate<0>(gops, ms);
+  if (mode == 1) return int_rate<1>(gops, ms);
+  if (mode == 2) return int_rate<2>(gops, ms);
+  return fail(POYD_EINVAL, "poyd_int_pipe_rate: mode must be 0, 1 or 2");
 }
+
+extern "C" int poyd_int32_peak(double *gops, double *ms) { return int_rate<2>(gops, ms); }

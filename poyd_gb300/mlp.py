@@ -1,7 +1,7 @@
 """The join-proposal MLP (32-256-256-128-1, ReLU) on the project's own BF16
 tensor-core kernels (csrc/mlp.cu): forward, backward and Adam, with FP32
 master weights and FP32 accumulation.  No reference counterpart: this is
-the learned proposal of the candidate search."""
+the learned proposal that orders the candidate joins of a search pass."""
 from __future__ import annotations
 
 import ctypes as C

@@ -55,6 +55,7 @@ SIGNATURES = [
     ("poyd_profile_read", C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int]),
     ("poyd_launch_count", C.c_longlong, []),
     ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("poyd_int_pipe_rate", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 
 
@@ -66,9 +67,19 @@ def profile_read(name=None, clear=True):
 
 
 def int32_peak():
-    """Measured INT32 add+min issue rate in Gop/s."""
+    """Measured integer issue rate in Gop/s over both integer pipes (fused
+    add-min on the ALU pipe interleaved with multiply-add adds on the FMA
+    pipe): the denominator of the DP roofline."""
     g, ms = C.c_double(), C.c_double()
     check(lib().poyd_int32_peak(C.byref(g), C.byref(ms)))
+    return g.value
+
+
+def int_pipe_rate(mode):
+    """Integer issue rate in Gop/s: 0 fused add-min (ALU pipe), 1 multiply-add
+    adds (FMA pipe), 2 both interleaved."""
+    g, ms = C.c_double(), C.c_double()
+    check(lib().poyd_int_pipe_rate(int(mode), C.byref(g), C.byref(ms)))
     return g.value
 
 _lib = None

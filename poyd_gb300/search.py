@@ -1,8 +1,8 @@
 """Candidate-pass driver: Wagner build and SPR passes whose every candidate
 join is scored in one batch on the device.
 
-This is the caller side of the hot path (SURVEY 8(f) "search-loop
-integration").  The reference evaluates one candidate per call from
+This is the caller side of the hot path (the search-loop integration of
+the batched scorer).  The reference evaluates one candidate per call from
 ``single_spr_round`` (ptree.ml:1120-1176) and ``make_wagner_tree``
 (ptree.ml:941-1030) through ``AllDirChar.cost_fn`` -> ``Node.distance``
 (node.ml:914-947); here the candidates of a whole pass are collected and
