@@ -112,20 +112,20 @@ __global__ void k_lin_plan(LinPlanArgs A) {
     P.dlo = dlo; P.wd = wd;
     P.swap = swap;
     P.nstrips = (l1 + kRows - 1) / kRows;
-    const int S = wd + kLag * (kLanes - 1) + 1;
-    const int Spad = (S + kStepBlock - 1) / kStepBlock * kStepBlock;
-    P.sblocks = Spad / kStepBlock;
+    // strip period W (see the DP schedule) and the pair's 32-step blocks
+    int W = (wd + 2 + kStepBlock - 1) / kStepBlock * kStepBlock;
+    if (W < kMinPeriod) W = kMinPeriod;
+    P.sblocks = W / kStepBlock;
+    P.nblk = ((P.nstrips - 1) * W + kLag * (kLanes - 1) + 1 + wd + kStepBlock - 1) / kStepBlock;
     P.deltaw = dw;
     P.empty = 0;
     if (A.dos_empty) {
       if (na == 0) P.empty = 1;
       else if (nb == 0) P.empty = 2;
     }
-    P.pad_ = 0;
     A.plans[id] = P;
     // direction-matrix words; also the work estimate used to order pairs
-    A.dm_words[id] = (int64_t)P.nstrips * P.sblocks *
-                     lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
+    A.dm_words[id] = (int64_t)P.nblk * lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
     A.wd_out[id] = wd;
     if (A.cells) A.cells[id] = cells;
     if (la < 1 || lb < 1) atomicOr(A.err, 1);
@@ -192,7 +192,7 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   const int mode = A.mode;
   int r = P.l1 - 1, j = L2 - 1;
   int n = 0, nm = 0;
-  const int spad = sb * kStepBlock;
+  const int wdt = P.wd;
   bool bad = false;
   // kDpChoice: the four words of one (block, lane) -- both rows of the lane,
   // 32 steps -- form one 16-byte group; the walk keeps the current group
@@ -206,11 +206,12 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   while (r > 0 || (r == 0 && j >= 0)) {
     const int k = (r & (kRows - 1)) >> 1, strip = r >> 6;
     const int s = (j - r) - dlo + kLag * k + (r & 1);
-    if (j < 0 || s < 0 || s >= spad || n + 2 >= cap) {  // left the band: a bug
+    const int blk = strip * sb + (s >> 5);  // global step strip * W + s
+    const int bi = (j - r) - dlo;           // band index
+    if (j < 0 || bi < 0 || bi >= wdt || blk >= P.nblk || n + 2 >= cap) {  // left the band: a bug
       bad = true;
       break;
     }
-    const int blk = strip * sb + (s >> 5);
     int move;  // 0 align, 1 insert (s2 against a gap), 2 delete
     if (mode == kDpChoice) {
       const int key = blk * kLanes + k;
@@ -285,6 +286,21 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
 // Every value is biased by cost[s1[0]][s2[0]] (cell (0,0) holds it instead
 // of 0) so that all values stay non-negative; the bias is removed from the
 // result.
+//
+// Schedule.  Lane k works on its rows 64t + 2k and 64t + 2k + 1 of strip t
+// during the steps [tW + 3k, tW + 3k + W) of the pair, strip after strip
+// with no pipeline ramp in between; at step tW + 3k + i its first row is at
+// band index i (diagonal dlo + i) and its second row at index i - 1.
+// W = max(roundup32(wd + 2), 160): the two padding diagonals put a lane's
+// last steps of a strip out of band (the values it receives there from a
+// lane that has moved on are never used), and 160 steps leave two blocks
+// between lane 31's flush of a boundary value and lane 0's prefetch of it.
+// In the 32-step block at offset o of period t (steps tW + o .. tW + o + 31)
+// lane k switches from strip t-1 to strip t at step 3k - o when o < 96;
+// from o = 96 on every lane is in strip t and the next strip's profile and
+// parameters are prepared.  Column characters do not travel with the
+// values: each block stages, per strip present, the 64 columns its lanes
+// read in a per-warp window (lane k reads window[32 + u - k] at step u).
 // ---------------------------------------------------------------------------
 struct LinStrip {
   int HA, HB, diag, Pk, q;
@@ -293,12 +309,21 @@ struct LinStrip {
   int result;
 };
 
-// Shared memory of one k_lin_dp block.
+// Per-lane parameters of one strip.
+struct StripParams {
+  int baseA, cntA;  // first row valid at steps [baseA, baseA + cntA)
+  int baseB, cntB;  // second row likewise
+  int cDA, cDB;     // delete costs of the two row characters (+ rank)
+  const uint32_t *col;  // this lane's profile column
+};
+
+// Shared memory of one k_lin_dp block (dynamic: above the 48 KB static limit).
 struct LinSmem {
-  uint32_t ctab[32 * 33];               // cost[a][b] at a*33 + b (rows padded one bank)
-  int gcost[3][32];                     // cost[gap][b]; 4*cost[gap][b] + 1; ... + 2
-  uint32_t prof[kDpWarps][32][kLanes];  // per lane: cost[aA][c] | cost[aB][c] << 16 (x4 in kDpChoice)
-  uint8_t med[1024];                    // median table (fused traceback)
+  uint32_t ctab[32 * 33];                  // cost[a][b] at a*33 + b (rows padded one bank)
+  int gcost[3][32];                        // cost[gap][b]; 4*cost[gap][b] + 1; ... + 2
+  uint32_t prof[kDpWarps][2][32][kLanes];  // by strip parity, per lane: cost[aA][c] | cost[aB][c] << 16 (x4 in kDpChoice)
+  uint8_t win[kDpWarps][2][64];            // column windows of a block: strip t, strip t-1
+  uint8_t med[1024];                       // median table (fused traceback)
 };
 
 template <int MODE>
@@ -318,11 +343,6 @@ __device__ __forceinline__ int imad(int a, int b, int c) {
   asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
   return d;
 }
-__device__ __forceinline__ uint32_t lds32(uint32_t addr) {
-  uint32_t v;
-  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
-  return v;
-}
 
 // Appends one direction bit: (plane << 1) | [cand == h].  h is the minimum
 // of the candidates, so cand - h - 1 is negative exactly when cand == h.
@@ -330,91 +350,140 @@ __device__ __forceinline__ uint32_t dir_bit(uint32_t plane, int cand, int h) {
   return __funnelshift_l((uint32_t)(cand - h - 1), plane, 1);
 }
 
-// 32 steps of one strip.  Each lane owns two rows: row A = r0 + 2k handles
-// diagonal d at step s = d - dlo + 3k, row B = row A + 1 handles d - 1 in
-// the same step, so row B's delete predecessor is row A's value computed
-// just before and both cells use the same column character.  MASK applies
-// the per-row band/matrix validity (needed only in blocks where some row is
-// outside its band); CAP records the final cell (last strip only).
-template <int MODE, bool MASK, bool CAP>
-__device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, const int *gcost,
-                                          uint32_t ps, uint32_t gs, const DpK &K,
-                                          int cDA, int cDB, int vbA, int cntA, int vbB, int cntB,
-                                          int finA, int finB, uint32_t *dmw, int lane) {
+// This lane's parameters of strip s (cnt 0 outside 0 <= s < T); builds its
+// profile column when asked.
+template <int MODE>
+__device__ __forceinline__ StripParams strip_params(const LinSmem &sm, uint32_t *col,
+                                                    const uint8_t *s1, int L1, int T, int s,
+                                                    int W, int dlo, int wd, int gap, int rank_d,
+                                                    bool build, int lane) {
+  constexpr int kScale = DpMode<MODE>::kScale;
+  StripParams p;
+  const int rA = s * kRows + 2 * lane, rB = rA + 1;
+  const bool in = s >= 0 && s < T;
+  const bool okA = in && rA < L1, okB = in && rB < L1;
+  const int aA = okA ? s1[rA] : 0, aB = okB ? s1[rB] : 0;
+  if (build) {
+    // read back only by this lane: no warp synchronisation needed
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c)
+      col[c * kLanes] = kScale * (sm.ctab[aA * 33 + c] | (sm.ctab[aB * 33 + c] << 16));
+  }
+  p.cDA = kScale * (int)sm.ctab[aA * 33 + gap] + rank_d;
+  p.cDB = kScale * (int)sm.ctab[aB * 33 + gap] + rank_d;
+  const int offA = (-dlo - rA) > 0 ? (-dlo - rA) : 0;
+  const int offB = (-dlo - rB) > 0 ? (-dlo - rB) : 0;
+  p.baseA = s * W + kLag * lane + offA;
+  p.cntA = okA ? wd - offA : 0;
+  p.baseB = s * W + kLag * lane + 1 + offB;
+  p.cntB = okB ? wd - offB : 0;
+  p.col = col;
+  return p;
+}
+
+// 32 steps of one block, as two runs of 16 unrolled steps (the code of the
+// block variants stays small enough for the instruction cache).  KIND 0:
+// every lane in strip t and inside its band for all steps; KIND 2: lane k
+// uses strip t-1 (parameters Pp, window wp) before step uc and strip t (Pc,
+// window wc) from it, with per-step band masks (uc = 0, Pp = Pc for a
+// masked block inside one strip).  Each lane owns two rows: the first
+// handles index i at a step, the second index i - 1 in the same step, so the
+// second row's delete predecessor is the first row's value computed just
+// before and both cells share the column character.  CAP records the final
+// cell.
+template <int MODE, int KIND, bool CAP>
+__device__ __forceinline__ void lin_block(LinStrip &S, const StripParams &Pc,
+                                          const StripParams &Pp, const uint8_t *wc,
+                                          const uint8_t *wp, int uc, int G0, const int *gcost,
+                                          const DpK &K, int finA, int finB, uint32_t *dmw,
+                                          int lane) {
   constexpr int kInfV = DpMode<MODE>::kInfV;
+  constexpr int kHalf = kStepBlock / 2;
+#pragma unroll 1
+  for (int e = 0; e < 2; ++e) {
+    const int u0 = e * kHalf;
+    const int vbAc = G0 + u0 - Pc.baseA, vbBc = G0 + u0 - Pc.baseB;
+    const int vbAp = G0 + u0 - Pp.baseA, vbBp = G0 + u0 - Pp.baseB;
+    const int ue = uc - u0, fA = finA - u0, fB = finB - u0;
+    const uint8_t *wce = wc + u0, *wpe = wp + u0;
+    uint32_t accA = 0, accB = 0;  // kDpChoice: 2-bit moves of this half
 #pragma unroll
-  for (int u = 0; u < kStepBlock; ++u) {
-    int up = __shfl_up_sync(kFull, S.Pk, 1);
-    if (lane == 0) up = S.q;
-    S.q = __shfl_sync(kFull, S.q, (lane + 1) & 31);
-    const int c = up & 31;
-    int ha, hb;
-    if (MODE == kDpSets) {
-      const int hup = (int)((unsigned)up >> 5);
-      const uint32_t pr = prof[c * kLanes];  // {cost[aA][c], cost[aB][c]}
-      const int g = gcost[c];                // cost[gap][c]
-      // row A: delete from the lane above, align from its previous value
-      const int Av = S.diag + (int)(pr & 0xffffu);
-      const int Dv = hup + cDA;
-      const int Iv = S.HA + g;
-      ha = min(min(Av, Dv), Iv);
-      if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
-      // row B: delete from row A now, align from row A's previous value
-      const int Av2 = S.HA + (int)(pr >> 16);
-      const int Dv2 = ha + cDB;
-      const int Iv2 = S.HB + g;
-      hb = min(min(Av2, Dv2), Iv2);
-      if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
-      S.a0 = dir_bit(S.a0, Av, ha);
-      S.a1 = dir_bit(S.a1, Iv, ha);
-      S.a2 = dir_bit(S.a2, Dv, ha);
-      S.b0 = dir_bit(S.b0, Av2, hb);
-      S.b1 = dir_bit(S.b1, Iv2, hb);
-      S.b2 = dir_bit(S.b2, Dv2, hb);
+    for (int v = 0; v < kHalf; ++v) {
+      int up = __shfl_up_sync(kFull, S.Pk, 1);
+      if (lane == 0) up = S.q;
+      S.q = __shfl_sync(kFull, S.q, (lane + 1) & 31);
+      const bool nw = KIND != 2 || v >= ue;
+      const int c = (nw ? wce : wpe)[v];
+      const uint32_t *pcol = nw ? Pc.col : Pp.col;
+      const int cDA = nw ? Pc.cDA : Pp.cDA, cDB = nw ? Pc.cDB : Pp.cDB;
+      bool okA = true, okB = true;
+      if (KIND == 2) {
+        okA = nw ? (unsigned)(vbAc + v) < (unsigned)Pc.cntA : (unsigned)(vbAp + v) < (unsigned)Pp.cntA;
+        okB = nw ? (unsigned)(vbBc + v) < (unsigned)Pc.cntB : (unsigned)(vbBp + v) < (unsigned)Pp.cntB;
+      }
+      const uint32_t pr = pcol[c * kLanes];  // {cost[aA][c], cost[aB][c]}
+      const int g = gcost[c];                // cost[gap][c] (+ rank)
+      int ha, hb;
+      if (MODE == kDpSets) {
+        // first row: delete from the lane above, align from its previous value
+        const int Av = S.diag + (int)(pr & 0xffffu);
+        const int Dv = up + cDA;
+        const int Iv = S.HA + g;
+        ha = min(min(Av, Dv), Iv);
+        if (KIND != 0) ha = okA ? ha : kInfV;
+        // second row: delete from the first row now, align from its previous value
+        const int Av2 = S.HA + (int)(pr >> 16);
+        const int Dv2 = ha + cDB;
+        const int Iv2 = S.HB + g;
+        hb = min(min(Av2, Dv2), Iv2);
+        if (KIND != 0) hb = okB ? hb : kInfV;
+        S.a0 = dir_bit(S.a0, Av, ha);
+        S.a1 = dir_bit(S.a1, Iv, ha);
+        S.a2 = dir_bit(S.a2, Dv, ha);
+        S.b0 = dir_bit(S.b0, Av2, hb);
+        S.b1 = dir_bit(S.b1, Iv2, hb);
+        S.b2 = dir_bit(S.b2, Dv2, hb);
+      } else {
+        const int hi = (int)(pr >> 16);  // cost[aB][c]
+        const int Av = imad(hi, K.m64k, imad((int)pr, K.one, S.diag));
+        const int Iv = imad(g, K.one, S.HA);
+        ha = __viaddmin_s32(up, cDA, min(Av, Iv));
+        if (MODE == kDpChoice) {
+          // acc * 4 + (ha & 3) as acc * 4 + ha - (ha & ~3), exact mod 2^32
+          const int hc = ha & ~3;
+          accA = (uint32_t)imad(hc, K.m1, imad((int)accA, K.four, ha));
+          ha = hc;
+        }
+        if (KIND != 0) ha = okA ? ha : kInfV;
+        const int Av2 = imad(hi, K.one, S.HA);
+        const int Iv2 = imad(g, K.one, S.HB);
+        hb = __viaddmin_s32(ha, cDB, min(Av2, Iv2));
+        if (MODE == kDpChoice) {
+          const int hc = hb & ~3;
+          accB = (uint32_t)imad(hc, K.m1, imad((int)accB, K.four, hb));
+          hb = hc;
+        }
+        if (KIND != 0) hb = okB ? hb : kInfV;
+      }
       if (CAP) {
-        if (u == finA) S.result = ha;
-        if (u == finB) S.result = hb;
+        if (v == fA) S.result = ha;
+        if (v == fB) S.result = hb;
       }
-      S.Pk = (int)(((unsigned)hb << 5) | (unsigned)c);
-      S.diag = hup;
-    } else {
-      const int hup = (int)((unsigned)up >> 5);
-      const uint32_t pr = lds32((uint32_t)imad(c, K.k128, (int)ps));  // {cost[aA][c], cost[aB][c]}
-      const int g = (int)lds32((uint32_t)imad(c, K.four, (int)gs));  // cost[gap][c] (+ rank)
-      const int hi = (int)(pr >> 16);                             // cost[aB][c]
-      // row A: delete from the lane above, align from its previous value
-      const int Av = imad(hi, K.m64k, imad((int)pr, K.one, S.diag));
-      const int Iv = imad(g, K.one, S.HA);
-      ha = __viaddmin_s32(hup, cDA, min(Av, Iv));
-      if (MODE == kDpChoice) {
-        // acc * 4 + (ha & 3) as acc * 4 + ha - (ha & ~3), exact mod 2^32
-        const int hc = ha & ~3;
-        if (u < 16) S.a0 = (uint32_t)imad(hc, K.m1, imad((int)S.a0, K.four, ha));
-        else S.a1 = (uint32_t)imad(hc, K.m1, imad((int)S.a1, K.four, ha));
-        ha = hc;
-      }
-      if (MASK) ha = ((unsigned)(vbA + u) < (unsigned)cntA) ? ha : kInfV;
-      // row B: delete from row A now, align from row A's previous value
-      const int Av2 = imad(hi, K.one, S.HA);
-      const int Iv2 = imad(g, K.one, S.HB);
-      hb = __viaddmin_s32(ha, cDB, min(Av2, Iv2));
-      if (MODE == kDpChoice) {
-        const int hc = hb & ~3;
-        if (u < 16) S.b0 = (uint32_t)imad(hc, K.m1, imad((int)S.b0, K.four, hb));
-        else S.b1 = (uint32_t)imad(hc, K.m1, imad((int)S.b1, K.four, hb));
-        hb = hc;
-      }
-      if (MASK) hb = ((unsigned)(vbB + u) < (unsigned)cntB) ? hb : kInfV;
-      if (CAP) {
-        if (u == finA) S.result = ha;
-        if (u == finB) S.result = hb;
-      }
-      S.Pk = imad(hb, K.k32, c);
-      S.diag = hup;
+      S.Pk = hb;
+      if (lane == 31) S.q = hb;
+      S.diag = up;
+      S.HA = ha;
+      S.HB = hb;
     }
-    if (lane == 31) S.q = S.Pk;
-    S.HA = ha;
-    S.HB = hb;
+    if (MODE == kDpChoice) {
+      if (e == 0) {
+        S.a0 = accA;
+        S.b0 = accB;
+      } else {
+        S.a1 = accA;
+        S.b1 = accB;
+      }
+    }
   }
   if (MODE == kDpSets) {
     uint2 *w = (uint2 *)dmw;
@@ -427,107 +496,148 @@ __device__ __forceinline__ void lin_block(LinStrip &S, const uint32_t *prof, con
 }
 
 template <int MODE>
-__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const LinSmem &sm, uint32_t *prof,
+__device__ __forceinline__ void lin_pair(const LinDpArgs &A, const LinSmem &sm, int warp,
                                          const LinPlan &P, int64_t dm_off, int id, int *bnd,
                                          int lane) {
   constexpr int kScale = DpMode<MODE>::kScale, kInfV = DpMode<MODE>::kInfV;
-  constexpr int kWords = lin_dm_words(MODE);  // DM words per (strip, 32-step block)
+  constexpr int kWords = lin_dm_words(MODE);  // DM words per 32-step block
   const uint8_t *s1 = A.seq + P.s1_off;
   const uint8_t *s2 = A.seq + P.s2_off;
   const int L1 = P.l1, L2 = P.l2, dlo = P.dlo, wd = P.wd;
+  const int T = P.nstrips, W = P.sblocks * kStepBlock, nblk = P.nblk;
   const int gap = A.gap;
   // backtrack priority (algn.c:3605-3666): insert before delete when swaped
   const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
   const int rank_i = MODE == kDpChoice ? (swaped ? 1 : 2) : 0;
   const int rank_d = MODE == kDpChoice ? 3 - rank_i : 0;
   const int *gcost = sm.gcost[rank_i];
-  // shared-memory byte addresses of this lane's profile column and of gcost
-  const uint32_t ps = (uint32_t)__cvta_generic_to_shared(prof);
-  const uint32_t gs = (uint32_t)__cvta_generic_to_shared(gcost);
+  uint32_t *col0 = const_cast<uint32_t *>(&sm.prof[warp][0][0][lane]);
+  uint32_t *col1 = const_cast<uint32_t *>(&sm.prof[warp][1][0][lane]);
+  uint8_t *win = const_cast<uint8_t *>(&sm.win[warp][0][0]);
+  // this lane's read position in the windows of strip t and strip t-1
+  const uint8_t *wc = win + 32 - lane, *wp = win + 64 + 32 - lane;
   const int bias = kScale * (int)sm.ctab[s1[0] * 33 + s2[0]];
 
   for (int x = lane; x < wd; x += 32) bnd[x] = (x == -dlo) ? 0 : kInfV;
   __syncwarp();
 
-  const int Spad = P.sblocks * kStepBlock;
-  const int r_last = L1 - 1;
-  const int d_last = L2 - L1;
+  // the final cell (L1-1, L2-1): owner lane, row and step
+  const int r_last = L1 - 1, d_last = L2 - L1;
+  const int kf = (r_last & (kRows - 1)) >> 1, hf = r_last & 1;
+  const int G_fin = (T - 1) * W + kLag * kf + (d_last - dlo) + hf;
   LinStrip S;
   S.result = 0;
+  S.HA = kInfV;
+  S.HB = kInfV;
+  S.diag = kInfV;
+  S.Pk = kInfV;
+  S.a0 = S.a1 = S.a2 = S.b0 = S.b1 = S.b2 = 0;
+  if (lane == 0) S.diag = bnd[0];
   uint32_t *dm = MODE != kDpCost ? A.dm + dm_off : nullptr;
 
-  for (int strip = 0; strip < P.nstrips; ++strip) {
-    const int r0 = strip * kRows;
-    const int rA = r0 + 2 * lane, rB = rA + 1;
-    const bool okA = rA < L1, okB = rB < L1;
-    const bool last = strip == P.nstrips - 1;
-    const int aA = okA ? s1[rA] : 0, aB = okB ? s1[rB] : 0;
-    // this lane's profile of its two row characters (read back only by the
-    // same lane: no warp synchronisation needed)
-#pragma unroll 8
-    for (int c = 0; c < 32; ++c)
-      prof[c * kLanes] = kScale * (sm.ctab[aA * 33 + c] | (sm.ctab[aB * 33 + c] << 16));
-    const int cDA = kScale * (int)sm.ctab[aA * 33 + gap] + rank_d;
-    const int cDB = kScale * (int)sm.ctab[aB * 33 + gap] + rank_d;
-    const int offA = (-dlo - rA) > 0 ? (-dlo - rA) : 0;
-    const int offB = (-dlo - rB) > 0 ? (-dlo - rB) : 0;
-    const int lowerA = kLag * lane + offA, lowerB = kLag * lane + 1 + offB;
-    const int cntA = okA ? wd - offA : 0, cntB = okB ? wd - offB : 0;
-    const int sfinA = (rA == r_last) ? (d_last - dlo + kLag * lane) : -1000000;
-    const int sfinB = (rB == r_last) ? (d_last - dlo + kLag * lane + 1) : -1000000;
-    // steps where both rows of every lane are inside their bands
-    const int lo = lowerA > lowerB ? lowerA : lowerB;
-    const int hi = (lowerA + cntA) < (lowerB + cntB) ? (lowerA + cntA) : (lowerB + cntB);
-    const int all_lo = (int)__reduce_max_sync(kFull, (unsigned)lo);
-    const int all_hi = (int)__reduce_min_sync(kFull, (unsigned)hi);
-    S.HA = kInfV;
-    S.HB = kInfV;
-    S.diag = kInfV;
-    S.Pk = (int)((unsigned)kInfV << 5);
-    auto qload = [&](int s0) -> int {
-      const int x = s0 + lane + 1;
-      const int hv = (x < wd) ? bnd[x] : kInfV;
-      const int j = r0 + dlo + s0 + lane;
-      const int c = (j >= 0 && j < L2) ? s2[j] : 0;
-      return (int)(((unsigned)hv << 5) | (unsigned)c);
-    };
-    S.q = qload(0);
-    if (lane == 0) S.diag = bnd[0];
-    // kDpSets word (strip, block b, plane p, lane k, row half h):
-    //   (strip * sblocks + b) * 192 + p * 64 + 2k + h
-    // kDpChoice word (strip, block b, lane k, row half h, step half e):
-    //   (strip * sblocks + b) * 128 + 4k + 2h + e
-    uint32_t *dmrow = MODE == kDpCost ? nullptr
-                    : dm + (int64_t)strip * P.sblocks * kWords +
-                          (MODE == kDpSets ? 2 * lane : 4 * lane);
-    for (int s0 = 0; s0 < Spad; s0 += kStepBlock) {
-      const int qn = (s0 + kStepBlock < Spad) ? qload(s0 + kStepBlock) : 0;
-      uint32_t *dmw = MODE == kDpCost ? nullptr : dmrow + (s0 / kStepBlock) * kWords;
-      const int vbA = s0 - lowerA, vbB = s0 - lowerB;
-      if (last) {
-        lin_block<MODE, true, true>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, sfinA - s0,
-                                    sfinB - s0, dmw, lane);
-      } else if (s0 >= all_lo && s0 + kStepBlock <= all_hi) {
-        lin_block<MODE, false, false>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
-                                      dmw, lane);
-      } else {
-        lin_block<MODE, true, false>(S, prof, gcost, ps, gs, A.k, cDA, cDB, vbA, cntA, vbB, cntB, -1, -1,
-                                     dmw, lane);
-      }
-      const int x = s0 + lane - (kLag * 31 + 1);
-      if (x >= 0 && x < wd) bnd[x] = (int)((unsigned)S.q >> 5);
-      S.q = qn;
-    }
+  StripParams Pp = strip_params<MODE>(sm, col1, s1, L1, T, -1, W, dlo, wd, gap, rank_d, false, lane);
+  StripParams Pc = strip_params<MODE>(sm, col0, s1, L1, T, 0, W, dlo, wd, gap, rank_d, true, lane);
+  StripParams Pn = Pp;
+  auto unmasked_range = [&](const StripParams &p, int &lo, int &hi) {
+    const int l = p.baseA > p.baseB ? p.baseA : p.baseB;
+    const int h = (p.baseA + p.cntA) < (p.baseB + p.cntB) ? (p.baseA + p.cntA) : (p.baseB + p.cntB);
+    lo = __reduce_max_sync(kFull, l);
+    hi = __reduce_min_sync(kFull, h);
+  };
+  int all_lo, all_hi;
+  unmasked_range(Pc, all_lo, all_hi);
+
+  // lane 0's inputs of a block: the row above its strip (the previous
+  // strip's last row, from the boundary slab) at index i + 1; index W reads
+  // slot 0, the new strip's first align predecessor
+  // (blocks are addressed by period t and offset o: G0 = t * W + o)
+  auto qload = [&](int o) -> int {
+    int x = o + lane + 1;
+    if (x == W) x = 0;
+    return (x < wd) ? bnd[x] : kInfV;
+  };
+  // this lane's two bytes of the column windows of the block at (t, o)
+  auto wload = [&](int t, int o, uint32_t &cw, uint32_t &pw) {
+    const int jc = t * kRows + dlo + o - 32 + lane;  // strip t
+    const int jp = jc - kRows + W;                   // strip t-1
+    const int c0 = (jc >= 0 && jc < L2) ? s2[jc] : 0;
+    const int c1 = (jc + 32 >= 0 && jc + 32 < L2) ? s2[jc + 32] : 0;
+    const int p0 = (jp >= 0 && jp < L2) ? s2[jp] : 0;
+    const int p1 = (jp + 32 >= 0 && jp + 32 < L2) ? s2[jp + 32] : 0;
+    cw = (uint32_t)c0 | ((uint32_t)c1 << 8);
+    pw = (uint32_t)p0 | ((uint32_t)p1 << 8);
+  };
+  auto wstore = [&](uint32_t cw, uint32_t pw) {
     __syncwarp();
+    win[lane] = (uint8_t)cw;
+    win[lane + 32] = (uint8_t)(cw >> 8);
+    win[64 + lane] = (uint8_t)pw;
+    win[64 + lane + 32] = (uint8_t)(pw >> 8);
+    __syncwarp();
+  };
+  S.q = qload(0);
+  {
+    uint32_t cw, pw;
+    wload(0, 0, cw, pw);
+    wstore(cw, pw);
   }
-  const int src = (r_last % kRows) >> 1;
-  const int result = __shfl_sync(kFull, S.result, src);
+
+  int t0 = 0, o = 0;
+  for (int b = 0; b < nblk; ++b, o += kStepBlock) {
+    if (o == W) {
+      o = 0;
+      ++t0;
+    }
+    const int G0 = b * kStepBlock;
+    if (b > 0 && o == 0) {  // a new period: strip t0 becomes current
+      Pp = Pc;
+      Pc = Pn;
+      unmasked_range(Pc, all_lo, all_hi);
+    }
+    if (o == 96)  // every lane is in strip t0: prepare strip t0 + 1
+      Pn = strip_params<MODE>(sm, ((t0 + 1) & 1) ? col1 : col0, s1, L1, T, t0 + 1, W, dlo, wd,
+                              gap, rank_d, t0 + 1 < T, lane);
+    const int o1 = (o + kStepBlock == W) ? 0 : o + kStepBlock;  // the next block
+    const int t1 = (o1 == 0) ? t0 + 1 : t0;
+    const int qn = qload(o1);
+    uint32_t cw, pw;
+    wload(t1, o1, cw, pw);
+    uint32_t *dmw = MODE == kDpCost ? nullptr
+                  : dm + (int64_t)b * kWords + (MODE == kDpSets ? 2 * lane : 4 * lane);
+    const bool cap = G_fin >= G0 && G_fin < G0 + kStepBlock;
+    const int finA = (cap && lane == kf && hf == 0) ? G_fin - G0 : -1;
+    const int finB = (cap && lane == kf && hf == 1) ? G_fin - G0 : -1;
+    if (o < 96) {
+      const int uc = kLag * lane - o;
+      if (cap)
+        lin_block<MODE, 2, true>(S, Pc, Pp, wc, wp, uc, G0, gcost, A.k, finA, finB, dmw, lane);
+      else
+        lin_block<MODE, 2, false>(S, Pc, Pp, wc, wp, uc, G0, gcost, A.k, -1, -1, dmw, lane);
+    } else if (cap) {
+      lin_block<MODE, 2, true>(S, Pc, Pc, wc, wc, 0, G0, gcost, A.k, finA, finB, dmw, lane);
+    } else if (G0 >= all_lo && G0 + kStepBlock <= all_hi) {
+      lin_block<MODE, 0, false>(S, Pc, Pc, wc, wc, 0, G0, gcost, A.k, -1, -1, dmw, lane);
+    } else {
+      lin_block<MODE, 2, false>(S, Pc, Pc, wc, wc, 0, G0, gcost, A.k, -1, -1, dmw, lane);
+    }
+    // lane 31's second-row values of this block (lane L holds step G0 + L)
+    // become the boundary row of the next strip
+    {
+      const int pA = G0 + lane - kLag * 31;  // lane 31's first-row position
+      const int x = (pA >= t0 * W ? pA - t0 * W : pA - (t0 - 1) * W) - 1;
+      if (pA >= 0 && x >= 0 && x < wd) bnd[x] = S.q;
+    }
+    S.q = qn;
+    wstore(cw, pw);
+  }
+  const int result = __shfl_sync(kFull, S.result, kf);
   if (lane == 0) A.cost[id] = (result - bias) / kScale;
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
-  __shared__ LinSmem sm;
+__global__ void __launch_bounds__(kDpWarps * 32, 3) k_lin_dp(LinDpArgs A) {
+  extern __shared__ __align__(16) unsigned char lin_dsm[];
+  LinSmem &sm = *reinterpret_cast<LinSmem *>(lin_dsm);
   for (int i = threadIdx.x; i < 1024; i += blockDim.x)
     sm.ctab[(i >> 5) * 33 + (i & 31)] = A.tables->packed[i] & 0xffffu;
   if (MODE == kDpChoice && A.fuse_tb)
@@ -541,7 +651,6 @@ __global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  uint32_t *prof = &sm.prof[warp][0][lane];
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int *bnd = A.scratch + gw * A.slab;
   for (;;) {
@@ -554,7 +663,7 @@ __global__ void __launch_bounds__(kDpWarps * 32, 4) k_lin_dp(LinDpArgs A) {
     if (P.empty) {
       if (lane == 0) A.cost[id] = 0;
     } else {
-      lin_pair<MODE>(A, sm, prof, P, MODE != kDpCost ? A.dm_off[id] : 0, id, bnd, lane);
+      lin_pair<MODE>(A, sm, warp, P, MODE != kDpCost ? A.dm_off[id] : 0, id, bnd, lane);
     }
     if (MODE == kDpChoice && A.fuse_tb) {
       // Publish this pair's direction matrix; the warp completing the batch
@@ -585,17 +694,35 @@ void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st) {
   k_lin_plan<<<(unsigned)blocks, threads, 0, st>>>(A);
 }
 
+// Opts k_lin_dp<MODE> in to its dynamic shared memory (once per device).
+template <int MODE>
+static void lin_dp_optin(int dev) {
+  static int done[64] = {};
+  if (!done[dev & 63]) {
+    cudaFuncSetAttribute(k_lin_dp<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(LinSmem));
+    done[dev & 63] = 1;
+  }
+}
+
+template <int MODE>
+static int lin_dp_prepare(int dev) {
+  lin_dp_optin<MODE>(dev);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<MODE>, kDpWarps * 32,
+                                                sizeof(LinSmem));
+  return per_sm;
+}
+
 int lin_dp_blocks(int mode) {
   static int cache[3][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   int &c = cache[mode][dev & 63];
   if (!c) {
-    int per_sm = 0, sms = 0;
-    const int t = kDpWarps * 32;
-    if (mode == kDpSets) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpSets>, t, 0);
-    else if (mode == kDpChoice) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpChoice>, t, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lin_dp<kDpCost>, t, 0);
+    int per_sm = mode == kDpSets ? lin_dp_prepare<kDpSets>(dev)
+               : mode == kDpChoice ? lin_dp_prepare<kDpChoice>(dev) : lin_dp_prepare<kDpCost>(dev);
+    int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
@@ -603,9 +730,15 @@ int lin_dp_blocks(int mode) {
 }
 
 void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st) {
-  if (mode == kDpSets) k_lin_dp<kDpSets><<<blocks, kDpWarps * 32, 0, st>>>(A);
-  else if (mode == kDpChoice) k_lin_dp<kDpChoice><<<blocks, kDpWarps * 32, 0, st>>>(A);
-  else k_lin_dp<kDpCost><<<blocks, kDpWarps * 32, 0, st>>>(A);
+  const size_t sm = sizeof(LinSmem);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (mode == kDpSets) lin_dp_optin<kDpSets>(dev);
+  else if (mode == kDpChoice) lin_dp_optin<kDpChoice>(dev);
+  else lin_dp_optin<kDpCost>(dev);
+  if (mode == kDpSets) k_lin_dp<kDpSets><<<blocks, kDpWarps * 32, sm, st>>>(A);
+  else if (mode == kDpChoice) k_lin_dp<kDpChoice><<<blocks, kDpWarps * 32, sm, st>>>(A);
+  else k_lin_dp<kDpCost><<<blocks, kDpWarps * 32, sm, st>>>(A);
 }
 
 void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st) {

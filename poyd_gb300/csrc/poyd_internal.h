@@ -20,6 +20,7 @@ constexpr int kRows = 64;       // rows per strip: two per lane
 constexpr int kLag = 3;         // steps between consecutive lanes
 constexpr int kStepBlock = 32;  // steps per queue block and per direction word
 constexpr int kDpWarps = 8;     // warps per k_lin_dp block
+constexpr int kMinPeriod = 160; // shortest strip period (boundary flush-to-prefetch distance)
 // k_lin_dp modes: costs only; full direction sets; backtrack moves (values x4)
 constexpr int kDpCost = 0, kDpSets = 1, kDpChoice = 2;
 constexpr int kInfChoice = 3 << 25;  // out-of-band value of kDpChoice (x4 scale)
@@ -36,10 +37,10 @@ struct LinPlan {
   int32_t dlo, wd;         // band diagonals [dlo, dlo + wd)
   int32_t swap;            // 1: rows are the caller's b
   int32_t nstrips;         // ceil(l1 / 64)
-  int32_t sblocks;         // 32-step blocks per strip
+  int32_t sblocks;         // strip period W in 32-step blocks
   int32_t deltaw;          // width extension used
   int32_t empty;           // DOS.median empty rule: 1 = a empty, 2 = b empty
-  int32_t pad_;
+  int32_t nblk;            // 32-step blocks of the whole sweep
 };
 static_assert(sizeof(LinPlan) == 64, "LinPlan layout");
 
