@@ -12,7 +12,8 @@ pair by the plan kernel, mirroring algn.c:872-968); GCUPS = cells / s.
 
 ``value`` is device throughput with inputs resident in HBM; ``e2e`` is the
 same metric through the public API with pinned host buffers, the input
-upload and the full result download inside the timed region.  N > 1 runs one
+upload and the download of every result (packed: aligned pairs, medians
+with gaps, medians, costs, lengths) inside the timed region.  N > 1 runs one
 replica per GPU (the pairs are independent; no collective).  ``--impl
 reference`` times the CPU restatement of the reference (oracle/) on all host
 cores over a bounded sample of the same workload.
@@ -280,14 +281,20 @@ def run_ours(args):
         h2d = sum(int(x.numel() * x.element_size()) for x in pinned)
 
         def e2e_step(out_host):
+            # results leave the device packed (only the bytes that hold
+            # alignments and medians), then are read on the host
             b = align.PairBatch.from_packed(pinned, device=dev, non_blocking=True)
             r = align.align_2(b, cm)
+            p = r.pack()
             if out_host is None:
-                out_host = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
-                            for x in (r.cost, r.out, r.out_len)]
-            for dst, src in zip(out_host, (r.cost, r.out, r.out_len)):
-                dst.copy_(src, non_blocking=True)
+                out_host = [torch.empty(r.cost.shape, dtype=r.cost.dtype, pin_memory=True),
+                            torch.empty(r.out.numel(), dtype=torch.uint8, pin_memory=True),
+                            torch.empty(r.out_len.shape, dtype=r.out_len.dtype, pin_memory=True)]
+            out_host[0].copy_(p.cost, non_blocking=True)
+            out_host[1][:p.packed.numel()].copy_(p.packed, non_blocking=True)
+            out_host[2].copy_(p.out_len, non_blocking=True)
             torch.cuda.synchronize()
+            e2e_step.d2h = (p.cost.numel() * 4 + p.packed.numel() + p.out_len.numel() * 4)
             return out_host
 
         out_host = e2e_step(None)  # untimed: allocates the pinned result buffers
@@ -297,7 +304,7 @@ def run_ours(args):
         for _ in range(n_e2e):
             out_host = e2e_step(out_host)
         dt = (time.perf_counter() - t0) / n_e2e
-        d2h = sum(int(x.numel() * x.element_size()) for x in out_host)
+        d2h = int(e2e_step.d2h)
         _, dt_max = aggregate(cells, dt, dev, world)
         e2e = {"value": total_cells / dt_max / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}

@@ -134,6 +134,18 @@ int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
                        int32_t *out_len, int64_t *band_cells, int32_t flags,
                        void *stream);
 
+/* Packs the results of poyd_align_2_batch for a download (no reference
+ * counterpart: the reference hands back one seq block per call).  Pair i's
+ * aligned a, aligned b and median with gaps (out_len[2i] bytes each) and its
+ * median (out_len[2i+1] bytes) are copied back to back, in that order, to
+ * packed + packed_off[i], where packed_off[i] is the sum over j < i of
+ * 3 * out_len[2j] + out_len[2j+1].  Device pointers; asynchronous on
+ * `stream`.  POYD_ERANGE is not checked here: pass only out_len >= 0. */
+int poyd_pack_alignments(int32_t n, const uint8_t *out, const int64_t *out_off,
+                         const int32_t *a_len, const int32_t *b_len,
+                         const int32_t *out_len, uint8_t *packed,
+                         const int64_t *packed_off, void *stream);
+
 /* ---------------------------------------------------------------------
  * Single-pair drop-ins with the OCaml externals' argument order
  * (sequence.ml:453-466, 731-758).  Host pointers; each call runs the

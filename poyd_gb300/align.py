@@ -202,6 +202,61 @@ class AlignResult:
         return res
 
 
+    def pack(self, stream=None) -> "PackedAlignments":
+        """The results packed back to back on the device (aligned a, aligned
+        b, median with gaps, median per pair), ready for one download of
+        only the bytes that hold results."""
+        n = self.cost.numel()
+        dev = self.cost.device
+        ln = self.out_len.view(-1, 2).to(torch.int64)
+        sizes = 3 * ln[:, 0] + ln[:, 1]
+        off = torch.cumsum(sizes, 0) - sizes
+        if n:
+            total, lo = torch.stack([sizes.sum(), ln.min()]).cpu().tolist()
+        else:
+            total, lo = 0, 0
+        if lo < 0:
+            raise native.PoydError(-3, "traceback left the band for pair(s) "
+                                   f"{torch.nonzero(ln[:, 0] < 0).flatten()[:8].tolist()}")
+        packed = torch.empty(max(total, 16), dtype=torch.uint8, device=dev)
+        a_len = (self.cap - 2).to(torch.int32)  # a_len + b_len; split is irrelevant to cap
+        zeros = torch.zeros_like(a_len)
+        check(lib().poyd_pack_alignments(
+            n, self.out.data_ptr(), self.out_off.data_ptr(), a_len.data_ptr(), zeros.data_ptr(),
+            self.out_len.data_ptr(), packed.data_ptr(), off.data_ptr(), _stream_handle(stream)))
+        return PackedAlignments(self.cost, packed[:total], self.out_len)
+
+
+@dataclass
+class PackedAlignments:
+    """Batched align_2 results packed back to back (see AlignResult.pack):
+    pair i holds 3 * n_i + m_i bytes, n_i = out_len[2i], m_i = out_len[2i+1]."""
+
+    cost: torch.Tensor     # int32 [n]
+    packed: torch.Tensor   # uint8
+    out_len: torch.Tensor  # int32 [n, 2]
+
+    def to_host(self):
+        """Same dicts as AlignResult.to_host, from the packed bytes (which may
+        already be host tensors)."""
+        buf = self.packed.cpu().numpy()
+        ln = self.out_len.view(-1, 2).cpu().numpy().astype(np.int64)
+        cost = self.cost.cpu().numpy()
+        sizes = 3 * ln[:, 0] + ln[:, 1]
+        off = np.cumsum(sizes) - sizes
+        res = []
+        for i in range(len(cost)):
+            o, n, nm = int(off[i]), int(ln[i, 0]), int(ln[i, 1])
+            res.append({
+                "cost": int(cost[i]),
+                "a": buf[o:o + n].copy(),
+                "b": buf[o + n:o + 2 * n].copy(),
+                "median_wg": buf[o + 2 * n:o + 3 * n].copy(),
+                "median": buf[o + 3 * n:o + 3 * n + nm].copy(),
+            })
+        return res
+
+
 def align_2(batch: PairBatch, cm: CostMatrix, dos_empty: bool = False,
             band_cells: bool = False, stream=None) -> AlignResult:
     """Batched ``DOS.median`` pieces (seqCS.ml:747-776): ``align_2``,

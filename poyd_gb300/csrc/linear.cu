@@ -686,6 +686,39 @@ __global__ void __launch_bounds__(kDpWarps * 32, 3) k_lin_dp(LinDpArgs A) {
 }
 
 // ---------------------------------------------------------------------------
+// Packing of batched align_2 results: one warp per pair copies the used tail
+// of each of its four right-aligned slots back to back.
+// ---------------------------------------------------------------------------
+__global__ void k_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
+                                  const int32_t *a_len, const int32_t *b_len,
+                                  const int32_t *out_len, uint8_t *packed,
+                                  const int64_t *packed_off) {
+  const int lane = threadIdx.x & 31;
+  const int64_t id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (id >= n) return;
+  const int64_t cap = (int64_t)a_len[id] + b_len[id] + 2;
+  const int64_t na = out_len[2 * id], nm = out_len[2 * id + 1];
+  const uint8_t *src = out + out_off[id];
+  uint8_t *dst = packed + packed_off[id];
+  for (int k = 0; k < 4; ++k) {
+    const int64_t len = k < 3 ? na : nm;
+    const uint8_t *s = src + (k + 1) * cap - len;
+    uint8_t *d = dst + (k < 3 ? k * na : 3 * na);
+    for (int64_t x = lane; x < len; x += 32) d[x] = s[x];
+  }
+}
+
+void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
+                            const int32_t *a_len, const int32_t *b_len,
+                            const int32_t *out_len, uint8_t *packed,
+                            const int64_t *packed_off, cudaStream_t st) {
+  const int threads = 256;
+  const int64_t blocks = ((int64_t)n * 32 + threads - 1) / threads;
+  k_pack_alignments<<<(unsigned)blocks, threads, 0, st>>>(n, out, out_off, a_len, b_len,
+                                                          out_len, packed, packed_off);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st) {

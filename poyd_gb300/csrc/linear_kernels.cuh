@@ -75,5 +75,9 @@ void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
 int lin_dp_blocks(int mode);
 void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st);
 void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st);
+void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
+                            const int32_t *a_len, const int32_t *b_len,
+                            const int32_t *out_len, uint8_t *packed,
+                            const int64_t *packed_off, cudaStream_t st);
 
 }  // namespace poyd

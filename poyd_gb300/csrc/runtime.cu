@@ -245,6 +245,20 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
 using namespace poyd;
 
 extern "C" const char *poyd_last_error(void) { return g_err; }
+
+extern "C" int poyd_pack_alignments(int32_t n, const uint8_t *out, const int64_t *out_off,
+                                    const int32_t *a_len, const int32_t *b_len,
+                                    const int32_t *out_len, uint8_t *packed,
+                                    const int64_t *packed_off, void *stream) {
+  if (n < 0 || (n > 0 && (!out || !out_off || !a_len || !b_len || !out_len || !packed ||
+                          !packed_off)))
+    return fail(POYD_EINVAL, "poyd_pack_alignments: null argument");
+  if (n == 0) return POYD_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  { ProfScope ps("pack_alignments", st); launch_pack_alignments(n, out, out_off, a_len, b_len, out_len, packed, packed_off, st); }
+  CK(cudaGetLastError());
+  return POYD_OK;
+}
 extern "C" int poyd_version(void) { return 1; }
 
 extern "C" int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,

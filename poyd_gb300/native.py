@@ -54,6 +54,8 @@ SIGNATURES = [
     ("poyd_profile_enable", C.c_int, [C.c_int]),
     ("poyd_profile_read", C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int]),
     ("poyd_launch_count", C.c_longlong, []),
+    ("poyd_pack_alignments", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("poyd_int_pipe_rate", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]

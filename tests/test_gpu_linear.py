@@ -147,3 +147,26 @@ def test_codes_above_31_rejected():
             align.align_2(batch, cm)
     ok = align.PairBatch.from_host([a], [synth.with_gap(synth.random_dna(rng, 50))])
     assert int(align.cost_2(ok, align.CostMatrix.dna(1, 2))[0].item()) >= 0
+
+
+def test_packed_results_equal_slots():
+    """AlignResult.pack() carries exactly the slot contents (aligned a, b,
+    median with gaps, median per pair), DOS empty-rule pairs included."""
+    rng = np.random.default_rng(21)
+    A, B = _random_pairs(77, 40, 600)
+    EA, EB = _edge_pairs(rng)
+    A += EA
+    B += EB
+    g = synth.with_gap
+    A.append(g(np.full(0, 16, np.uint8)))
+    B.append(g(synth.random_dna(rng, 30)))
+    cm = align.CostMatrix.dna(1, 2)
+    res = align.align_2(align.PairBatch.from_host(A, B), cm, dos_empty=True)
+    slots = res.to_host()
+    packed = res.pack()
+    assert packed.packed.numel() == sum(3 * len(r["a"]) + len(r["median"]) for r in slots)
+    host = align.PackedAlignments(packed.cost.cpu(), packed.packed.cpu(), packed.out_len.cpu())
+    for r, p in zip(slots, host.to_host()):
+        assert r["cost"] == p["cost"]
+        for k in ("a", "b", "median_wg", "median"):
+            assert np.array_equal(r[k], p[k]), k
