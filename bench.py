@@ -496,13 +496,16 @@ def run_learned(args):
     sc = learned.learned_scorer(prop, be, frac=0.03, stats=stats)
     t0 = time.perf_counter()
     hist_l = []
+    diag = None
     for _ in range(3 * args.max_passes):
-        st = search.spr_pass(tl, be, max_moves=16, scorer=sc)
+        st = search.spr_pass(tl, be, max_moves=16, scorer=sc, diag=diag)
+        diag = st.diag
         hist_l.append(st.cost_after)
         if st.cost_after <= target:
             break
         if st.moves_accepted == 0:
-            st = search.spr_pass(tl, be, max_moves=16)  # exhaustive fallback
+            st = search.spr_pass(tl, be, max_moves=16, diag=diag)  # exhaustive fallback
+            diag = st.diag
             hist_l.append(st.cost_after)
             if st.moves_accepted == 0 or st.cost_after <= target:
                 break

@@ -183,12 +183,15 @@ def run_search(t: search.Tree, be, scorer=None, max_passes: int = 30, max_moves:
     pass when `scorer` is the learned proposal).  Returns (history, seconds)."""
     hist = []
     t0 = time.perf_counter()
+    diag = None
     for _ in range(max_passes):
-        st = search.spr_pass(t, be, max_moves=max_moves, scorer=scorer)
+        st = search.spr_pass(t, be, max_moves=max_moves, scorer=scorer, diag=diag)
+        diag = st.diag
         hist.append(st.cost_after)
         if st.moves_accepted == 0:
             if scorer is not None and fallback:
-                st = search.spr_pass(t, be, max_moves=max_moves)
+                st = search.spr_pass(t, be, max_moves=max_moves, diag=diag)
+                diag = st.diag
                 hist.append(st.cost_after)
                 if st.moves_accepted == 0:
                     break

@@ -233,10 +233,12 @@ class GpuBackend:
             tmp_s = torch.empty((n, self.ns, self.k), dtype=torch.int32, device=self.dev)
             native.check(L.poyd_sank_median_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
                                                   _p(ia), _p(ib), _p(tmp_s), None, None, st))
-        # move the medians into the pool
+        # move the medians into the pool (one transfer brings the lengths
+        # and both costs to the host)
         ln = res.out_len.view(-1, 2)[:, 1].to(torch.int64)
-        lens = ln.cpu().numpy()
-        if lens.min() < 0:
+        host = torch.cat([ln, res.cost.to(torch.int64), added]).cpu().numpy()
+        lens, do_cost, f_cost = host[:n], host[n:2 * n], host[2 * n:]
+        if n and lens.min() < 0:
             raise native.PoydError(-3, "median traceback failed")
         src = res.out_off + 4 * res.cap - ln
         dst_off = np.array([self._reserve(int(x)) for x in lens], np.int64)
@@ -253,7 +255,20 @@ class GpuBackend:
         if self.ns:
             self.sank[oi] = tmp_s
         self.stats["median_pairs"] += n
-        return res.cost.cpu().numpy().astype(np.int64), added.cpu().numpy()
+        return do_cost, f_cost
+
+    def rebind_nodes(self, dst: np.ndarray, src: np.ndarray):
+        """Nodes dst take over the medians computed into nodes src (the
+        scratch slots of an evaluated move)."""
+        dst = np.asarray(dst, np.int64)
+        src = np.asarray(src, np.int64)
+        self.off[dst], self.len[dst] = self.off[src], self.len[src]
+        d = torch.from_numpy(dst).to(self.dev)
+        s = torch.from_numpy(src).to(self.dev)
+        if self.nf:
+            self.fitch[d] = self.fitch[s]
+        if self.ns:
+            self.sank[d] = self.sank[s]
 
     def distances(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
         """Candidate-join distance d(a_i, b_i) = DOS.distance + Fitch + Sankoff."""
@@ -366,6 +381,7 @@ class PassStats:
     cost_after: int = 0
     seconds_scoring: float = 0.0
     seconds_total: float = 0.0
+    diag: Diagnosis | None = None  # diagnosis of the tree after the pass
 
 
 def euler(t: Tree):
@@ -410,13 +426,15 @@ def spr_candidates(t: Tree):
     return S[keep], E[keep]
 
 
-def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None):
+def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None):
     """One SPR pass: score every candidate join in one batch (or through
     `scorer`, which may score a subset), then try the best-scoring moves in
-    order; a move is kept only if the exact re-diagnosed tree cost drops."""
+    order; a move is kept only if the exact re-diagnosed tree cost drops.
+    `diag` may carry the current tree's diagnosis (a previous pass's
+    `PassStats.diag`) to skip the initial downpass."""
     t0 = time.perf_counter()
     st = PassStats()
-    diag = downpass(t, be)
+    diag = downpass(t, be) if diag is None else diag
     st.cost_before = diag.total
     S, E = spr_candidates(t)
     st.candidates = len(S)
@@ -448,22 +466,32 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None):
     # Rounds: the exact cost of every remaining move is computed in one
     # batched incremental diagnosis; the best improving move is applied and
     # the tree re-diagnosed; moves no longer valid are dropped.
+    # The accepted move's recomputed medians become the tree's own (no
+    # re-diagnosis per move); one full downpass at the end of the pass
+    # checks the incremental totals.
     best = diag.total
     while moves:
         st.moves_tried += len(moves)
-        totals = evaluate_moves(t, be, diag, moves)
+        detail = {}
+        totals = evaluate_moves(t, be, diag, moves, detail)
         k = int(np.argmin(totals))
         if totals[k] >= best:
+            be.release_nodes(2 * t.n)
             break
         s, e = moves.pop(k)
         w = t.prune(s)
         t.insert(s, e, w)
-        diag = downpass(t, be)
-        assert diag.total == totals[k], (diag.total, totals[k])
-        best = diag.total
+        commit_move(be, diag, detail[k], totals[k])
+        be.release_nodes(2 * t.n)
+        best = int(totals[k])
         st.moves_accepted += 1
         moves = [(a, b) for a, b in moves if _valid_move(t, a, b)]
+    if st.moves_accepted:
+        check = downpass(t, be)
+        assert check.total == best, (check.total, best)
+        diag = check
     st.cost_after = best
+    st.diag = diag
     st.seconds_total = time.perf_counter() - t0
     return st
 
@@ -483,12 +511,16 @@ def _heights(t: Tree) -> dict:
     return h
 
 
-def evaluate_moves(t: Tree, be, diag: Diagnosis, moves) -> np.ndarray:
+def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarray:
     """Exact total cost of the tree after each SPR move (s onto the edge above
     e), computed together: a move changes only the ancestors of the prune
     point and of the regraft point, so each trial recomputes just those nodes
     (into scratch node slots), and the dirty nodes of every trial at one
-    height form one batch of medians."""
+    height form one batch of medians.
+
+    With `detail` (a dict), the scratch slots are kept and detail[m] lists
+    (node, scratch slot, DO cost, Fitch cost) of trial m's recomputed nodes,
+    for commit_move; the caller then releases the slots."""
     h_base = _heights(t)
     base_sank = be.sank_cost(t.root)
     tid_next = 2 * t.n
@@ -520,7 +552,7 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves) -> np.ndarray:
             tid_next += 1
             a, b = T.kids[v]
             ref = lambda c: tid[c] if c in dirty else c
-            recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v]))
+            recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v], v))
             old[m] += diag.do_cost[v] + diag.fitch_cost[v]
         roots.append(tid[T.root])
     be.ensure_nodes(tid_next)
@@ -529,8 +561,24 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves) -> np.ndarray:
         r = np.array(recs[lvl], np.int64)
         do, fi = be.medians(r[:, 1], r[:, 2], r[:, 3])
         np.add.at(new, r[:, 0], do + fi)
+        if detail is not None:
+            for i in range(len(r)):
+                detail.setdefault(int(r[i, 0]), []).append(
+                    (int(r[i, 4]), int(r[i, 3]), int(do[i]), int(fi[i])))
     totals = np.array([diag.total - old[m] + new[m] - base_sank + be.sank_cost(roots[m])
                        for m in range(len(moves))], np.int64)
-    be.release_nodes(2 * t.n)
+    if detail is None:
+        be.release_nodes(2 * t.n)
     return totals
+
+
+def commit_move(be, diag: Diagnosis, rows, total: int):
+    """Makes an evaluated move's recomputed medians the tree's own (the move
+    must already be applied to the tree): each recomputed node takes over
+    its scratch slot's medians and costs."""
+    be.rebind_nodes([v for v, _, _, _ in rows], [tid for _, tid, _, _ in rows])
+    for v, _, do, fi in rows:
+        diag.do_cost[v] = do
+        diag.fitch_cost[v] = fi
+    diag.total = int(total)
 

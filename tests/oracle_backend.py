@@ -75,6 +75,12 @@ class OracleBackend:
     def ensure_nodes(self, n_nodes):
         pass
 
+    def rebind_nodes(self, dst, src):
+        for v, t in zip(dst, src):
+            self.seq[int(v)] = self.seq[int(t)]
+            self.fitch[int(v)] = self.fitch[int(t)]
+            self.sank[int(v)] = self.sank[int(t)]
+
     def release_nodes(self, first):
         for d in (self.seq, self.fitch, self.sank):
             for v in [v for v in d if v >= first]:
