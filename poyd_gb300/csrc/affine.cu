@@ -23,6 +23,7 @@
 #include <numeric>
 #include <vector>
 #include "affine_kernels.cuh"
+#include "back_writer.cuh"
 
 namespace poyd {
 
@@ -293,10 +294,6 @@ __global__ void __launch_bounds__(256) k_aff_dp(AffDpArgs A) {
   }
 }
 
-__device__ __forceinline__ void pre(uint8_t *buf, int64_t cap, int64_t &n, int v) {
-  if (n < cap) buf[cap - 1 - n] = (uint8_t)v;
-  ++n;
-}
 
 __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
   __shared__ uint8_t med[1024];
@@ -326,7 +323,20 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
   const int sb = P.sblocks, e0 = P.e0, lenj = P.lenj;
   int i = P.leni, j = P.lenj;
   int ic = si[i], jc = sj[j];
-  int64_t nr = 0, nw = 0, nm = 0;
+  int64_t nr = 0, nm = 0;
+  // the four outputs are written backwards through word-buffered writers
+  BackWriter wri(ri + cap - 1), wrj(rj + cap - 1), wow(ow + cap - 1), wom(om + cap - 1);
+  int last_m = -1;  // the median byte written last (its position cap - nm)
+  auto put_r = [&](int x, int y) {  // one column of resi / resj
+    wri.put((uint32_t)x);
+    wrj.put((uint32_t)y);
+    ++nr;
+  };
+  auto put_m = [&](int x) {
+    wom.put((uint32_t)x);
+    last_m = x;
+    ++nm;
+  };
   int mode = 0;  // 0 todo, 1 vertical, 2 horizontal, 3 diagonal, 4 align
   bool bad = false;
   while (i != 0 && j != 0) {
@@ -342,20 +352,20 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
       mode = t == 0 ? 2 : t == 1 ? 4 : t == 2 ? 1 : 3;
     } else if (mode == 1) {
       if (c & 4u) mode = 0;
-      if (!(ic & 16)) { pre(om, cap, nm, ic | 16); pre(ow, cap, nw, ic | 16); }
-      else pre(ow, cap, nw, 16);
-      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, 16);
+      if (!(ic & 16)) { put_m(ic | 16); wow.put(ic | 16); }
+      else wow.put(16);
+      put_r(ic, 16);
       --i; ic = si[i];
     } else if (mode == 2) {
       if (c & 8u) mode = 0;
-      if (!(jc & 16)) { pre(om, cap, nm, jc | 16); pre(ow, cap, nw, jc | 16); }
-      else pre(ow, cap, nw, 16);
-      pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, jc);
+      if (!(jc & 16)) { put_m(jc | 16); wow.put(jc | 16); }
+      else wow.put(16);
+      put_r(16, jc);
       --j; jc = sj[j];
     } else if (mode == 3) {
       if (c & 16u) mode = 0;
-      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, jc);
-      pre(ow, cap, nw, 16);
+      put_r(ic, jc);
+      wow.put(16);
       --i; --j; jc = sj[j]; ic = si[i];
     } else {
       const uint32_t a = (c >> 5) & 3u;
@@ -363,28 +373,32 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
       else if (a == 1) mode = 3;
       else if (a == 2) mode = 1;
       const int m = med[((ic & 15) << 5) | (jc & 15)];
-      pre(om, cap, nm, m); pre(ow, cap, nw, m);
-      pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, jc);
+      put_m(m); wow.put(m);
+      put_r(ic, jc);
       --i; --j; jc = sj[j]; ic = si[i];
     }
     if (nr + 4 >= cap) { bad = true; break; }
   }
   while (!bad && i != 0) {
-    if (!(ic & 16)) { pre(om, cap, nm, ic | 16); pre(ow, cap, nw, ic | 16); }
-    else pre(ow, cap, nw, 16);
-    pre(ri, cap, nr, ic); --nr; pre(rj, cap, nr, 16);
+    if (!(ic & 16)) { put_m(ic | 16); wow.put(ic | 16); }
+    else wow.put(16);
+    put_r(ic, 16);
     --i; ic = si[i];
   }
   while (!bad && j != 0) {
-    if (!(jc & 16)) { pre(om, cap, nm, jc | 16); pre(ow, cap, nw, jc | 16); }
-    else pre(ow, cap, nw, 16);
-    pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, jc);
+    if (!(jc & 16)) { put_m(jc | 16); wow.put(jc | 16); }
+    else wow.put(16);
+    put_r(16, jc);
     --j; jc = sj[j];
   }
-  pre(ri, cap, nr, 16); --nr; pre(rj, cap, nr, 16);
-  pre(ow, cap, nw, 16);
+  put_r(16, 16);
+  wow.put(16);
   // an empty median has no position 0 in the reference; treated as not a gap
-  if (nm == 0 || om[cap - nm] != 16) pre(om, cap, nm, 16);
+  if (nm == 0 || last_m != 16) put_m(16);
+  wri.flush();
+  wrj.flush();
+  wow.flush();
+  wom.flush();
   A.out_len[2 * id] = bad ? -1 : (int32_t)nr;
   A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
 }
@@ -454,10 +468,8 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
     if (want_align) total += hw[t];
     maxwd = std::max(maxwd, hwd[t]);
   }
-  std::vector<int32_t> order((size_t)n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t x, int32_t y) { return hw[x] > hw[y]; });
+  std::vector<int32_t> order;
+  longest_first(hw, order);
   int64_t *doff = dmw + n;
   int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
   int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);

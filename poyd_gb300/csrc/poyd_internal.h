@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <cuda_runtime.h>
+#include <vector>
 #include "poyd_gb300.h"
 
 namespace poyd {
@@ -62,6 +63,8 @@ enum WsSlot {
 };
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);
+// Pair order for the persistent DP kernels: largest work first (stable).
+void longest_first(const std::vector<int64_t> &work, std::vector<int32_t> &order);
 int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *stream);
 
 // Launch accounting (profile.cu): bracket one kernel launch on `st`.

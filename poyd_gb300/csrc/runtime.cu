@@ -107,6 +107,28 @@ static int check_cm(const poyd_cm *cm, int *maxc) {
   return POYD_OK;
 }
 
+void longest_first(const std::vector<int64_t> &work, std::vector<int32_t> &order) {
+  // a stable two-pass radix sort on a descending 24-bit key (work / 128),
+  // linear in n
+  const int32_t n = (int32_t)work.size();
+  std::vector<int32_t> tmp((size_t)n);
+  std::vector<uint32_t> key((size_t)n);
+  order.assign((size_t)n, 0);
+  for (int32_t i = 0; i < n; ++i) {
+    const int64_t q = std::min<int64_t>(work[i] >> 7, (1 << 24) - 1);
+    key[i] = (uint32_t)((1 << 24) - 1 - q);
+    tmp[i] = i;
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    const int sh = 12 * pass;
+    std::vector<int32_t> cnt((1 << 12) + 1, 0);
+    for (int32_t i = 0; i < n; ++i) ++cnt[((key[tmp[i]] >> sh) & 4095) + 1];
+    for (int b = 0; b < (1 << 12); ++b) cnt[b + 1] += cnt[b];
+    for (int32_t i = 0; i < n; ++i) order[cnt[(key[tmp[i]] >> sh) & 4095]++] = tmp[i];
+    if (pass == 0) std::swap(order, tmp);
+  }
+}
+
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream) {
   return upload_tables_ws(workspace((cudaStream_t)stream), cm, dev, stream);
 }
@@ -178,23 +200,9 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     if (want_align) total += hw[i];
     maxwd = std::max(maxwd, hwd[i]);
   }
-  // Longest first (dm_words ~ strips x band steps is the band area): a
-  // stable two-pass radix sort on a descending 24-bit key, linear in n.
-  std::vector<int32_t> order((size_t)n), tmp((size_t)n);
-  std::vector<uint32_t> key((size_t)n);
-  for (int32_t i = 0; i < n; ++i) {
-    const int64_t q = std::min<int64_t>(hw[i] >> 7, (1 << 24) - 1);  // multiples of 128
-    key[i] = (uint32_t)((1 << 24) - 1 - q);
-    tmp[i] = i;
-  }
-  for (int pass = 0; pass < 2; ++pass) {
-    const int sh = 12 * pass;
-    std::vector<int32_t> cnt((1 << 12) + 1, 0);
-    for (int32_t i = 0; i < n; ++i) ++cnt[((key[tmp[i]] >> sh) & 4095) + 1];
-    for (int b = 0; b < (1 << 12); ++b) cnt[b + 1] += cnt[b];
-    for (int32_t i = 0; i < n; ++i) order[cnt[(key[tmp[i]] >> sh) & 4095]++] = tmp[i];
-    if (pass == 0) std::swap(order, tmp);
-  }
+  // longest first: dm_words ~ strips x band steps is the band area
+  std::vector<int32_t> order;
+  longest_first(hw, order);
   int64_t *doff = dmw + n;
   int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
   int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
