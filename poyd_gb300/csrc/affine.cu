@@ -148,135 +148,193 @@ __global__ void k_aff_plan(AffPlanArgs A) {
   if (A.maxc * (long long)(la + lb + 2) >= (1 << 22)) atomicOr(A.err, 2);
 }
 
+// Shared memory of one k_aff_dp block.
+struct AffSmem {
+  uint32_t tab[1024];            // packed {cost[a][b], cost[gap][b]}
+  uint8_t win[8][64];            // per warp: the 64 columns of a 32-step block
+  int4 ring_in[8][32];           // per warp: lane 0's inputs of the block
+  int4 ring_out[8][32];          // per warp: lane 31's states of the block
+};
+
+// 16 steps of one strip: cells (i, j = i + d) with d = kDlo + s - 2 * lane at
+// step s = s0 + u.  The four states of row i-1 at column j come from lane
+// k-1 by shuffles (lane 0: from ring_in, the previous strip's last row), the
+// column characters from the block's window, and lane 31's states go to
+// ring_out.  The cell rules restate FILL_EXTEND_HORIZONTAL / _VERTICAL /
+// _BLOCK_DIAGONAL[_NOBT], FILL_CLOSE_BLOCK_DIAGONAL and ASSIGN_MINIMUM
+// (algn.c:1740-1977, 2251-2280); the boundary cells restate
+// initialize_matrices_affine[_nobt] and the band edges of
+// algn_fill_plane_3_aff[_nobt] (algn.c:2124-2248, 2309-2400).
+struct AffRow {
+  int ic, ip, si_ext, si_open, si_vext, i;
+  const uint32_t *srow;
+  int uL, uR, uF;  // steps (relative to the half block) of the left / right boundary cell and of the final cell
+};
+struct AffState {
+  int eh_l, cb_l;                  // this row's previous cell (horizontal predecessor)
+  int eh_d, ev_d, eb_d, cb_d;      // row above, previous column (diagonal predecessor)
+  int m_eh, m_ev, m_eb, m_cb;      // this row's last cell, for the lane below
+  uint32_t word;
+  int result;
+};
+
 template <bool BT>
-__device__ __forceinline__ void aff_pair(const AffDpArgs &A, const uint32_t *tab,
+__device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const AffSmem &sm,
+                                         const uint8_t *wlane, const int4 *rin, int4 *rout,
+                                         int s0, int go, uint32_t *dmb, int lane) {
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    int u_eh = __shfl_up_sync(kFullA, S.m_eh, 1);
+    int u_ev = __shfl_up_sync(kFullA, S.m_ev, 1);
+    int u_eb = __shfl_up_sync(kFullA, S.m_eb, 1);
+    int u_cb = __shfl_up_sync(kFullA, S.m_cb, 1);
+    if (lane == 0) {
+      const int4 v = rin[u];
+      u_eh = v.x; u_ev = v.y; u_eb = v.z; u_cb = v.w;
+    }
+    const int jc = wlane[u], jp = wlane[u - 1];
+    const int j = R.i + kDlo + s0 + u - 2 * lane;
+    // column quantities (algn.c:2321-2328 / 2451-2457)
+    const int sj_ext = (int)(sm.tab[jc] >> 16);  // prepend[jc] = cost[gap][jc]
+    const int sj_open = (!(jp & 16) && (jc & 16)) ? 0 : go;
+    const int hext = (j == 1) ? sj_ext : (((jp & 16) && !(jc & 16)) ? sj_open + sj_ext : sj_ext);
+    // FILL_EXTEND_HORIZONTAL
+    const int e1 = S.eh_l + hext, e2 = S.cb_l + sj_open + sj_ext;
+    int eh = min(e1, e2);
+    // FILL_EXTEND_VERTICAL
+    const int v1 = u_ev + R.si_vext, v2 = u_cb + R.si_open + R.si_ext;
+    int ev = min(v1, v2);
+    // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]
+    const bool both = (R.ic & 16) && (jc & 16);
+    const int dg = both ? 0 : kHigh;
+    const int od = BT ? dg : (both ? ((!(R.ip & 16) && !(jc & 16)) ? 0 : 2 * go) : kHigh);
+    const int b1 = S.eb_d + dg, b2 = S.cb_d + od;
+    int eb = min(b1, b2);
+    // FILL_CLOSE_BLOCK_DIAGONAL
+    const int cdiag = (int)(R.srow[jc & 15] & 0xffffu);
+    const int extra = max(sj_open, R.si_open);
+    const int fa = S.cb_d + cdiag;
+    const int fv = S.ev_d + cdiag + ((R.ic & 16) ? sj_open : 0);
+    const int fh = S.eh_d + cdiag + ((jc & 16) ? R.si_open : 0);
+    const int fd = S.eb_d + cdiag + extra;
+    int cb = min(min(fa, fv), min(fh, fd));
+    // ASSIGN_MINIMUM
+    int f = min(min(eh, ev), min(eb, cb));
+    uint32_t code = 0;
+    if (BT) {
+      // among tied states: DO_HORIZONTAL > DO_ALIGN > DO_VERTICAL > DO_DIAGONAL
+      // (algn.c:2005-2012); ALIGN_TO_HORIZONTAL > _DIAGONAL > _VERTICAL
+      // (algn.c:2049-2051)
+      const uint32_t todo = eh == f ? 0u : (cb == f ? 1u : (ev == f ? 2u : 3u));
+      const uint32_t achoice = fh == cb ? 0u : (fd == cb ? 1u : (fv == cb ? 2u : 3u));
+      code = todo | (v1 < v2 ? 0u : 4u) | (e1 < e2 ? 0u : 8u) | (b1 < b2 ? 0u : 16u) |
+             (achoice << 5);
+    }
+    if (R.i == 0) {  // initialize_matrices_affine row 0
+      if (j == 0) { eh = go; ev = go; eb = 0; cb = 0; f = 0; }
+      else { eh = S.eh_l + sj_ext; cb = eh; eb = kHigh; ev = kHigh; f = eh; }
+    } else if (u == R.uL) {  // vertical boundary cell left of the band
+      eh = kHigh; cb = kHigh; eb = kHigh; ev = v1; f = ev;
+      code = kCodeLeft;
+    } else if (u == R.uR) {  // HIGH_NUM cell right of the band
+      eh = kHigh; ev = kHigh; eb = kHigh; cb = kHigh;
+      code = kCodeRight;
+    }
+    if (u == R.uF) S.result = f;
+    if (BT) {
+      S.word = (S.word << 8) | code;
+      if ((u & 3) == 3) dmb[(u >> 2) * 32] = S.word;
+    }
+    S.m_eh = eh; S.m_ev = ev; S.m_eb = eb; S.m_cb = cb;
+    if (lane == 31) rout[u] = make_int4(eh, ev, eb, cb);
+    S.eh_d = u_eh; S.ev_d = u_ev; S.eb_d = u_eb; S.cb_d = u_cb;
+    S.eh_l = eh; S.cb_l = cb;
+  }
+}
+
+template <bool BT>
+__device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int warp,
                                          const AffPlan &P, int64_t dm_off, int id, int4 *bnd,
                                          int lane) {
   const uint8_t *si = A.seq + P.si_off;
   const uint8_t *sj = A.seq + P.sj_off;
   const int leni = P.leni, lenj = P.lenj, e0 = P.e0, wd = P.wd, go = A.go;
   const int Spad = P.sblocks * 4;
-  int result = 0;
+  uint8_t *win = sm.win[warp];
+  int4 *rin = sm.ring_in[warp], *rout = sm.ring_out[warp];
+  // this lane's column j at block step u is window index 32 + u - lane
+  const uint8_t *wl = win + 32 - lane;
+  const int4 kHigh4 = make_int4(kHigh, kHigh, kHigh, kHigh);
+  AffState S;
+  S.result = 0;
   uint32_t *dm = BT ? A.dm + dm_off : nullptr;
 
   for (int strip = 0; strip < P.nstrips; ++strip) {
     const int r0 = strip * 32;
-    const int i = r0 + lane;
-    const bool rowok = i <= leni;
-    const int ic = rowok ? si[i] : 0;
-    const int ip = (rowok && i > 0) ? si[i - 1] : 0;
-    const int si_ext = (int)(tab[(ic << 5) | 16] & 0xffffu);
-    const int si_open = (!(ip & 16) && (ic & 16)) ? 0 : go;
-    const int si_ng = ic & 15;
-    const int si_vext = (i > 1 && (ip & 16) && !(ic & 16)) ? si_open + si_ext : si_ext;
-    const int d_lb = (-i > kDlo) ? -i : kDlo;
-    const bool has_rb = e0 <= lenj - i;
-    const int s_fin = (i == leni) ? (lenj - leni) - kDlo + 2 * lane : -1;
-    const uint32_t *srow = tab + (si_ng << 5);
+    AffRow R;
+    R.i = r0 + lane;
+    const bool rowok = R.i <= leni;
+    R.ic = rowok ? si[R.i] : 0;
+    R.ip = (rowok && R.i > 0) ? si[R.i - 1] : 0;
+    R.si_ext = (int)(sm.tab[(R.ic << 5) | 16] & 0xffffu);
+    R.si_open = (!(R.ip & 16) && (R.ic & 16)) ? 0 : go;
+    R.si_vext = (R.i > 1 && (R.ip & 16) && !(R.ic & 16)) ? R.si_open + R.si_ext : R.si_ext;
+    R.srow = sm.tab + ((R.ic & 15) << 5);
+    const int d_lb = (-R.i > kDlo) ? -R.i : kDlo;
+    const bool has_rb = e0 <= lenj - R.i;
+    const int sL = d_lb - kDlo + 2 * lane;
+    const int sR = has_rb ? e0 - kDlo + 2 * lane : -1000000;
+    const int sF = (R.i == leni) ? (lenj - leni) - kDlo + 2 * lane : -1000000;
 
-    int eh_l = kHigh, cb_l = kHigh;
-    int eh_d = kHigh, ev_d = kHigh, eb_d = kHigh, cb_d = kHigh;
-    int m_eh = kHigh, m_ev = kHigh, m_eb = kHigh, m_cb = kHigh, m_col = 0;
+    S.eh_l = kHigh; S.cb_l = kHigh;
+    S.eh_d = kHigh; S.ev_d = kHigh; S.eb_d = kHigh; S.cb_d = kHigh;
+    S.m_eh = kHigh; S.m_ev = kHigh; S.m_eb = kHigh; S.m_cb = kHigh;
+    S.word = 0;
     if (lane == 0 && strip > 0) {
       const int4 v = bnd[0];
-      eh_d = v.x; ev_d = v.y; eb_d = v.z; cb_d = v.w;
+      S.eh_d = v.x; S.ev_d = v.y; S.eb_d = v.z; S.cb_d = v.w;
     }
-    int4 nxt = (strip > 0) ? bnd[1 < wd ? 1 : 0] : make_int4(kHigh, kHigh, kHigh, kHigh);
-    uint32_t word = 0;
-    for (int s = 0; s < Spad; ++s) {
-      int u_eh = __shfl_up_sync(kFullA, m_eh, 1);
-      int u_ev = __shfl_up_sync(kFullA, m_ev, 1);
-      int u_eb = __shfl_up_sync(kFullA, m_eb, 1);
-      int u_cb = __shfl_up_sync(kFullA, m_cb, 1);
-      int col = __shfl_up_sync(kFullA, m_col, 1);
-      const int d = kDlo + s - 2 * lane;
-      const int j = i + d;
-      if (lane == 0) {
-        u_eh = nxt.x; u_ev = nxt.y; u_eb = nxt.z; u_cb = nxt.w;
-        const int x = s + 2;
-        nxt = (strip > 0 && x < wd) ? bnd[x] : make_int4(kHigh, kHigh, kHigh, kHigh);
-        const int jc = (j >= 0 && j <= lenj) ? sj[j] : 0;
-        const int jp = (j >= 1 && j <= lenj + 1) ? sj[j - 1] : 0;
-        col = jc | (jp << 5);
+    for (int s0 = 0; s0 < Spad; s0 += 32) {
+      // stage the block: lane 0's inputs bnd[s + 1], the 64 columns
+      // r0 - 40 + s0 - 32 + x (x = 0..63), lane 31's states go to ring_out
+      __syncwarp();
+      {
+        const int x = s0 + lane + 1;
+        rin[lane] = (strip > 0 && x < wd) ? bnd[x] : kHigh4;
+        const int jb = r0 + kDlo + s0 - 32 + lane;
+        win[lane] = (jb >= 0 && jb <= lenj) ? sj[jb] : 0;
+        win[lane + 32] = (jb + 32 >= 0 && jb + 32 <= lenj) ? sj[jb + 32] : 0;
       }
-      const int jc = col & 31, jp = (col >> 5) & 31;
-      // column quantities (algn.c:2321-2328 / 2451-2457)
-      const int sj_ext = (int)(tab[jc] >> 16);  // prepend[jc] = cost[gap][jc]
-      const int sj_open = (!(jp & 16) && (jc & 16)) ? 0 : go;
-      const int hext = (j == 1) ? sj_ext : (((jp & 16) && !(jc & 16)) ? sj_open + sj_ext : sj_ext);
-      // FILL_EXTEND_HORIZONTAL
-      const int e1 = eh_l + hext, e2 = cb_l + sj_open + sj_ext;
-      int eh = e1 < e2 ? e1 : e2;
-      // FILL_EXTEND_VERTICAL
-      const int v1 = u_ev + si_vext, v2 = u_cb + si_open + si_ext;
-      int ev = v1 < v2 ? v1 : v2;
-      // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]
-      const bool both = (ic & 16) && (jc & 16);
-      const int dg = both ? 0 : kHigh;
-      const int od = BT ? dg : (both ? ((!(ip & 16) && !(jc & 16)) ? 0 : 2 * go) : kHigh);
-      const int b1 = eb_d + dg, b2 = cb_d + od;
-      int eb = b1 < b2 ? b1 : b2;
-      // FILL_CLOSE_BLOCK_DIAGONAL
-      const int cdiag = (int)(srow[jc & 15] & 0xffffu);
-      const int extra = sj_open < si_open ? si_open : sj_open;
-      const int fa = cb_d + cdiag;
-      const int fv = ev_d + cdiag + ((ic & 16) ? sj_open : 0);
-      const int fh = eh_d + cdiag + ((jc & 16) ? si_open : 0);
-      const int fd = eb_d + cdiag + extra;
-      int cb = fa;
-      uint32_t amask = 1;  // ALIGN_TO_ALIGN
-      if (cb >= fv) { if (cb > fv) { cb = fv; amask = 2; } else amask |= 2; }
-      if (cb >= fh) { if (cb > fh) { cb = fh; amask = 4; } else amask |= 4; }
-      if (cb >= fd) { if (cb > fd) { cb = fd; amask = 8; } else amask |= 8; }
-      // ASSIGN_MINIMUM
-      int f = eh;
-      uint32_t dmask = 4;  // DO_HORIZONTAL
-      if (f >= ev) { if (f > ev) { f = ev; dmask = 2; } else dmask |= 2; }
-      if (f >= eb) { if (f > eb) { f = eb; dmask = 8; } else dmask |= 8; }
-      if (f >= cb) { if (f > cb) { f = cb; dmask = 1; } else dmask |= 1; }
-      uint32_t code = 0;
-      if (BT) {
-        // dmask bits: 1 ALIGN, 2 VERTICAL, 4 HORIZONTAL, 8 DIAGONAL
-        const uint32_t todo = (dmask & 4) ? 0u : (dmask & 1) ? 1u : (dmask & 2) ? 2u : 3u;
-        const uint32_t achoice = (amask & 4) ? 0u : (amask & 8) ? 1u : (amask & 2) ? 2u : 3u;
-        code = todo | (v1 < v2 ? 0u : 4u) | (e1 < e2 ? 0u : 8u) | (b1 < b2 ? 0u : 16u) |
-               (achoice << 5);
+      __syncwarp();
+      uint32_t *dmb = BT ? dm + ((int64_t)strip * P.sblocks + (s0 >> 2)) * 32 + lane : nullptr;
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int hs = s0 + 16 * h;
+        R.uL = sL - hs;
+        R.uR = sR - hs;
+        R.uF = sF - hs;
+        aff_half<BT>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
+                     BT ? dmb + 4 * 32 * h : nullptr, lane);
       }
-      if (i == 0) {  // initialize_matrices_affine row 0
-        if (j == 0) { eh = go; ev = go; eb = 0; cb = 0; f = 0; }
-        else { eh = eh_l + sj_ext; cb = eh; eb = kHigh; ev = kHigh; f = eh; }
-      } else if (d == d_lb) {  // vertical boundary cell left of the band
-        eh = kHigh; cb = kHigh; eb = kHigh; ev = u_ev + si_vext; f = ev;
-        code = kCodeLeft;
-      } else if (has_rb && d == e0) {  // HIGH_NUM cell right of the band
-        eh = kHigh; ev = kHigh; eb = kHigh; cb = kHigh;
-        code = kCodeRight;
+      __syncwarp();
+      {
+        const int x = s0 + lane - 62;  // lane 31's band index at block step lane
+        if (x >= 0 && x < wd) bnd[x] = rout[lane];
       }
-      if (s == s_fin) result = f;
-      if (BT) {
-        word = (word << 8) | code;
-        if ((s & 3) == 3) dm[((int64_t)strip * P.sblocks + (s >> 2)) * 32 + lane] = word;
-      }
-      m_eh = eh; m_ev = ev; m_eb = eb; m_cb = cb; m_col = col;
-      if (lane == 31) {
-        const int x = s - 62;
-        if (x >= 0 && x < wd) bnd[x] = make_int4(eh, ev, eb, cb);
-      }
-      eh_d = u_eh; ev_d = u_ev; eb_d = u_eb; cb_d = u_cb;
-      eh_l = eh; cb_l = cb;
     }
     __syncwarp();
   }
-  result = __shfl_sync(kFullA, result, leni & 31);
-  if (lane == 0) A.cost[id] = result;
+  S.result = __shfl_sync(kFullA, S.result, leni & 31);
+  if (lane == 0) A.cost[id] = S.result;
 }
 
 template <bool BT>
 __global__ void __launch_bounds__(256) k_aff_dp(AffDpArgs A) {
-  __shared__ uint32_t tab[1024];
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) tab[t] = A.tables->packed[t];
+  __shared__ AffSmem sm;
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) sm.tab[t] = A.tables->packed[t];
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int4 *bnd = A.scratch + gw * A.slab;
   for (;;) {
@@ -290,10 +348,9 @@ __global__ void __launch_bounds__(256) k_aff_dp(AffDpArgs A) {
       if (lane == 0) A.cost[id] = 0;
       continue;
     }
-    aff_pair<BT>(A, tab, P, BT ? A.dm_off[id] : 0, id, bnd, lane);
+    aff_pair<BT>(A, sm, warp, P, BT ? A.dm_off[id] : 0, id, bnd, lane);
   }
 }
-
 
 __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
   __shared__ uint8_t med[1024];
