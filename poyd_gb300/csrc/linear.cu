@@ -310,8 +310,8 @@ struct DpMode {
 // at half a warp instruction per clock: min / select / logic / shifts run on
 // the ALU pipe, while the adds, the field extraction and the packing are
 // issued as multiply-adds (IMAD on the FMA pipe) through imad().  The
-// multipliers are kernel arguments (DpK: 1, -1, 4, 32, 128, -65536), so the
-// compiler cannot fold them back into ALU adds and shifts.
+// multipliers are kernel arguments (DpK: 1, -1, 4, -65536), so the compiler
+// cannot fold them back into ALU adds and shifts.
 __device__ __forceinline__ int imad(int a, int b, int c) {
   int d;
   asm("mad.lo.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));

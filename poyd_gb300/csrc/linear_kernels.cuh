@@ -44,9 +44,9 @@ struct LinTbArgs {
 
 // Runtime multipliers of the DP's multiply-add arithmetic (see linear.cu).
 struct DpK {
-  int one, m1, four, k32, k128, m64k;
+  int one, m1, four, m64k;
 };
-inline DpK dp_constants() { return DpK{1, -1, 4, 32, 128, -65536}; }
+inline DpK dp_constants() { return DpK{1, -1, 4, -65536}; }
 
 struct LinDpArgs {
   int n;
@@ -68,7 +68,7 @@ struct LinDpArgs {
   int fuse_tb;
   int *batch_done;
   LinTbArgs tb;
-  DpK k;  // multiplier constants (1, -1, 4, 32, 128, -65536)
+  DpK k;  // multiplier constants (1, -1, 4, -65536)
 };
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
