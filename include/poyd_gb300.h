@@ -118,7 +118,10 @@ int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uint8_t *seq,
  *           median_2_with_gaps (algn.c:4011-4024);
  *   affine: align_affine_3 (algn.c:2551-2619).
  * Pair i owns the device slot out + out_off[i] of 4*cap_i bytes,
- * cap_i = a_len[i] + b_len[i] + 2, split in four right-aligned sequences:
+ * cap_i = a_len[i] + b_len[i] + 2 rounded up to a multiple of 4 (the longest
+ * alignment plus the leading gap; the rounding keeps every pair's outputs
+ * word aligned alike when out_off[i] is a multiple of 4), split in four
+ * right-aligned sequences:
  *   [0, cap)      aligned a         (align_2's s1p / affine resi)
  *   [cap, 2cap)   aligned b         (s2p / resj)
  *   [2cap, 3cap)  median with gaps  (median_2_with_gaps / medianwg)

@@ -133,8 +133,9 @@ class PairBatch:
         return cls(*t)
 
     def out_layout(self):
-        """Per-pair output slot offsets (4 sequences of cap = la + lb + 2)."""
-        cap = self.a_len.to(torch.int64) + self.b_len.to(torch.int64) + 2
+        """Per-pair output slot offsets: 4 sequences of cap = la + lb + 2
+        rounded up to a multiple of 4 (the library's slot_cap)."""
+        cap = (self.a_len.to(torch.int64) + self.b_len.to(torch.int64) + 2 + 3) // 4 * 4
         sizes = 4 * cap
         off = torch.zeros_like(sizes)
         off[1:] = torch.cumsum(sizes, 0)[:-1]
@@ -219,7 +220,7 @@ class AlignResult:
             raise native.PoydError(-3, "traceback left the band for pair(s) "
                                    f"{torch.nonzero(ln[:, 0] < 0).flatten()[:8].tolist()}")
         packed = torch.empty(max(total, 16), dtype=torch.uint8, device=dev)
-        a_len = (self.cap - 2).to(torch.int32)  # a_len + b_len; split is irrelevant to cap
+        a_len = (self.cap - 2).to(torch.int32)  # slot_cap(cap - 2, 0) == cap
         zeros = torch.zeros_like(a_len)
         check(lib().poyd_pack_alignments(
             n, self.out.data_ptr(), self.out_off.data_ptr(), a_len.data_ptr(), zeros.data_ptr(),

@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
   const AffPlan P = A.plans[id];
   const int li = P.leni + 1, lj = P.lenj + 1;
   const int la = P.swap ? lj : li, lb = P.swap ? li : lj;
-  const int64_t cap = (int64_t)la + lb + 2;
+  const int64_t cap = slot_cap(la, lb);
   uint8_t *oa = A.out + A.out_off[id];
   uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
   const uint8_t *si = A.seq + P.si_off, *sj = A.seq + P.sj_off;

@@ -144,7 +144,7 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   const LinPlan P = A.plans[id];
   const int gap = A.gap;
   const int la = P.swap ? P.l2 : P.l1, lb = P.swap ? P.l1 : P.l2;
-  const int64_t cap = (int64_t)la + lb + 2;
+  const int64_t cap = slot_cap(la, lb);
   uint8_t *oa = A.out + A.out_off[id];
   uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
   const uint8_t *s1 = A.seq + P.s1_off, *s2 = A.seq + P.s2_off;
@@ -670,7 +670,7 @@ __global__ void k_pack_alignments(int n, const uint8_t *out, const int64_t *out_
   const int lane = threadIdx.x & 31;
   const int64_t id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (id >= n) return;
-  const int64_t cap = (int64_t)a_len[id] + b_len[id] + 2;
+  const int64_t cap = slot_cap(a_len[id], b_len[id]);
   const int64_t na = out_len[2 * id], nm = out_len[2 * id + 1];
   const uint8_t *src = out + out_off[id];
   uint8_t *dst = packed + packed_off[id];

@@ -30,6 +30,15 @@ __host__ __device__ constexpr int lin_dm_words(int mode) {
   return mode == kDpSets ? 3 * kRows : (mode == kDpChoice ? 2 * kRows : 0);
 }
 
+// Capacity of each of the four right-aligned output sequences of a batched
+// align_2 pair: la + lb + 2 (the longest alignment plus the leading gap),
+// rounded up to a multiple of 4 so that every pair's outputs are word
+// aligned alike (the tracebacks' word-buffered writers then flush in step
+// across a warp).
+__host__ __device__ inline int64_t slot_cap(int64_t la, int64_t lb) {
+  return (la + lb + 2 + 3) & ~(int64_t)3;
+}
+
 // Per-pair plan of the linear banded DP, produced on the device.
 struct LinPlan {
   int64_t s1_off, s2_off;  // rows (longer) and columns sequences

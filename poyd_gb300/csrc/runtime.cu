@@ -398,7 +398,7 @@ extern "C" int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8
   DevTables *tabs = nullptr;
   int rc = upload_tables_ws(w, cm, &tabs, mat->st);
   if (rc) return rc;
-  const int64_t slot = (int64_t)l1 + l2 + 2;
+  const int64_t slot = slot_cap(l1, l2);
   const size_t tail = ((size_t)4 * slot + 63) & ~(size_t)63;
   uint8_t *out = (uint8_t *)ws_buffer(w, WS_OUT, tail + 64);
   if (!out) return fail(POYD_ENOMEM, "backtrack output allocation failed");
@@ -450,12 +450,12 @@ static int affine_one(const uint8_t *si, int32_t li, const uint8_t *sj, int32_t 
   OnePair P;
   rc = stage_pair(w, si, li, sj, lj, 0, &P, st);
   if (rc) return rc;
-  const int64_t slot = (int64_t)li + lj + 2;
+  const int64_t slot = slot_cap(li, lj);
   uint8_t *out = nullptr;
   int32_t *olen = nullptr;
   int64_t *ooff = nullptr;
   if (align) {
-    if (cap < slot) return fail(POYD_ERANGE, "output capacity below len(si) + len(sj) + 2");
+    if (cap < (int64_t)li + lj + 2) return fail(POYD_ERANGE, "output capacity below len(si) + len(sj) + 2");
     const size_t tail = ((size_t)4 * slot + 63) & ~(size_t)63;
     out = (uint8_t *)ws_buffer(w, WS_OUT, tail + 64);
     if (!out) return fail(POYD_ENOMEM, "affine output allocation failed");

@@ -41,7 +41,7 @@ def dm_bytes_estimate(la: int, lb: int) -> int:
     l1, l2 = max(la, lb), min(la, lb)
     band = (l1 - l2) + 2 * (50 + int(0.05 * l1) + 8) + 100
     band = min(band, l1 + l2)
-    return ((l1 + 63) // 64) * 64 * (band + 128) // 2 + 4 * (la + lb + 2)
+    return ((l1 + 63) // 64) * 64 * (band + 128) // 2 + 4 * (la + lb + 5)
 
 
 class SequencePool:
