@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -192,58 +193,84 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
   if (hwd[n] & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
   if (hwd[n] & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
-  std::vector<int64_t> off((size_t)n);
-  int64_t total = 0;
   int maxwd = 1;
-  for (int32_t i = 0; i < n; ++i) {
-    off[i] = total;
-    if (want_align) total += hw[i];
-    maxwd = std::max(maxwd, hwd[i]);
-  }
+  for (int32_t i = 0; i < n; ++i) maxwd = std::max(maxwd, hwd[i]);
   // longest first: dm_words ~ strips x band steps is the band area
   std::vector<int32_t> order;
   longest_first(hw, order);
+  // Waves: consecutive runs of that order whose direction matrices fit the
+  // device-memory budget, one persistent launch each (one wave when the
+  // whole batch fits, the usual case).  The single-pair protocol (out ==
+  // nullptr) keeps its one matrix for the later backtrack.
+  int64_t budget = INT64_MAX;
+  if (want_align && out) {
+    size_t freeb = 0, totb = 0;
+    cudaMemGetInfo(&freeb, &totb);
+    budget = (int64_t)((double)(freeb + w->size[WS_DM]) * 0.8);
+    if (const char *e = std::getenv("POYD_DM_BUDGET_BYTES")) budget = std::atoll(e);
+    budget = std::max<int64_t>(budget / 4, 1);  // in 32-bit words
+  }
+  std::vector<int32_t> wave_at{0};
+  int64_t wave_words = 0, max_words = 1;
+  for (int32_t p = 0; p < n; ++p) {
+    const int64_t x = want_align ? hw[order[p]] : 0;
+    if (p > wave_at.back() && wave_words + x > budget) {
+      wave_at.push_back(p);
+      wave_words = 0;
+    }
+    wave_words += x;
+    max_words = std::max(max_words, wave_words);
+  }
+  wave_at.push_back(n);
   int64_t *doff = dmw + n;
   int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
   int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
   if (!dord || !counter) return fail(POYD_ENOMEM, "order allocation failed");
-  CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(dord, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(counter, 0, 4, st));
   uint32_t *dm = nullptr;
   if (want_align) {
-    dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)std::max<int64_t>(total, 1));
+    dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)max_words);
     if (!dm) return fail(POYD_ENOMEM, "direction matrix allocation (%lld bytes) failed",
-                         (long long)(total * 4));
+                         (long long)(max_words * 4));
   }
   const int blocks = lin_dp_blocks(mode);
   const int64_t slab = maxwd + 64;
   int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * kDpWarps);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
-  LinTbArgs TA;
-  TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
-  TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
-  TA.swaped = -1; TA.mode = mode; TA.order = dord;
   // Batched align_2 with backtrack moves: the traceback runs inside the DP
   // kernel, batch by batch as their fills complete.
   const bool fuse = want_align && out && mode == kDpChoice;
   int *batch_done = nullptr;
   if (fuse) {
-    const size_t nb = ((size_t)n + kLanes - 1) / kLanes;
-    batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * nb);
+    batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * (((size_t)n + kLanes - 1) / kLanes));
     if (!batch_done) return fail(POYD_ENOMEM, "batch counter allocation failed");
-    CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * nb, st));
   }
-  LinDpArgs DA;
-  DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
-  DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
-  DA.cost = cost; DA.swaped = -1;
-  DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
-  { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
-  CK(cudaGetLastError());
-  if (want_align && out && !fuse) {  // out == nullptr: keep the DM for a later backtrack
-    { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
+  std::vector<int64_t> off((size_t)n, 0);
+  for (size_t v = 0; v + 1 < wave_at.size(); ++v) {
+    const int32_t p0 = wave_at[v], p1 = wave_at[v + 1], m = p1 - p0;
+    int64_t total = 0;
+    for (int32_t p = p0; p < p1; ++p) {
+      off[order[p]] = total;
+      if (want_align) total += hw[order[p]];
+    }
+    CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(counter, 0, 4, st));
+    if (fuse) CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * (((size_t)m + kLanes - 1) / kLanes), st));
+    LinTbArgs TA;
+    TA.n = m; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
+    TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+    TA.swaped = -1; TA.mode = mode; TA.order = dord + p0;
+    LinDpArgs DA;
+    DA.n = m; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord + p0;
+    DA.tables = tabs; DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch;
+    DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
+    DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
+    { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
     CK(cudaGetLastError());
+    if (want_align && out && !fuse) {
+      { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }
+      CK(cudaGetLastError());
+    }
   }
   return POYD_OK;
 }

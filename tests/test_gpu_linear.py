@@ -170,3 +170,20 @@ def test_packed_results_equal_slots():
         assert r["cost"] == p["cost"]
         for k in ("a", "b", "median_wg", "median"):
             assert np.array_equal(r[k], p[k]), k
+
+
+def test_direction_matrix_waves_match_one_launch(monkeypatch):
+    """A batch whose direction matrices exceed the device budget runs in
+    waves of the longest-first order; the results are those of one launch."""
+    A, B = _random_pairs(91, 80, 700)
+    cm = align.CostMatrix.dna(1, 2)
+    batch = align.PairBatch.from_host(A, B)
+    ref = align.align_2(batch, cm, dos_empty=True).to_host()
+    monkeypatch.setenv("POYD_DM_BUDGET_BYTES", str(256 * 1024))
+    waved = align.align_2(batch, cm, dos_empty=True).to_host()
+    monkeypatch.delenv("POYD_DM_BUDGET_BYTES")
+    assert len(ref) == len(waved)
+    for r, w in zip(ref, waved):
+        assert r["cost"] == w["cost"]
+        for k in ("a", "b", "median_wg", "median"):
+            assert np.array_equal(r[k], w[k]), k
