@@ -29,4 +29,46 @@ struct BackWriter {
   }
 };
 
+// Three sequences written backwards in step (one byte each per column) whose
+// write positions are congruent modulo 4 (their slots are a multiple of 4
+// bytes apart): one alignment check serves all three.
+struct BackWriter3 {
+  uint8_t *p0, *p1, *p2;
+  uint32_t b0, b1, b2;
+  int pend;
+  __device__ BackWriter3(uint8_t *t0, uint8_t *t1, uint8_t *t2)
+      : p0(t0), p1(t1), p2(t2), b0(0), b1(0), b2(0), pend(0) {}
+  __device__ __forceinline__ void put(uint32_t v0, uint32_t v1, uint32_t v2) {
+    b0 = (b0 << 8) | v0;
+    b1 = (b1 << 8) | v1;
+    b2 = (b2 << 8) | v2;
+    ++pend;
+    if (((uintptr_t)p0 & 3u) == 0) {
+      if (pend == 4) {
+        *(uint32_t *)p0 = b0;
+        *(uint32_t *)p1 = b1;
+        *(uint32_t *)p2 = b2;
+      } else {
+        for (int i = 0; i < pend; ++i) {
+          p0[i] = (uint8_t)(b0 >> (8 * i));
+          p1[i] = (uint8_t)(b1 >> (8 * i));
+          p2[i] = (uint8_t)(b2 >> (8 * i));
+        }
+      }
+      pend = 0;
+    }
+    --p0;
+    --p1;
+    --p2;
+  }
+  __device__ __forceinline__ void flush() {
+    for (int i = 0; i < pend; ++i) {
+      p0[1 + i] = (uint8_t)(b0 >> (8 * i));
+      p1[1 + i] = (uint8_t)(b1 >> (8 * i));
+      p2[1 + i] = (uint8_t)(b2 >> (8 * i));
+    }
+    pend = 0;
+  }
+};
+
 }  // namespace poyd

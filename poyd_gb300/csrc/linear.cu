@@ -140,6 +140,7 @@ __global__ void k_lin_plan(LinPlanArgs A) {
 // (one thread per pair) or, for batched align_2, inside k_lin_dp by the warp
 // that finishes the last DP of a 32-pair batch (one lane per pair).
 // ---------------------------------------------------------------------------
+template <int MODE>
 __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int id) {
   const LinPlan P = A.plans[id];
   const int gap = A.gap;
@@ -163,7 +164,6 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   // backtrack priority (algn.c:3605-3666): the caller's first argument is
   // the rows sequence unless the pair was swapped
   const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
-  const int mode = A.mode;
   int r = P.l1 - 1, j = L2 - 1;
   int n = 0, nm = 0;
   const int wdt = P.wd;
@@ -175,7 +175,10 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   const uint4 *dm4 = (const uint4 *)dm;
   uint4 cur = make_uint4(0, 0, 0, 0);
   int cur_key = -1;
-  BackWriter wa(oa + cap - 1), wb(ob + cap - 1), ww(ow + cap - 1), wm(om + cap - 1);
+  // aligned a, aligned b and median with gaps advance together; their slots
+  // are cap apart (a multiple of 4), so one writer serves the three
+  BackWriter3 wabw(oa + cap - 1, ob + cap - 1, ow + cap - 1);
+  BackWriter wm(om + cap - 1);
   // cell (r, j) ends the walk once r * L2 + j < 0
   while (r > 0 || (r == 0 && j >= 0)) {
     const int k = (r & (kRows - 1)) >> 1, strip = r >> 6;
@@ -187,7 +190,7 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
       break;
     }
     int move;  // 0 align, 1 insert (s2 against a gap), 2 delete
-    if (mode == kDpChoice) {
+    if (MODE == kDpChoice) {
       const int key = blk * kLanes + k;
       if (key != cur_key) {
         cur = dm4[key];
@@ -214,9 +217,7 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
     j -= dj;
     const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
     const int m = med[(ca << 5) | cb];
-    wa.put((uint32_t)ca);
-    wb.put((uint32_t)cb);
-    ww.put((uint32_t)m);
+    wabw.put((uint32_t)ca, (uint32_t)cb, (uint32_t)m);
     if (m != gap) {
       wm.put((uint32_t)m);
       ++nm;
@@ -226,9 +227,7 @@ __device__ __noinline__ void tb_pair(const LinTbArgs &A, const uint8_t *med, int
   // ancestor_2 ends with the leading gap (algn.c:4140-4141)
   wm.put((uint32_t)gap);
   ++nm;
-  wa.flush();
-  wb.flush();
-  ww.flush();
+  wabw.flush();
   wm.flush();
   A.out_len[2 * id] = bad ? -1 : (int32_t)n;
   A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
@@ -239,7 +238,10 @@ __global__ void __launch_bounds__(128) k_lin_traceback(LinTbArgs A) {
   for (int i = threadIdx.x; i < 1024; i += blockDim.x) med[i] = A.tables->median[i];
   __syncthreads();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < A.n) tb_pair(A, med, A.order ? A.order[t] : t);
+  if (t >= A.n) return;
+  const int id = A.order ? A.order[t] : t;
+  if (A.mode == kDpChoice) tb_pair<kDpChoice>(A, med, id);
+  else tb_pair<kDpSets>(A, med, id);
 }
 
 // ---------------------------------------------------------------------------
@@ -652,7 +654,8 @@ __global__ void __launch_bounds__(kDpWarps * 32, 3) k_lin_dp(LinDpArgs A) {
       }
       if (__shfl_sync(kFull, last, 0)) {
         __threadfence();
-        if (lane < size) tb_pair(A.tb, sm.med, A.order ? A.order[b * kLanes + lane] : b * kLanes + lane);
+        if (lane < size)
+          tb_pair<kDpChoice>(A.tb, sm.med, A.order ? A.order[b * kLanes + lane] : b * kLanes + lane);
         __syncwarp();
       }
     }
