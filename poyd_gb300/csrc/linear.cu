@@ -6,25 +6,26 @@
 // (algn.c:4126-4147) and median_2_with_gaps (algn.c:4011-4024).
 //
 // Layout on the GPU.  One warp owns one pair (persistent grid, pairs taken
-// longest-first).  Lane k owns DP rows r0 + 2k and r0 + 2k + 1 of a 64-row
-// strip; the warp sweeps the band in diagonal coordinates d = j - r, which
-// makes the band edges of every row the same two diagonals [dlo, dlo+wd)
-// (the reference's ukk left/right cells).  Lane k handles diagonal d of its
-// first row at step s = d - dlo + 3k and d - 1 of its second row in the same
-// step: the value of the row above at (d+1) -- the "delete" predecessor --
-// arrives from lane k-1 by one shuffle that also carries the column
-// character; the previous shuffle's value is the "align" predecessor and the
-// lane's own previous value the "insert" predecessor.  Lane 0 is fed the
-// previous strip's last row from a register queue that rotates one lane per
-// step and is refilled / flushed with one coalesced 128-byte load / store
-// every 32 steps (the boundary row lives in a per-warp global slab of wd
-// ints).  Cells outside the band or the matrix hold an out-of-band value
-// that removes exactly the moves the reference's edge cells omit.  Costs come
-// from a per-lane profile in shared memory (both row characters' costs
-// against every column character in one word, laid out [char][lane] so a
-// step's 32 lookups hit 32 banks).  Direction information is written per
-// 32-step block with one coalesced store (see the mode notes below); the
-// traceback addresses it by (strip, block, lane).
+// longest-first).  Lane k owns DP rows 64t + 2k and 64t + 2k + 1 of strip t;
+// the warp sweeps the band in diagonal coordinates d = j - r, which makes
+// the band edges of every row the same two diagonals [dlo, dlo+wd) (the
+// reference's ukk left/right cells).  Strips follow one another without a
+// pipeline ramp (the schedule is described at the band DP below): lane k's
+// first row is at band index i at step tW + 3k + i and its second row at
+// i - 1 in the same step.  The value of the row above at (d+1) -- the
+// "delete" predecessor -- arrives from lane k-1 by one shuffle; the previous
+// shuffle's value is the "align" predecessor and the lane's own previous
+// value the "insert" predecessor.  Lane 0 is fed the previous strip's last
+// row from a register queue that rotates one lane per step and is refilled /
+// flushed with one coalesced 128-byte load / store every 32 steps (the
+// boundary row lives in a per-warp global slab of wd ints).  Cells outside
+// the band or the matrix hold an out-of-band value that removes exactly the
+// moves the reference's edge cells omit.  Column characters come from
+// per-warp shared windows, costs from a per-lane profile in shared memory
+// (both row characters' costs against every column character in one word,
+// laid out [char][lane] so a step's 32 lookups hit 32 banks).  Direction
+// information is written per 32-step block with one coalesced store (see
+// the mode notes below); the traceback addresses it by (global block, lane).
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "poyd_internal.h"
