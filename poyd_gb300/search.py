@@ -22,6 +22,10 @@ after a join is recomputed by a full batched downpass, which alone decides
 acceptance.  Batching a pass changes which improving tree is found first
 (the reference accepts sequentially), not the cost of any tree.
 
+:func:`root_costs` diagnoses a tree as the reference reports it: the tree
+cost under every rooting (every directed subtree median, then every
+edge's root median, batched), the reported cost being the cheapest.
+
 Backends: :class:`GpuBackend` runs the CUDA kernels; the oracle backend in
 tests/ implements the same interface on the CPU restatement, so a search
 driven through either yields identical trees, costs and node medians.
@@ -127,6 +131,15 @@ class Tree:
             if v >= self.n:
                 stack.extend(self.kids[v])
         return out
+
+    def min_codes(self) -> np.ndarray:
+        """Smallest leaf id under every node (POY's ``min_child_code``,
+        node.ml:674; a leaf's is its own taxon code)."""
+        mc = np.arange(len(self.parent), dtype=np.int64)
+        for v in self.nodes()[::-1]:
+            if v >= self.n:
+                mc[v] = min(mc[self.kids[v][0]], mc[self.kids[v][1]])
+        return mc
 
     def levels(self):
         """Internal nodes grouped by height (all children before parents)."""
@@ -339,13 +352,23 @@ class Diagnosis:
     total: int = 0
 
 
+def _by_code(a, b, mc):
+    """Median argument order of ``Node.cs_median`` (node.ml:344-349): the
+    child holding the smaller taxon code first (DO medians break ties by
+    argument order)."""
+    a = np.asarray(a, np.int64)
+    b = np.asarray(b, np.int64)
+    sw = np.asarray(mc[a] > mc[b])
+    return np.where(sw, b, a), np.where(sw, a, b)
+
+
 def downpass(tree: Tree, be, nodes=None) -> Diagnosis:
     """Preliminary medians of every internal node, one batch per height."""
     d = Diagnosis()
+    mc = tree.min_codes()
     for level in tree.levels():
         lv = np.array(level, np.int64)
-        a = tree.kids[lv, 0]
-        b = tree.kids[lv, 1]
+        a, b = _by_code(tree.kids[lv, 0], tree.kids[lv, 1], mc)
         do, fi = be.medians(a, b, lv)
         for i, v in enumerate(level):
             d.do_cost[v] = int(do[i])
@@ -522,6 +545,7 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
     (node, scratch slot, DO cost, Fitch cost) of trial m's recomputed nodes,
     for commit_move; the caller then releases the slots."""
     h_base = _heights(t)
+    mc_base = t.min_codes()
     base_sank = be.sank_cost(t.root)
     tid_next = 2 * t.n
     recs = {}      # level -> list of (trial, a_ref, b_ref, out_tid)
@@ -547,10 +571,15 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
                 h[v] = 1 + max(height(T.kids[v][0]), height(T.kids[v][1]))
             return h[v]
 
+        mc = {}   # min codes of the trial tree's dirty nodes
+        code = lambda c: mc[c] if c in dirty else mc_base[c]
         for v in sorted(dirty, key=height):
             tid[v] = tid_next
             tid_next += 1
             a, b = T.kids[v]
+            if code(a) > code(b):
+                a, b = b, a
+            mc[v] = code(a)
             ref = lambda c: tid[c] if c in dirty else c
             recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v], v))
             old[m] += diag.do_cost[v] + diag.fitch_cost[v]
@@ -582,3 +611,115 @@ def commit_move(be, diag: Diagnosis, rows, total: int):
         diag.fitch_cost[v] = fi
     diag.total = int(total)
 
+
+
+# ---------------------------------------------------------------------------
+# All-rootings diagnosis
+# ---------------------------------------------------------------------------
+@dataclass
+class RootCosts:
+    edges: np.ndarray   # [m, 2] undirected edges (u < v) of the unrooted tree
+    costs: np.ndarray   # [m] tree cost when rooted on each edge
+
+    def best(self):
+        """(cost, edge) of the cheapest rooting (first edge on ties)."""
+        k = int(np.argmin(self.costs))
+        return int(self.costs[k]), (int(self.edges[k, 0]), int(self.edges[k, 1]))
+
+
+def unrooted_adjacency(tree: Tree) -> dict:
+    """Neighbours of every node of `tree` taken as unrooted: the root's
+    two children are joined by one edge and the root itself dropped."""
+    n = tree.n
+    nodes = tree.nodes()
+    adj = {v: [] for v in nodes}
+    for v in nodes:
+        if v >= n:
+            for c in tree.kids[v]:
+                adj[v].append(int(c))
+                adj[int(c)].append(v)
+    r = tree.root
+    if r >= n:
+        a, b = (int(x) for x in tree.kids[r])
+        adj[a].remove(r)
+        adj[b].remove(r)
+        adj[a].append(b)
+        adj[b].append(a)
+        del adj[r]
+    return adj
+
+
+def root_costs(tree: Tree, be) -> RootCosts:
+    """The reference's tree diagnosis in its default cost mode: the median
+    of every directed subtree -- both directions of every edge, children
+    before parents, one batch per subtree height (``internal_downpass``,
+    allDirChar.ml:722-786) -- then the root median on every edge, one
+    batch (``refresh_all_edges``).  The reference roots the tree on the
+    edge of lowest root cost (``pick_best_root`` with
+    ``blindly_trust_downpass``, allDirChar.ml:791-869) and reports that
+    cost; ``RootCosts.best()`` gives it.  Medians take their arguments in
+    ``min_child_code`` order (node.ml:344-349).
+
+    Scratch node ids from 2 * tree.n hold the directed medians; they are
+    released on return."""
+    n = tree.n
+    adj = unrooted_adjacency(tree)
+    if len(adj) < 2:
+        return RootCosts(np.zeros((0, 2), np.int64), np.zeros(0, np.int64))
+    # directed subtree (u seen from v): height, min code, node id, children
+    info = {}
+    nxt = 2 * n
+    for u0 in adj:
+        for v0 in adj[u0]:
+            stack = [(u0, v0)]
+            while stack:
+                u, v = stack[-1]
+                if (u, v) in info:
+                    stack.pop()
+                    continue
+                if u < n:
+                    info[(u, v)] = (0, u, u, None)
+                    stack.pop()
+                    continue
+                kids = [(c, u) for c in adj[u] if c != v]
+                todo = [k for k in kids if k not in info]
+                if todo:
+                    stack.extend(todo)
+                    continue
+                k1, k2 = kids
+                if info[k1][1] > info[k2][1]:
+                    k1, k2 = k2, k1
+                info[(u, v)] = (1 + max(info[k1][0], info[k2][0]), info[k1][1], nxt, (k1, k2))
+                nxt += 1
+                stack.pop()
+    edges = sorted({(min(u, v), max(u, v)) for u in adj for v in adj[u]})
+    be.ensure_nodes(nxt + len(edges))
+    cost = {e: 0 for e, x in info.items() if x[3] is None}
+    levels = {}
+    for e, x in info.items():
+        if x[3] is not None:
+            levels.setdefault(x[0], []).append(e)
+    for h in sorted(levels):
+        es = levels[h]
+        a = np.array([info[info[e][3][0]][2] for e in es], np.int64)
+        b = np.array([info[info[e][3][1]][2] for e in es], np.int64)
+        out = np.array([info[e][2] for e in es], np.int64)
+        do, fi = be.medians(a, b, out)
+        for i, e in enumerate(es):
+            k1, k2 = info[e][3]
+            cost[e] = cost[k1] + cost[k2] + int(do[i]) + int(fi[i])
+    a, b, base = [], [], []
+    for u, v in edges:
+        d1, d2 = (u, v), (v, u)
+        if info[d1][1] > info[d2][1]:
+            d1, d2 = d2, d1
+        a.append(info[d1][2])
+        b.append(info[d2][2])
+        base.append(cost[d1] + cost[d2])
+    out = np.arange(nxt, nxt + len(edges), dtype=np.int64)
+    do, fi = be.medians(np.array(a, np.int64), np.array(b, np.int64), out)
+    tot = np.array(base, np.int64) + do + fi
+    if getattr(be, "ns", 0):
+        tot = tot + np.array([be.sank_cost(int(v)) for v in out], np.int64)
+    be.release_nodes(2 * n)
+    return RootCosts(np.array(edges, np.int64).reshape(-1, 2), tot)

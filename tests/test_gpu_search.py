@@ -38,3 +38,22 @@ def test_wagner_and_spr_match_oracle(seed, n_fitch, n_sank):
         (so.cost_before, so.cost_after, so.moves_accepted)
     assert sg.cost_after <= sg.cost_before
     _compare_nodes(tg, g, o)
+
+
+@pytest.mark.parametrize("seed,n_fitch,n_sank,sub,indel,go", [(11, 0, 0, 1, 2, -1),
+                                                              (12, 40, 8, 1, 2, -1),
+                                                              (13, 0, 0, 1, 1, -1),
+                                                              (14, 0, 0, 2, 1, 1)])
+def test_root_costs_match_oracle(seed, n_fitch, n_sank, sub, indel, go):
+    """All-rootings diagnosis (every directed subtree median, then every
+    edge's root median) through the CUDA kernels equals the oracle's, for
+    linear matrices and an affine one (gap opening 1)."""
+    data = simulate.simulate(seed, 24, 400, n_fitch, n_sank)
+    g = search.GpuBackend(data, align.CostMatrix.dna(sub, indel, go if go >= 0 else None))
+    o = OracleBackend(data, O.cm_dna(sub, indel, go))
+    t, diag = search.wagner(data.n_taxa, o)
+    rg = search.root_costs(t, g)
+    ro = search.root_costs(t, o)
+    assert np.array_equal(rg.edges, ro.edges)
+    assert np.array_equal(rg.costs, ro.costs)
+    assert rg.best() == ro.best() and rg.best()[0] <= diag.total
