@@ -149,6 +149,28 @@ int poyd_pack_alignments(int32_t n, const uint8_t *out, const int64_t *out_off,
                          const int32_t *out_len, uint8_t *packed,
                          const int64_t *packed_off, void *stream);
 
+/* Batched Sequence.Align.closest (sequence.ml:967-1033), the final-state
+ * step of DOS.to_single (seqCS.ml:730-745) that AllDirChar.assign_single
+ * runs from the root outwards (allDirChar.ml:288-328): for pair i, the
+ * single sequence of node m_i given its parent's single sequence p_i.
+ * The pair is aligned as by poyd_align_2_batch (same slots, cap_i from
+ * p_len[i] and m_len[i]; cost[i] = that alignment's cost), then every
+ * column of m_i takes its state closest to p_i's column
+ * (Cost_matrix.Two_D.get_closest, cost_matrix.ml:681-698: lowest state
+ * bit among the cheapest), gaps are dropped and the leading gap kept.
+ * Identical sequences are not aligned: their gap bits past position 0
+ * are cleared instead (sequence.ml:1003-1013).  The single sequence is
+ * written right-aligned in the slot's fourth segment [3cap, 4cap) with
+ * its length in out_len[2i+1]; out_len[2i+1] = -1 if the alignment
+ * failed, -2 if a column has no state.  m_i all gaps gives m_i.  With
+ * POYD_FLAG_DOS_EMPTY, a parent that is all gaps is replaced by m_i
+ * (DOS.to_single's rule).  Needs a matrix with combinations. */
+int poyd_closest_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                       const int64_t *p_off, const int32_t *p_len,
+                       const int64_t *m_off, const int32_t *m_len,
+                       int32_t *cost, uint8_t *out, const int64_t *out_off,
+                       int32_t *out_len, int32_t flags, void *stream);
+
 /* ---------------------------------------------------------------------
  * Single-pair drop-ins with the OCaml externals' argument order
  * (sequence.ml:453-466, 731-758).  Host pointers; each call runs the

@@ -93,6 +93,7 @@ def lib():
                                         C.POINTER(C.c_int)]
         L.or_dos_median.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), u8p,
                                     C.POINTER(C.c_int), u8p, u8p, u8p, C.POINTER(C.c_int)]
+        L.or_closest.argtypes = [u8p, C.c_int, u8p, C.c_int, C.POINTER(OrCM), C.c_int, u8p]
         L.or_dos_median_many.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OrCM),
                                          C.c_void_p]
@@ -265,6 +266,17 @@ def dos_median(a, b, m):
                             C.byref(lm), _ptr(ra), _ptr(rb), _ptr(wg), C.byref(la))
     return (c, sm[:lm.value].copy(), ra[:la.value].copy(), rb[:la.value].copy(),
             wg[:la.value].copy())
+
+
+def closest(parent, mine, m, dos_empty: bool = True):
+    """DOS.to_single (dos_empty) / Sequence.Align.closest: the single
+    sequence of `mine` given its parent's single sequence."""
+    p, s = _u8(parent), _u8(mine)
+    out = np.zeros(len(p) + len(s) + 2, np.uint8)
+    n = lib().or_closest(_ptr(p), len(p), _ptr(s), len(s), C.byref(m), int(dos_empty), _ptr(out))
+    if n < 0:
+        raise ValueError("closest: a column of `mine` has no states")
+    return out[:n].copy()
 
 
 def nonadd_median(a, b):

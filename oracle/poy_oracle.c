@@ -761,6 +761,69 @@ int or_dos_median(const uint8_t *a, int la, const uint8_t *b, int lb,
 }
 
 /* ------------------------------------------------------------------------ */
+/* DOS.to_single (seqCS.ml:730-745) over Sequence.Align.closest             */
+/* (sequence.ml:967-1033), combinations on (combine = 1)                    */
+/* ------------------------------------------------------------------------ */
+
+/* Cost_matrix.Two_D.get_closest (cost_matrix.ml:681-698): the state of b
+ * closest to a; the states are tried lowest bit first (list_of_bits is
+ * built high bit first and reversed) and the first strict minimum wins.
+ * Returns -1 where b has no state ("No bits on?"). */
+static int or_get_closest(const or_cm *m, int a, int b) {
+    int gap = m->gap, best = a, bc = 0, found = 0, x;
+    if (a != gap && b != gap) b = ((a & gap) && (b & gap)) ? gap : (b & ~gap);
+    for (x = 0; x < m->lcm; x++) {
+        int v = 1 << x;
+        if (b & v) {
+            int c = m->cost[TBL(a, v)];
+            if (!found || c < bc) { best = v; bc = c; found = 1; }
+        }
+    }
+    return found ? best : -1;
+}
+
+/* The single sequence of `mine` given its parent's single `parent`.
+ * dos_empty selects DOS.to_single's rules (mine all gaps -> mine; parent
+ * all gaps -> closest(mine, mine)); without it, Sequence.Align.closest's
+ * (mine all gaps -> mine).  Returns the length written to `out`
+ * (capacity lp + lm + 2), or -1 on a column without states. */
+int or_closest(const uint8_t *parent, int lp, const uint8_t *mine, int lm,
+               const or_cm *m, int dos_empty, uint8_t *out) {
+    int gap = m->gap, n, i, k = 0;
+    uint8_t *ra, *rb;
+    if (is_empty(mine, lm, gap)) { memcpy(out, mine, (size_t)lm); return lm; }
+    if (dos_empty && is_empty(parent, lp, gap)) { parent = mine; lp = lm; }
+    ra = (uint8_t *)malloc((size_t)lp + lm + 2);
+    rb = (uint8_t *)malloc((size_t)lp + lm + 2);
+    if (lp == lm && memcmp(parent, mine, (size_t)lm) == 0) {
+        /* identical: no alignment, the gap bit cleared past position 0 */
+        n = lm;
+        for (i = 0; i < n; i++) {
+            ra[i] = (uint8_t)(i > 0 ? (parent[i] & ~gap) : parent[i]);
+            rb[i] = (uint8_t)(i > 0 ? (mine[i] & ~gap) : mine[i]);
+        }
+    } else if (m->cost_model == 1) {
+        uint8_t *md = (uint8_t *)malloc((size_t)lp + lm + 2);
+        uint8_t *mw = (uint8_t *)malloc((size_t)lp + lm + 2);
+        int lmd, lmw;
+        or_align_affine_3(parent, lp, mine, lm, m, md, &lmd, mw, &lmw, ra, rb, &n);
+        free(md);
+        free(mw);
+    } else {
+        or_align_2(parent, lp, mine, lm, m, ra, rb, &n);
+    }
+    out[k++] = (uint8_t)gap;
+    for (i = 0; i < n; i++) {
+        int v = or_get_closest(m, ra[i], rb[i]);
+        if (v < 0) { k = -1; break; }
+        if (v != gap) out[k++] = (uint8_t)v;
+    }
+    free(ra);
+    free(rb);
+    return k;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Fitch (nonaddCSc.c, CHARSIZE 8)                                          */
 /* ------------------------------------------------------------------------ */
 

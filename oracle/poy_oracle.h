@@ -133,6 +133,13 @@ int or_dos_median(const uint8_t *a, int la, const uint8_t *b, int lb,
                   const or_cm *m, uint8_t *seqm, int *lm, uint8_t *ra,
                   uint8_t *rb, uint8_t *medwg, int *lal);
 
+/* ---- DOS.to_single (seqCS.ml:730-745) / Sequence.Align.closest
+ * (sequence.ml:967-1033) ---- */
+/* Single sequence of `mine` given its parent's; writes `out` (capacity
+ * lp + lm + 2), returns its length or -1 (a column without states). */
+int or_closest(const uint8_t *parent, int lp, const uint8_t *mine, int lm,
+               const or_cm *m, int dos_empty, uint8_t *out);
+
 /* DOS.median on pairs idx[0..n) of a packed batch (CPU timing driver);
  * returns the total band cells, writes each pair's cost. */
 int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,

@@ -277,6 +277,26 @@ def align_2(batch: PairBatch, cm: CostMatrix, dos_empty: bool = False,
     return AlignResult(cost, out, out_off, out_len, cap, cells)
 
 
+def closest(batch: PairBatch, cm: CostMatrix, dos_empty: bool = True,
+            stream=None) -> AlignResult:
+    """Batched ``Sequence.Align.closest`` (sequence.ml:967-1033): pair i =
+    (parent single sequence a_i, node median b_i) gives the node's single
+    sequence in the ``median`` place of the result (``DOS.to_single``'s
+    empty rules with `dos_empty`, seqCS.ml:730-745); ``cost`` is the
+    alignment cost of the pair."""
+    dev = batch.seq.device
+    out_off, total, cap = batch.out_layout()
+    out = torch.empty(max(total, 16), dtype=torch.uint8, device=dev)
+    cost = torch.empty(batch.n, dtype=torch.int32, device=dev)
+    out_len = torch.empty(2 * batch.n, dtype=torch.int32, device=dev)
+    check(lib().poyd_closest_batch(
+        cm.ref, batch.n, batch.seq.data_ptr(), batch.a_off.data_ptr(), batch.a_len.data_ptr(),
+        batch.b_off.data_ptr(), batch.b_len.data_ptr(), cost.data_ptr(), out.data_ptr(),
+        out_off.data_ptr(), out_len.data_ptr(), native.FLAG_DOS_EMPTY if dos_empty else 0,
+        _stream_handle(stream)))
+    return AlignResult(cost, out, out_off, out_len, cap, None)
+
+
 # ---- single-pair forms with the reference's signatures --------------------
 
 def cost_2_pair(s1, s2, cm: CostMatrix, deltaw: int | None = None) -> int:

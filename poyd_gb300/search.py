@@ -246,13 +246,27 @@ class GpuBackend:
             tmp_s = torch.empty((n, self.ns, self.k), dtype=torch.int32, device=self.dev)
             native.check(L.poyd_sank_median_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
                                                   _p(ia), _p(ib), _p(tmp_s), None, None, st))
-        # move the medians into the pool (one transfer brings the lengths
-        # and both costs to the host)
+        do_cost, f_cost = self._store(res, out, added)
+        oi = torch.from_numpy(np.asarray(out, np.int64)).to(self.dev)
+        if self.nf:
+            self.fitch[oi] = tmp_f
+        if self.ns:
+            self.sank[oi] = tmp_s
+        self.stats["median_pairs"] += n
+        return do_cost, f_cost
+
+    def _store(self, res: align.AlignResult, out, extra=None):
+        """Moves each pair's fourth output sequence (the median, or the
+        single sequence of ``closest``) into the pool as node out_i; one
+        transfer brings the lengths, the costs and `extra` to the host.
+        Returns (costs, extra) as numpy int64."""
+        n = len(out)
         ln = res.out_len.view(-1, 2)[:, 1].to(torch.int64)
-        host = torch.cat([ln, res.cost.to(torch.int64), added]).cpu().numpy()
-        lens, do_cost, f_cost = host[:n], host[n:2 * n], host[2 * n:]
+        parts = [ln, res.cost.to(torch.int64)] + ([extra] if extra is not None else [])
+        host = torch.cat(parts).cpu().numpy()
+        lens, cost = host[:n], host[n:2 * n]
         if n and lens.min() < 0:
-            raise native.PoydError(-3, "median traceback failed")
+            raise native.PoydError(-3, "traceback failed (code %d)" % int(lens.min()))
         src = res.out_off + 4 * res.cap - ln
         dst_off = np.array([self._reserve(int(x)) for x in lens], np.int64)
         total = int(lens.sum())
@@ -262,13 +276,38 @@ class GpuBackend:
         dst = torch.from_numpy(dst_off).to(self.dev)
         self.pool[dst[seg] + pos] = res.out[src[seg] + pos]
         self.off[out], self.len[out] = dst_off, lens.astype(np.int32)
-        oi = torch.from_numpy(np.asarray(out, np.int64)).to(self.dev)
-        if self.nf:
-            self.fitch[oi] = tmp_f
-        if self.ns:
-            self.sank[oi] = tmp_s
-        self.stats["median_pairs"] += n
-        return do_cost, f_cost
+        return cost, (host[2 * n:] if extra is not None else None)
+
+    def singles(self, parent: np.ndarray, node: np.ndarray, out: np.ndarray):
+        """Final-state sequences: out_i = closest(parent_i, node_i)
+        (``DOS.to_single``); Fitch and Sankoff rows are not assigned."""
+        if len(out) == 0:
+            return
+        self._store(align.closest(self._batch(parent, node), self.cm, dos_empty=True), out)
+
+    def _empty(self, v: np.ndarray) -> np.ndarray:
+        """Whether each node's sequence is all gaps (``Sequence.is_empty``)."""
+        v = np.asarray(v, np.int64)
+        ln = self.len[v].astype(np.int64)
+        t = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(self.dev)
+        seg = torch.repeat_interleave(torch.arange(len(v), device=self.dev), t(ln))
+        pos = torch.arange(int(ln.sum()), device=self.dev) - t(np.cumsum(ln) - ln)[seg]
+        idx = t(self.off[v])[seg] + pos
+        nongap = torch.zeros(len(v), dtype=torch.int64, device=self.dev).index_add_(
+            0, seg, (self.pool[idx] != self.cm.gap).to(torch.int64))
+        return (nongap == 0).cpu().numpy()
+
+    def do_distances(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        """``DOS.distance`` (seqCS.ml:819-867) alone between nodes a_i, b_i,
+        with missing distance 0 where either is all gaps."""
+        a = np.asarray(a, np.int64)
+        b = np.asarray(b, np.int64)
+        do, _ = align.cost_2(self._batch(a, b), self.cm, deltaw="dos")
+        do = do.to(torch.int64).cpu().numpy()
+        u, inv = np.unique(np.concatenate([a, b]), return_inverse=True)
+        e = self._empty(u)[inv]
+        do[e[:len(a)] | e[len(a):]] = 0
+        return do
 
     def rebind_nodes(self, dst: np.ndarray, src: np.ndarray):
         """Nodes dst take over the medians computed into nodes src (the
@@ -649,24 +688,22 @@ def unrooted_adjacency(tree: Tree) -> dict:
     return adj
 
 
-def root_costs(tree: Tree, be) -> RootCosts:
-    """The reference's tree diagnosis in its default cost mode: the median
-    of every directed subtree -- both directions of every edge, children
-    before parents, one batch per subtree height (``internal_downpass``,
-    allDirChar.ml:722-786) -- then the root median on every edge, one
-    batch (``refresh_all_edges``).  The reference roots the tree on the
-    edge of lowest root cost (``pick_best_root`` with
-    ``blindly_trust_downpass``, allDirChar.ml:791-869) and reports that
-    cost; ``RootCosts.best()`` gives it.  Medians take their arguments in
-    ``min_child_code`` order (node.ml:344-349).
+@dataclass
+class _AllDir:
+    adj: dict
+    info: dict          # directed subtree (u seen from v) -> (height, min code, node id, children)
+    edges: list         # undirected edges (u < v)
+    root_ids: np.ndarray  # node id of each edge's root median
+    do_cost: np.ndarray   # DO part of each rooting's cost
+    other: np.ndarray     # Fitch + Sankoff part
+    next_id: int          # first node id past the medians
 
-    Scratch node ids from 2 * tree.n hold the directed medians; they are
-    released on return."""
+
+def _all_directions(tree: Tree, be) -> _AllDir | None:
     n = tree.n
     adj = unrooted_adjacency(tree)
     if len(adj) < 2:
-        return RootCosts(np.zeros((0, 2), np.int64), np.zeros(0, np.int64))
-    # directed subtree (u seen from v): height, min code, node id, children
+        return None
     info = {}
     nxt = 2 * n
     for u0 in adj:
@@ -694,7 +731,8 @@ def root_costs(tree: Tree, be) -> RootCosts:
                 stack.pop()
     edges = sorted({(min(u, v), max(u, v)) for u in adj for v in adj[u]})
     be.ensure_nodes(nxt + len(edges))
-    cost = {e: 0 for e, x in info.items() if x[3] is None}
+    cdo = {e: 0 for e, x in info.items() if x[3] is None}
+    cfi = dict(cdo)
     levels = {}
     for e, x in info.items():
         if x[3] is not None:
@@ -707,19 +745,120 @@ def root_costs(tree: Tree, be) -> RootCosts:
         do, fi = be.medians(a, b, out)
         for i, e in enumerate(es):
             k1, k2 = info[e][3]
-            cost[e] = cost[k1] + cost[k2] + int(do[i]) + int(fi[i])
-    a, b, base = [], [], []
+            cdo[e] = cdo[k1] + cdo[k2] + int(do[i])
+            cfi[e] = cfi[k1] + cfi[k2] + int(fi[i])
+    a, b, bdo, bfi = [], [], [], []
     for u, v in edges:
         d1, d2 = (u, v), (v, u)
         if info[d1][1] > info[d2][1]:
             d1, d2 = d2, d1
         a.append(info[d1][2])
         b.append(info[d2][2])
-        base.append(cost[d1] + cost[d2])
+        bdo.append(cdo[d1] + cdo[d2])
+        bfi.append(cfi[d1] + cfi[d2])
     out = np.arange(nxt, nxt + len(edges), dtype=np.int64)
     do, fi = be.medians(np.array(a, np.int64), np.array(b, np.int64), out)
-    tot = np.array(base, np.int64) + do + fi
+    other = np.array(bfi, np.int64) + fi
     if getattr(be, "ns", 0):
-        tot = tot + np.array([be.sank_cost(int(v)) for v in out], np.int64)
-    be.release_nodes(2 * n)
-    return RootCosts(np.array(edges, np.int64).reshape(-1, 2), tot)
+        other = other + np.array([be.sank_cost(int(v)) for v in out], np.int64)
+    return _AllDir(adj, info, edges, out, np.array(bdo, np.int64) + do, other,
+                   nxt + len(edges))
+
+
+def root_costs(tree: Tree, be) -> RootCosts:
+    """The reference's tree diagnosis in its default cost mode: the median
+    of every directed subtree -- both directions of every edge, children
+    before parents, one batch per subtree height (``internal_downpass``,
+    allDirChar.ml:722-786) -- then the root median on every edge, one
+    batch (``refresh_all_edges``).  The reference roots the tree on the
+    edge of lowest root cost (``pick_best_root`` with
+    ``blindly_trust_downpass``, allDirChar.ml:791-869); ``RootCosts.best()``
+    gives it.  Medians take their arguments in ``min_child_code`` order
+    (node.ml:344-349).
+
+    `be` may be a list of backends, one per character set (e.g. one per
+    '#' fragment): their costs add up per rooting.  Scratch node ids from
+    2 * tree.n hold the directed medians; they are released on return."""
+    bes = list(be) if isinstance(be, (list, tuple)) else [be]
+    tot = None
+    for b in bes:
+        D = _all_directions(tree, b)
+        if D is None:
+            return RootCosts(np.zeros((0, 2), np.int64), np.zeros(0, np.int64))
+        b.release_nodes(2 * tree.n)
+        tot = D.do_cost + D.other if tot is None else tot + D.do_cost + D.other
+    return RootCosts(np.array(D.edges, np.int64).reshape(-1, 2), tot)
+
+
+@dataclass
+class FinalCost:
+    cost: int           # the tree cost the reference reports
+    root_edge: tuple    # (a, b): a on the handle's side
+    root_cost: int      # the best rooting's downpass cost (pick_best_root)
+
+
+def final_cost(tree: Tree, be) -> FinalCost:
+    """The tree cost the reference reports after a diagnosis
+    (``Ptree.get_cost `Adjusted``, poy_test.ml:43): ``pick_best_root``
+    (see :func:`root_costs`), then ``assign_single``
+    (allDirChar.ml:288-404) and ``check_cost`` (allDirChar.ml:185-212).
+
+    assign_single gives every node a single sequence from the root
+    outwards: the root's is ``closest(root median, a's subtree median)``
+    for the root edge (a, b), a on the handle's side; every node's is
+    ``closest(parent's single, its subtree median seen from the parent)``
+    (``DOS.to_single``, seqCS.ml:730-745), one batch per distance from the
+    root.  check_cost sums ``DOS.distance`` between the single sequences
+    of every edge and adds the rooting's non-DO (Fitch, Sankoff) cost.
+    On the reference's test trees this equals the best rooting's cost for
+    linear matrices and differs (by up to a few percent, either way) for
+    affine ones.
+
+    The tree's own root plays the handle: an edge is oriented from the
+    parent, the root's two children from the first.  Among rootings of
+    equal cost the first edge in (u, v) order is taken."""
+    bes = list(be) if isinstance(be, (list, tuple)) else [be]
+    Ds = [_all_directions(tree, b) for b in bes]
+    if Ds[0] is None:
+        return FinalCost(0, (), 0)
+    tot = sum(D.do_cost + D.other for D in Ds)
+    k = int(np.argmin(tot))
+    D = Ds[0]
+    u, v = D.edges[k]
+    if tree.parent[v] == u:
+        a, b = u, v
+    elif tree.parent[u] == v:
+        a, b = v, u
+    else:
+        a, b = (int(x) for x in tree.kids[tree.root])
+    cost = 0
+    for B, D in zip(bes, Ds):
+        cost += _assign_single_cost(B, D, k, a, b)
+        B.release_nodes(2 * tree.n)
+    return FinalCost(cost, (int(a), int(b)), int(tot[k]))
+
+
+def _assign_single_cost(be, D: _AllDir, k: int, a: int, b: int) -> int:
+    """assign_single from root edge k = (a, b) and check_cost, one
+    backend's characters."""
+    nxt = D.next_id
+    be.ensure_nodes(nxt + 1 + len(D.adj))
+    root = nxt
+    nxt += 1
+    be.singles(np.array([D.root_ids[k]]), np.array([D.info[(a, b)][2]]), np.array([root]))
+    single = {}
+    front = [(a, b, root), (b, a, root)]
+    while front:
+        par = np.array([f[2] for f in front], np.int64)
+        mine = np.array([D.info[(c, p)][2] for c, p, _ in front], np.int64)
+        out = np.arange(nxt, nxt + len(front), dtype=np.int64)
+        nxt += len(front)
+        be.singles(par, mine, out)
+        nf = []
+        for (c, p, _), o in zip(front, out):
+            single[c] = int(o)
+            nf.extend((x, c, int(o)) for x in D.adj[c] if x != p)
+        front = nf
+    ea = np.array([single[x] for x, _ in D.edges], np.int64)
+    eb = np.array([single[y] for _, y in D.edges], np.int64)
+    return int(be.do_distances(ea, eb).sum()) + int(D.other[k])

@@ -56,6 +56,20 @@ class OracleBackend:
             out.append(d + int(tot))
         return np.array(out, np.int64)
 
+    def singles(self, parent, node, out):
+        for p, v, o in zip(parent, node, out):
+            self.seq[int(o)] = O.closest(self.seq[int(p)], self.seq[int(v)], self.om)
+
+    def do_distances(self, a, b):
+        out = []
+        for x, y in zip(a, b):
+            s1, s2 = self.seq[int(x)], self.seq[int(y)]
+            if np.all(s1 == 16) or np.all(s2 == 16):
+                out.append(0)   # missing distance
+            else:
+                out.append(O.cost_2(s1, s2, self.om, max(abs(len(s1) - len(s2)), 8)))
+        return np.array(out, np.int64)
+
     def sank_cost(self, v):
         if not self.ns:
             return 0

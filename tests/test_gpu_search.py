@@ -57,3 +57,17 @@ def test_root_costs_match_oracle(seed, n_fitch, n_sank, sub, indel, go):
     assert np.array_equal(rg.edges, ro.edges)
     assert np.array_equal(rg.costs, ro.costs)
     assert rg.best() == ro.best() and rg.best()[0] <= diag.total
+
+
+@pytest.mark.parametrize("sub,indel,go", [(1, 2, -1), (2, 1, 1), (3, 1, 5)])
+def test_final_cost_matches_oracle(sub, indel, go):
+    """Best rooting, single-state assignment and the edge-distance sum
+    through the CUDA kernels equal the oracle's, with two DO character
+    sets sharing one root."""
+    sets = [simulate.simulate(s, 20, 300) for s in (21, 22)]
+    cm = align.CostMatrix.dna(sub, indel, go if go >= 0 else None)
+    om = O.cm_dna(sub, indel, go)
+    t, _ = search.wagner(sets[0].n_taxa, OracleBackend(sets[0], om))
+    fg = search.final_cost(t, [search.GpuBackend(d, cm) for d in sets])
+    fo = search.final_cost(t, [OracleBackend(d, om) for d in sets])
+    assert (fg.cost, fg.root_edge, fg.root_cost) == (fo.cost, fo.root_edge, fo.root_cost)

@@ -1,19 +1,20 @@
 """Tree-level parity: the reference's own whole-tree cost tests.
 
-test/cost_tests:11-12 read each of test/1.fas .. 13.fas (every
-'#'-separated fragment a DO character), read a fixed tree
-(test/N.fas.tree for cc.poy with the default sub 1 / indel 2 matrix,
-test/N.fas.1.tree for cc1.poy after ``transform (tcm:(1,1))``) and compare
-the diagnosed tree cost with test/cc.costs and test/cc1.costs.  Here the
-same files are diagnosed with the all-rootings diagnosis over the oracle's
-DO medians (the backend the CUDA kernels match bit for bit): the cost of
-the best rooting, summed over the fragments with one root for all, must
-equal the golden cost.  The files are read where the reference tree is
-present and the test skips elsewhere; nothing of them is stored here.
+test/cost_tests:11-14 read each of test/1.fas .. 13.fas (every
+'#'-separated fragment a DO character), read a fixed tree and compare the
+tree cost poy_test reports (``Ptree.get_cost `Adjusted``, poy_test.ml:43)
+with a golden file:
 
-The affine models (cc2.poy, cc3.poy) are not covered: there the reported
-cost comes from the final-state assignment (``assign_single``), which is
-not restated."""
+  cc.poy   default matrix (sub 1, indel 2)          N.fas.tree    cc.costs
+  cc1.poy  transform (tcm:(1,1))                     N.fas.1.tree  cc1.costs
+  cc2.poy  transform (tcm:(2,1), gap_opening:1)      N.fas.2.tree  cc2.costs
+  cc3.poy  transform (tcm:(3,1), gap_opening:5)      N.fas.3.tree  cc3.costs
+
+Here the same files go through ``search.final_cost`` (best rooting, then
+single-state assignment and the edge-distance sum) over the oracle's DO
+medians, the backend the CUDA kernels match bit for bit.  The files are
+read where the reference tree is present and the test skips elsewhere;
+nothing of them is stored here."""
 import os
 
 import numpy as np
@@ -26,18 +27,14 @@ from tests.oracle_backend import OracleBackend
 REF_TEST = os.environ.get("POYD_REFERENCE_TEST", "/root/reference/test")
 have_ref = os.path.exists(os.path.join(REF_TEST, "cc.costs"))
 
-MODELS = {"cc": ((1, 2, -1), "tree"), "cc1": ((1, 1, -1), "1.tree")}
+MODELS = {"cc": ((1, 2, -1), "tree"), "cc1": ((1, 1, -1), "1.tree"),
+          "cc2": ((2, 1, 1), "2.tree"), "cc3": ((3, 1, 5), "3.tree")}
 
 
-def tree_cost(fas, tree_file, om):
+def diagnose(fas, tree_file, om):
     frags = formats.fasta_fragments(fas)
-    names = frags[0].names
-    t = formats.parse_tree(open(tree_file).read(), names)
-    total = None
-    for ds in frags:
-        rc = search.root_costs(t, OracleBackend(ds, om))
-        total = rc.costs if total is None else total + rc.costs
-    return int(total.min())
+    t = formats.parse_tree(open(tree_file).read(), frags[0].names)
+    return search.final_cost(t, [OracleBackend(ds, om) for ds in frags])
 
 
 @pytest.mark.skipif(not have_ref, reason="reference test files not present")
@@ -49,7 +46,7 @@ def test_golden_tree_costs(model):
     got = []
     for f in range(1, len(gold) + 1):
         fas = os.path.join(REF_TEST, "%d.fas" % f)
-        got.append(tree_cost(fas, fas + "." + suffix, om))
+        got.append(diagnose(fas, fas + "." + suffix, om).cost)
     assert got == gold
 
 
@@ -66,6 +63,21 @@ def test_rooted_downpass_is_one_rooting():
     assert int(rc.costs[k[0]]) == diag.total
     assert len(rc.edges) == 2 * data.n_taxa - 3
     assert rc.best()[0] == int(rc.costs.min()) <= diag.total
+    fc = search.final_cost(t, be)
+    assert fc.root_cost == rc.best()[0]
+
+
+def test_closest_rules():
+    """DOS.to_single's cases: identical sequences (gap bits cleared, no
+    alignment), an all-gap node (returned as is), an all-gap parent
+    (replaced by the node) and ambiguity resolved towards the parent."""
+    m = O.cm_dna(1, 2, -1)
+    s = np.array([16, 1, 17, 4], np.uint8)
+    assert O.closest(s, s, m).tolist() == [16, 1, 1, 4]
+    assert O.closest(np.array([16, 1], np.uint8), np.array([16, 16], np.uint8), m).tolist() == [16, 16]
+    assert O.closest(np.array([16], np.uint8), np.array([16, 5, 2], np.uint8), m).tolist() == [16, 1, 2]
+    assert O.closest(np.array([16, 4, 2], np.uint8), np.array([16, 5, 2], np.uint8), m).tolist() == [16, 4, 2]
+    assert O.closest(np.array([16, 1, 2], np.uint8), np.array([16, 15, 2], np.uint8), m).tolist() == [16, 1, 2]
 
 
 def test_formats():
