@@ -797,7 +797,7 @@ class FinalCost:
     root_cost: int      # the best rooting's downpass cost (pick_best_root)
 
 
-def final_cost(tree: Tree, be) -> FinalCost:
+def final_cost(tree: Tree, be, weight: int = 1) -> FinalCost:
     """The tree cost the reference reports after a diagnosis
     (``Ptree.get_cost `Adjusted``, poy_test.ml:43): ``pick_best_root``
     (see :func:`root_costs`), then ``assign_single``
@@ -816,7 +816,13 @@ def final_cost(tree: Tree, be) -> FinalCost:
 
     The tree's own root plays the handle: an edge is oriented from the
     parent, the root's two children from the first.  Among rootings of
-    equal cost the first edge in (u, v) order is taken."""
+    equal cost the first edge in (u, v) order is taken.
+
+    `weight` is the characters' weight factor (``transform
+    (weightfactor:w)``; node costs are ``weight * cost``, node.ml:350-357).
+    The root is chosen by absolute cost (allDirChar.ml:794), so the
+    rooting and the single sequences do not depend on it and it scales
+    every cost."""
     bes = list(be) if isinstance(be, (list, tuple)) else [be]
     Ds = [_all_directions(tree, b) for b in bes]
     if Ds[0] is None:
@@ -835,7 +841,7 @@ def final_cost(tree: Tree, be) -> FinalCost:
     for B, D in zip(bes, Ds):
         cost += _assign_single_cost(B, D, k, a, b)
         B.release_nodes(2 * tree.n)
-    return FinalCost(cost, (int(a), int(b)), int(tot[k]))
+    return FinalCost(weight * cost, (int(a), int(b)), weight * int(tot[k]))
 
 
 def _assign_single_cost(be, D: _AllDir, k: int, a: int, b: int) -> int:

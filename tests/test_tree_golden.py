@@ -10,6 +10,8 @@ with a golden file:
   cc2.poy  transform (tcm:(2,1), gap_opening:1)      N.fas.2.tree  cc2.costs
   cc3.poy  transform (tcm:(3,1), gap_opening:5)      N.fas.3.tree  cc3.costs
 
+and cnc*.poy repeat them with ``weightfactor:-1`` added (cnc*.costs).
+
 Here the same files go through ``search.final_cost`` (best rooting, then
 single-state assignment and the edge-distance sum) over the oracle's DO
 medians, the backend the CUDA kernels match bit for bit.  The files are
@@ -31,10 +33,10 @@ MODELS = {"cc": ((1, 2, -1), "tree"), "cc1": ((1, 1, -1), "1.tree"),
           "cc2": ((2, 1, 1), "2.tree"), "cc3": ((3, 1, 5), "3.tree")}
 
 
-def diagnose(fas, tree_file, om):
+def diagnose(fas, tree_file, om, weight=1):
     frags = formats.fasta_fragments(fas)
     t = formats.parse_tree(open(tree_file).read(), frags[0].names)
-    return search.final_cost(t, [OracleBackend(ds, om) for ds in frags])
+    return search.final_cost(t, [OracleBackend(ds, om) for ds in frags], weight)
 
 
 @pytest.mark.skipif(not have_ref, reason="reference test files not present")
@@ -43,11 +45,16 @@ def test_golden_tree_costs(model):
     (sub, indel, go), suffix = MODELS[model]
     om = O.cm_dna(sub, indel, go)
     gold = [int(x) for x in open(os.path.join(REF_TEST, model + ".costs")).read().split()]
-    got = []
+    neg = [int(x) for x in open(os.path.join(REF_TEST, "cn" + model[1:] + ".costs")).read().split()]
+    got, got_neg = [], []
     for f in range(1, len(gold) + 1):
         fas = os.path.join(REF_TEST, "%d.fas" % f)
         got.append(diagnose(fas, fas + "." + suffix, om).cost)
+        if f <= 2:   # weightfactor -1 on the small datasets; it scales every cost
+            got_neg.append(diagnose(fas, fas + "." + suffix, om, -1).cost)
     assert got == gold
+    assert got_neg == neg[:len(got_neg)]
+    assert [-c for c in got] == neg
 
 
 def test_rooted_downpass_is_one_rooting():
