@@ -149,6 +149,24 @@ int poyd_pack_alignments(int32_t n, const uint8_t *out, const int64_t *out_off,
                          const int32_t *out_len, uint8_t *packed,
                          const int64_t *packed_off, void *stream);
 
+/* Host-buffer form of poyd_align_2_batch for a caller whose sequences live
+ * in host memory (an OCaml stub over seq blocks, which the reference aligns
+ * one pair per call, sequence.ml:849-869).  seq, a_off, a_len, b_off, b_len
+ * are host arrays (seq in page-locked memory for a fast upload).  The batch
+ * runs as one DP launch.  Its output slots (4*cap_i bytes each, the layout
+ * of poyd_align_2_batch) are laid out in the order the DP finishes them, so
+ * they are downloaded while the DP runs.  The library sets out_off[i]: pair
+ * i's slot starts at out + out_off[i].  out (host, page-locked for overlap)
+ * must hold out_cap >= sum of 4 * cap_i bytes (POYD_ERANGE otherwise).
+ * Synchronous: on return cost[n], out_len[2n] and the slots are in host
+ * memory.  Linear matrices stream; affine ones download after the DP.
+ * Calls on one device are serialised. */
+int poyd_align_2_host(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                      const int64_t *a_off, const int32_t *a_len,
+                      const int64_t *b_off, const int32_t *b_len,
+                      int32_t *cost, uint8_t *out, int64_t out_cap,
+                      int64_t *out_off, int32_t *out_len, int32_t flags);
+
 /* Batched Sequence.Align.closest (sequence.ml:967-1033), the final-state
  * step of DOS.to_single (seqCS.ml:730-745) that AllDirChar.assign_single
  * runs from the root outwards (allDirChar.ml:288-328): for pair i, the

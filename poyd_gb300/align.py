@@ -277,6 +277,40 @@ def align_2(batch: PairBatch, cm: CostMatrix, dos_empty: bool = False,
     return AlignResult(cost, out, out_off, out_len, cap, cells)
 
 
+def host_outputs(parts, pin: bool = True) -> dict:
+    """Host result buffers for :func:`align_2_host` on a batch whose host
+    arrays are `parts` (``PairBatch.pack_host``); reusable across calls."""
+    a_len = torch.as_tensor(parts[2]).to(torch.int64)
+    b_len = torch.as_tensor(parts[4]).to(torch.int64)
+    n = int(a_len.numel())
+    cap = (a_len + b_len + 2 + 3) // 4 * 4
+    mk = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=pin)
+    return {"cost": mk(n, torch.int32), "out_len": mk(2 * n, torch.int32),
+            "out": mk(max(int(4 * cap.sum()), 16), torch.uint8),
+            "out_off": mk(max(n, 1), torch.int64), "cap": cap}
+
+
+def align_2_host(parts, cm: CostMatrix, dos_empty: bool = False,
+                 out: dict | None = None) -> AlignResult:
+    """Batched ``align_2`` from and to host memory (``poyd_align_2_host``):
+    `parts` are the host arrays of ``PairBatch.pack_host`` (page-locked for
+    speed).  The result slots (``align_2``'s layout, at offsets the library
+    chooses) are downloaded while the DP runs; everything is returned in
+    host memory."""
+    parts = [torch.as_tensor(x) for x in parts]
+    seq, a_off, a_len, b_off, b_len = parts
+    assert seq.dtype == torch.uint8 and a_off.dtype == torch.int64 and a_len.dtype == torch.int32
+    n = int(a_len.numel())
+    out = out if out is not None else host_outputs(parts, pin=seq.is_pinned())
+    check(lib().poyd_align_2_host(
+        cm.ref, n, seq.data_ptr(), a_off.data_ptr(), a_len.data_ptr(), b_off.data_ptr(),
+        b_len.data_ptr(), out["cost"].data_ptr(), out["out"].data_ptr(), int(out["out"].numel()),
+        out["out_off"].data_ptr(), out["out_len"].data_ptr(),
+        native.FLAG_DOS_EMPTY if dos_empty else 0))
+    return AlignResult(out["cost"][:n], out["out"], out["out_off"][:n], out["out_len"][:2 * n],
+                       out["cap"], None)
+
+
 def closest(batch: PairBatch, cm: CostMatrix, dos_empty: bool = True,
             stream=None) -> AlignResult:
     """Batched ``Sequence.Align.closest`` (sequence.ml:967-1033): pair i =

@@ -39,7 +39,7 @@ constexpr unsigned kFull = 0xffffffffu;
 // ---------------------------------------------------------------------------
 // Plan: orientation, deltaw, band geometry, DM size and band cell count.
 // ---------------------------------------------------------------------------
-__global__ void k_lin_plan(LinPlanArgs A) {
+__global__ void __launch_bounds__(128, 16) k_lin_plan(LinPlanArgs A) {
   const int lane = threadIdx.x & 31;
   const int id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (id >= A.n) return;
@@ -657,6 +657,12 @@ __global__ void __launch_bounds__(kDpWarps * 32, 3) k_lin_dp(LinDpArgs A) {
         __threadfence();
         if (lane < size)
           tb_pair<kDpChoice>(A.tb, sm.med, A.order ? A.order[b * kLanes + lane] : b * kLanes + lane);
+        if (A.done) {
+          // every lane's results visible to the host before the flag
+          __threadfence_system();
+          __syncwarp();
+          if (lane == 0) *(volatile int *)(A.done + b) = 1;
+        }
         __syncwarp();
       }
     }
@@ -667,7 +673,7 @@ __global__ void __launch_bounds__(kDpWarps * 32, 3) k_lin_dp(LinDpArgs A) {
 // Packing of batched align_2 results: one warp per pair copies the used tail
 // of each of its four right-aligned slots back to back.
 // ---------------------------------------------------------------------------
-__global__ void k_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
+__global__ void __launch_bounds__(128, 16) k_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
                                   const int32_t *a_len, const int32_t *b_len,
                                   const int32_t *out_len, uint8_t *packed,
                                   const int64_t *packed_off) {
@@ -690,7 +696,10 @@ void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
                             const int32_t *a_len, const int32_t *b_len,
                             const int32_t *out_len, uint8_t *packed,
                             const int64_t *packed_off, cudaStream_t st) {
-  const int threads = 256;
+  // 128-thread blocks (<= 32 registers each) fit in the registers a
+  // resident k_lin_dp grid leaves free on every SM, so a pipelined caller's
+  // pack runs beside the next chunk's DP instead of after it
+  const int threads = 128;
   const int64_t blocks = ((int64_t)n * 32 + threads - 1) / threads;
   k_pack_alignments<<<(unsigned)blocks, threads, 0, st>>>(n, out, out_off, a_len, b_len,
                                                           out_len, packed, packed_off);
@@ -700,7 +709,7 @@ void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
 // launchers
 // ---------------------------------------------------------------------------
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st) {
-  const int threads = 256;
+  const int threads = 128;  // fits beside a resident k_lin_dp grid (see above)
   const int64_t blocks = ((int64_t)A.n * 32 + threads - 1) / threads;
   k_lin_plan<<<(unsigned)blocks, threads, 0, st>>>(A);
 }

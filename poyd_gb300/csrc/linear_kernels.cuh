@@ -67,6 +67,9 @@ struct LinDpArgs {
   // traceback with `tb`
   int fuse_tb;
   int *batch_done;
+  // with fuse_tb: done[b] = 1 once batch b's results are written (host-mapped
+  // memory a caller polls to download finished slots early; may be null)
+  int *done;
   LinTbArgs tb;
   DpK k;  // multiplier constants (1, -1, 4, -65536)
 };

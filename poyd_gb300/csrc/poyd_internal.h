@@ -39,6 +39,23 @@ __host__ __device__ inline int64_t slot_cap(int64_t la, int64_t lb) {
   return (la + lb + 2 + 3) & ~(int64_t)3;
 }
 
+// Streamed download of a batched linear align_2 (poyd_align_2_host): the
+// output slots are laid out in the DP's longest-first order, so that the
+// slots of finished batches form a growing prefix the caller downloads
+// while the DP runs.
+struct LinStream {
+  const int32_t *a_len_h, *b_len_h;  // host copies of the lengths
+  int64_t *out_off_host;             // out: slot offset of every pair
+  int64_t *out_off_dev;              // device array receiving the same
+  int *done;                         // device pointer to host-mapped batch flags
+  std::vector<int32_t> order;        // out: the DP order
+  int waves = 0;                     // out: launches (flags are set for one wave only)
+};
+int align_2_streamed(const poyd_cm *cm, int32_t n, const uint8_t *seq, const int64_t *a_off,
+                     const int32_t *a_len, const int64_t *b_off, const int32_t *b_len,
+                     int32_t *cost, uint8_t *out, int32_t *out_len, int32_t flags,
+                     LinStream *ls, cudaStream_t st);
+
 // Per-pair plan of the linear banded DP, produced on the device.
 struct LinPlan {
   int64_t s1_off, s2_off;  // rows (longer) and columns sequences

@@ -161,7 +161,7 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
                         const int32_t *b_len, int32_t policy, const int32_t *deltaw,
                         int32_t *cost, int64_t *cells, bool want_align, int32_t flags,
                         uint8_t *out, const int64_t *out_off, int32_t *out_len,
-                        cudaStream_t st) {
+                        cudaStream_t st, LinStream *ls = nullptr) {
   DevTables *tabs = nullptr;
   int rc = upload_tables_ws(w, cm, &tabs, st);
   if (rc) return rc;
@@ -222,6 +222,19 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     max_words = std::max(max_words, wave_words);
   }
   wave_at.push_back(n);
+  if (ls) {  // output slots in DP order
+    int64_t o = 0;
+    for (int32_t p = 0; p < n; ++p) {
+      const int32_t id = order[p];
+      ls->out_off_host[id] = o;
+      o += 4 * slot_cap(ls->a_len_h[id], ls->b_len_h[id]);
+    }
+    CK(cudaMemcpyAsync(ls->out_off_dev, ls->out_off_host, sizeof(int64_t) * (size_t)n,
+                       cudaMemcpyHostToDevice, st));
+    out_off = ls->out_off_dev;
+    ls->order = order;
+    ls->waves = (int)wave_at.size() - 1;
+  }
   int64_t *doff = dmw + n;
   int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
   int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
@@ -265,6 +278,7 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     DA.tables = tabs; DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch;
     DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
     DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
+    DA.done = (ls && fuse && wave_at.size() == 2) ? ls->done : nullptr;
     { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
     CK(cudaGetLastError());
     if (want_align && out && !fuse) {
@@ -334,6 +348,19 @@ extern "C" int poyd_align_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *s
   return linear_batch(workspace((cudaStream_t)stream), cm, maxc, n, seq, a_off, a_len, b_off, b_len, POYD_DELTAW_DEFAULT,
                       nullptr, cost, band_cells, true, flags, out, out_off, out_len,
                       (cudaStream_t)stream);
+}
+
+int poyd::align_2_streamed(const poyd_cm *cm, int32_t n, const uint8_t *seq, const int64_t *a_off,
+                     const int32_t *a_len, const int64_t *b_off, const int32_t *b_len,
+                     int32_t *cost, uint8_t *out, int32_t *out_len, int32_t flags,
+                     LinStream *ls, cudaStream_t st) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (cm->cost_model == 1) return fail(POYD_EUNSUP, "streamed align_2: linear model only");
+  return linear_batch(workspace(st), cm, maxc, n, seq, a_off, a_len, b_off, b_len,
+                      POYD_DELTAW_DEFAULT, nullptr, cost, nullptr, true, flags, out, nullptr,
+                      out_len, st, ls);
 }
 
 // ---------------------------------------------------------------------------

@@ -56,6 +56,8 @@ SIGNATURES = [
     ("poyd_launch_count", C.c_longlong, []),
     ("poyd_pack_alignments", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("poyd_align_2_host", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    C.c_int64, _vp, _vp, _i32]),
     ("poyd_closest_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _i32, _vp]),
     ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -4,7 +4,7 @@ import pytest
 import torch
 
 from oracle import oracle as O
-from poyd_gb300 import align, synth
+from poyd_gb300 import align, native, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -170,6 +170,47 @@ def test_packed_results_equal_slots():
         assert r["cost"] == p["cost"]
         for k in ("a", "b", "median_wg", "median"):
             assert np.array_equal(r[k], p[k]), k
+
+
+@pytest.mark.parametrize("pin,model,budget", [(True, (1, 2, None), None),
+                                              (False, (1, 1, None), None),
+                                              (True, (1, 2, None), 256 * 1024),
+                                              (True, (2, 1, 1), None)])
+def test_host_buffer_batch_matches_device_batch(pin, model, budget, monkeypatch):
+    """poyd_align_2_host (slots in DP order, downloaded while the DP runs;
+    several direction-matrix waves; affine) returns every pair's results as
+    the device-resident batch does."""
+    rng = np.random.default_rng(model[0] * 7 + model[1])
+    A, B = _random_pairs(50 + model[1], 90, 900)
+    EA, EB = _edge_pairs(rng)
+    A += EA
+    B += EB
+    cm = align.CostMatrix.dna(*model)
+    parts = align.PairBatch.pack_host(A, B, pin=pin)
+    dev = align.align_2(align.PairBatch.from_host(A, B), cm, dos_empty=True).to_host()
+    if budget:
+        monkeypatch.setenv("POYD_DM_BUDGET_BYTES", str(budget))
+    host = align.align_2_host(parts, cm, dos_empty=True)
+    off = host.out_off.numpy()
+    cap = host.cap.numpy()
+    assert len(set(off.tolist())) == len(off)
+    assert np.all(off % 4 == 0) and np.all(off + 4 * cap <= host.out.numel())
+    for d, h in zip(dev, host.to_host()):
+        assert d["cost"] == h["cost"]
+        for k in ("a", "b", "median_wg", "median"):
+            assert np.array_equal(d[k], h[k]), k
+
+
+def test_host_buffer_batch_capacity_checked():
+    A, B = _random_pairs(60, 20, 300)
+    cm = align.CostMatrix.dna(1, 2)
+    parts = align.PairBatch.pack_host(A, B)
+    out = align.host_outputs(parts, pin=False)
+    out["out"] = out["out"][:100]
+    with pytest.raises(native.PoydError):
+        align.align_2_host(parts, cm, out=out)
+    ok = align.align_2_host(parts, cm)
+    assert ok.cost.numel() == len(A)
 
 
 def test_direction_matrix_waves_match_one_launch(monkeypatch):
