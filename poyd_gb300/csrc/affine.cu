@@ -151,10 +151,24 @@ __global__ void k_aff_plan(AffPlanArgs A) {
 // Shared memory of one k_aff_dp block.
 struct AffSmem {
   uint32_t tab[1024];            // packed {cost[a][b], cost[gap][b]}
-  uint8_t win[8][64];            // per warp: the 64 columns of a 32-step block
+  uint16_t cost[1024];           // cost[a][b]
+  int4 col[8][64];               // per warp: the 64 columns of a 32-step block (AffCol)
   int4 ring_in[8][32];           // per warp: lane 0's inputs of the block
   int4 ring_out[8][32];          // per warp: lane 31's states of the block
 };
+
+// Column quantities of column j (algn.c:2321-2328 / 2451-2457), computed
+// once per column when a block's window is staged:
+//   x = hext: the horizontal extension cost into column j
+//   y = sj_open + sj_ext: the horizontal opening cost
+//   z = sj_open
+//   w = sj[j]
+__device__ __forceinline__ int4 aff_column(const uint32_t *tab, int jc, int jp, int j, int go) {
+  const int sj_ext = (int)(tab[jc] >> 16);  // prepend[jc] = cost[gap][jc]
+  const int sj_open = (!(jp & 16) && (jc & 16)) ? 0 : go;
+  const int hext = (j == 1) ? sj_ext : (((jp & 16) && !(jc & 16)) ? sj_open + sj_ext : sj_ext);
+  return make_int4(hext, sj_open + sj_ext, sj_open, jc);
+}
 
 // 16 steps of one strip: cells (i, j = i + d) with d = kDlo + s - 2 * lane at
 // step s = s0 + u.  The four states of row i-1 at column j come from lane
@@ -167,7 +181,8 @@ struct AffSmem {
 // algn_fill_plane_3_aff[_nobt] (algn.c:2124-2248, 2309-2400).
 struct AffRow {
   int ic, ip, si_ext, si_open, si_vext, i;
-  const uint32_t *srow;
+  int icg;                 // ic has the gap bit: all ones, else 0
+  const uint16_t *srow;    // cost[ic & 15][.]
   int uL, uR, uF;  // steps (relative to the half block) of the left / right boundary cell and of the final cell
 };
 struct AffState {
@@ -178,10 +193,13 @@ struct AffState {
   int result;
 };
 
-template <bool BT>
+// ENDS: the strip holds row 0 or the last row (their boundary rules and the
+// final cell are checked only there).
+template <bool BT, bool ENDS>
 __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const AffSmem &sm,
-                                         const uint8_t *wlane, const int4 *rin, int4 *rout,
+                                         const int4 *clane, const int4 *rin, int4 *rout,
                                          int s0, int go, uint32_t *dmb, int lane) {
+  const int v_open = R.si_open + R.si_ext;
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
     int u_eh = __shfl_up_sync(kFullA, S.m_eh, 1);
@@ -192,29 +210,26 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
       const int4 v = rin[u];
       u_eh = v.x; u_ev = v.y; u_eb = v.z; u_cb = v.w;
     }
-    const int jc = wlane[u], jp = wlane[u - 1];
-    const int j = R.i + kDlo + s0 + u - 2 * lane;
-    // column quantities (algn.c:2321-2328 / 2451-2457)
-    const int sj_ext = (int)(sm.tab[jc] >> 16);  // prepend[jc] = cost[gap][jc]
-    const int sj_open = (!(jp & 16) && (jc & 16)) ? 0 : go;
-    const int hext = (j == 1) ? sj_ext : (((jp & 16) && !(jc & 16)) ? sj_open + sj_ext : sj_ext);
+    const int4 D = clane[u];  // this lane's column at this step
+    const int jc = D.w, sj_open = D.z;
     // FILL_EXTEND_HORIZONTAL
-    const int e1 = S.eh_l + hext, e2 = S.cb_l + sj_open + sj_ext;
+    const int e1 = S.eh_l + D.x, e2 = S.cb_l + D.y;
     int eh = min(e1, e2);
     // FILL_EXTEND_VERTICAL
-    const int v1 = u_ev + R.si_vext, v2 = u_cb + R.si_open + R.si_ext;
+    const int v1 = u_ev + R.si_vext, v2 = u_cb + v_open;
     int ev = min(v1, v2);
-    // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]
-    const bool both = (R.ic & 16) && (jc & 16);
+    // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]; _NOBT's open cost is 2 * go when
+    // both characters carry the gap bit (its no-open case needs sj[j] without it)
+    const bool both = R.icg && (jc & 16);
     const int dg = both ? 0 : kHigh;
-    const int od = BT ? dg : (both ? ((!(R.ip & 16) && !(jc & 16)) ? 0 : 2 * go) : kHigh);
+    const int od = BT ? dg : (both ? 2 * go : kHigh);
     const int b1 = S.eb_d + dg, b2 = S.cb_d + od;
     int eb = min(b1, b2);
     // FILL_CLOSE_BLOCK_DIAGONAL
-    const int cdiag = (int)(R.srow[jc & 15] & 0xffffu);
+    const int cdiag = (int)R.srow[jc & 15];
     const int extra = max(sj_open, R.si_open);
     const int fa = S.cb_d + cdiag;
-    const int fv = S.ev_d + cdiag + ((R.ic & 16) ? sj_open : 0);
+    const int fv = S.ev_d + cdiag + (sj_open & R.icg);
     const int fh = S.eh_d + cdiag + ((jc & 16) ? R.si_open : 0);
     const int fd = S.eb_d + cdiag + extra;
     int cb = min(min(fa, fv), min(fh, fd));
@@ -230,9 +245,9 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
       code = todo | (v1 < v2 ? 0u : 4u) | (e1 < e2 ? 0u : 8u) | (b1 < b2 ? 0u : 16u) |
              (achoice << 5);
     }
-    if (R.i == 0) {  // initialize_matrices_affine row 0
-      if (j == 0) { eh = go; ev = go; eb = 0; cb = 0; f = 0; }
-      else { eh = S.eh_l + sj_ext; cb = eh; eb = kHigh; ev = kHigh; f = eh; }
+    if (ENDS && R.i == 0) {  // initialize_matrices_affine row 0 (j = d there)
+      if (kDlo + s0 + u - 2 * lane == 0) { eh = go; ev = go; eb = 0; cb = 0; f = 0; }
+      else { eh = S.eh_l + (D.y - sj_open); cb = eh; eb = kHigh; ev = kHigh; f = eh; }
     } else if (u == R.uL) {  // vertical boundary cell left of the band
       eh = kHigh; cb = kHigh; eb = kHigh; ev = v1; f = ev;
       code = kCodeLeft;
@@ -240,7 +255,7 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
       eh = kHigh; ev = kHigh; eb = kHigh; cb = kHigh;
       code = kCodeRight;
     }
-    if (u == R.uF) S.result = f;
+    if (ENDS && u == R.uF) S.result = f;
     if (BT) {
       S.word = (S.word << 8) | code;
       if ((u & 3) == 3) dmb[(u >> 2) * 32] = S.word;
@@ -260,10 +275,10 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
   const uint8_t *sj = A.seq + P.sj_off;
   const int leni = P.leni, lenj = P.lenj, e0 = P.e0, wd = P.wd, go = A.go;
   const int Spad = P.sblocks * 4;
-  uint8_t *win = sm.win[warp];
+  int4 *win = sm.col[warp];
   int4 *rin = sm.ring_in[warp], *rout = sm.ring_out[warp];
   // this lane's column j at block step u is window index 32 + u - lane
-  const uint8_t *wl = win + 32 - lane;
+  const int4 *wl = win + 32 - lane;
   const int4 kHigh4 = make_int4(kHigh, kHigh, kHigh, kHigh);
   AffState S;
   S.result = 0;
@@ -279,7 +294,8 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
     R.si_ext = (int)(sm.tab[(R.ic << 5) | 16] & 0xffffu);
     R.si_open = (!(R.ip & 16) && (R.ic & 16)) ? 0 : go;
     R.si_vext = (R.i > 1 && (R.ip & 16) && !(R.ic & 16)) ? R.si_open + R.si_ext : R.si_ext;
-    R.srow = sm.tab + ((R.ic & 15) << 5);
+    R.srow = sm.cost + ((R.ic & 15) << 5);
+    R.icg = (R.ic & 16) ? -1 : 0;
     const int d_lb = (-R.i > kDlo) ? -R.i : kDlo;
     const bool has_rb = e0 <= lenj - R.i;
     const int sL = d_lb - kDlo + 2 * lane;
@@ -301,9 +317,13 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
       {
         const int x = s0 + lane + 1;
         rin[lane] = (strip > 0 && x < wd) ? bnd[x] : kHigh4;
+        // columns jb and jb + 32, each with its predecessor
         const int jb = r0 + kDlo + s0 - 32 + lane;
-        win[lane] = (jb >= 0 && jb <= lenj) ? sj[jb] : 0;
-        win[lane + 32] = (jb + 32 >= 0 && jb + 32 <= lenj) ? sj[jb + 32] : 0;
+        auto chr = [&](int j) { return (j >= 0 && j <= lenj) ? (int)sj[j] : 0; };
+        const int c0 = chr(jb), c1 = chr(jb + 32);
+        // window index 0 is read only as the predecessor of index 1
+        win[lane] = aff_column(sm.tab, c0, chr(jb - 1), jb, go);
+        win[lane + 32] = aff_column(sm.tab, c1, chr(jb + 31), jb + 32, go);
       }
       __syncwarp();
       uint32_t *dmb = BT ? dm + ((int64_t)strip * P.sblocks + (s0 >> 2)) * 32 + lane : nullptr;
@@ -313,8 +333,12 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
         R.uL = sL - hs;
         R.uR = sR - hs;
         R.uF = sF - hs;
-        aff_half<BT>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
-                     BT ? dmb + 4 * 32 * h : nullptr, lane);
+        if (strip == 0 || strip == P.nstrips - 1)
+          aff_half<BT, true>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
+                             BT ? dmb + 4 * 32 * h : nullptr, lane);
+        else
+          aff_half<BT, false>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
+                              BT ? dmb + 4 * 32 * h : nullptr, lane);
       }
       __syncwarp();
       {
@@ -329,9 +353,12 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
 }
 
 template <bool BT>
-__global__ void __launch_bounds__(256) k_aff_dp(AffDpArgs A) {
+__global__ void __launch_bounds__(256, 3) k_aff_dp(AffDpArgs A) {
   __shared__ AffSmem sm;
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) sm.tab[t] = A.tables->packed[t];
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) {
+    sm.tab[t] = A.tables->packed[t];
+    sm.cost[t] = (uint16_t)(A.tables->packed[t] & 0xffffu);
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
