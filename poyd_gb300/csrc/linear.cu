@@ -706,6 +706,89 @@ void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
 }
 
 // ---------------------------------------------------------------------------
+// Device-side ordering: longest first by log2 buckets, disjoint direction
+// matrices (their placement does not follow the order: each pair's DP
+// writes only its own region).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int order_bucket(const LinPlan &P) {
+  const unsigned long long work = (unsigned long long)P.nstrips * (unsigned)P.sblocks + 1;
+  const int lz = __clzll((long long)work);
+  const int lg = 63 - lz;                                     // floor(log2(work))
+  const int frac = (int)((work << lz) >> 58) & 31;            // next 5 bits
+  const int b = min(lg * 32 + frac, 1023);
+  return 1023 - b;                                            // most work first
+}
+
+__global__ void __launch_bounds__(128, 16) k_order_count(int n, const LinPlan *plans,
+                                                        const int64_t *dm_words, int64_t *dm_off,
+                                                        LinOrderScratch *os) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool ok = id < n;
+  int wd = 0;
+  unsigned long long w = 0;
+  if (ok) {
+    const LinPlan P = plans[id];
+    atomicAdd(&os->hist[order_bucket(P)], 1);
+    wd = P.wd;
+    w = (unsigned long long)dm_words[id];
+  }
+  // warp-aggregated region allocation and widest band
+  unsigned long long incl = w;
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += x;
+  }
+  unsigned long long base = 0;
+  if (lane == 31) base = atomicAdd(&os->total, incl);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  if (ok) dm_off[id] = (int64_t)(base + incl - w);
+  for (int d = 16; d > 0; d >>= 1) wd = max(wd, __shfl_xor_sync(0xffffffffu, wd, d));
+  if (lane == 0) atomicMax(&os->maxwd, wd);
+}
+
+__global__ void __launch_bounds__(1024) k_order_scan(LinOrderScratch *os) {
+  __shared__ int part[32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int v = os->hist[t];
+  int incl = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int x = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += x;
+  }
+  if (lane == 31) part[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int p = part[lane];
+    for (int d = 1; d < 32; d <<= 1) {
+      const int x = __shfl_up_sync(0xffffffffu, p, d);
+      if (lane >= d) p += x;
+    }
+    part[lane] = p;  // inclusive over warps
+  }
+  __syncthreads();
+  os->base[t] = (warp ? part[warp - 1] : 0) + incl - v;
+  os->hist[t] = 0;  // now the scatter cursor
+}
+
+__global__ void __launch_bounds__(128, 16) k_order_scatter(int n, const LinPlan *plans,
+                                                          LinOrderScratch *os, int32_t *order) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n) return;
+  const int b = order_bucket(plans[id]);
+  order[os->base[b] + atomicAdd(&os->hist[b], 1)] = id;
+}
+
+void launch_lin_order(int n, const LinPlan *plans, const int64_t *dm_words, int64_t *dm_off,
+                      LinOrderScratch *os, int32_t *order, cudaStream_t st) {
+  const int threads = 128;
+  const unsigned blocks = (unsigned)(((int64_t)n + threads - 1) / threads);
+  k_order_count<<<blocks, threads, 0, st>>>(n, plans, dm_words, dm_off, os);
+  k_order_scan<<<1, 1024, 0, st>>>(os);
+  k_order_scatter<<<blocks, threads, 0, st>>>(n, plans, os, order);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st) {

@@ -74,6 +74,19 @@ struct LinDpArgs {
   DpK k;  // multiplier constants (1, -1, 4, -65536)
 };
 
+// Device-side pair order and direction-matrix offsets (one launch wave):
+// pairs are bucketed by log2 of their lane-steps (32 buckets per octave,
+// longest first) and given disjoint direction-matrix regions.
+struct LinOrderScratch {
+  int hist[1024];           // pairs per bucket, then the scatter cursors
+  int base[1024];           // first order position of each bucket
+  unsigned long long total; // direction-matrix words of the batch
+  int maxwd;                // widest band
+  int pad;
+};
+void launch_lin_order(int n, const LinPlan *plans, const int64_t *dm_words, int64_t *dm_off,
+                      LinOrderScratch *os, int32_t *order, cudaStream_t st);
+
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
 int lin_dp_blocks(int mode);
 void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st);

@@ -168,9 +168,13 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   LinPlan *plans = (LinPlan *)ws_buffer(w, WS_PLANS, sizeof(LinPlan) * (size_t)n);
   int64_t *dmw = (int64_t *)ws_buffer(w, WS_DMWORDS, sizeof(int64_t) * 2 * (size_t)n);
   int32_t *wdb = (int32_t *)ws_buffer(w, WS_WD, sizeof(int32_t) * 2 * (size_t)n + 16);
-  int32_t *err = (int32_t *)ws_buffer(w, WS_ERR, 64);
-  if (!plans || !dmw || !wdb || !err) return fail(POYD_ENOMEM, "plan allocation failed");
-  CK(cudaMemsetAsync(err, 0, 4, st));
+  LinOrderScratch *os = (LinOrderScratch *)ws_buffer(w, WS_ORDSCR, sizeof(LinOrderScratch));
+  int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
+  int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
+  if (!plans || !dmw || !wdb || !os || !dord || !counter)
+    return fail(POYD_ENOMEM, "plan allocation failed");
+  int32_t *err = &os->pad;  // the plan's error bits travel with the order totals
+  CK(cudaMemsetAsync(os, 0, sizeof(LinOrderScratch), st));
   LinPlanArgs PA;
   PA.n = n; PA.seq = seq; PA.a_off = a_off; PA.a_len = a_len; PA.b_off = b_off; PA.b_len = b_len;
   PA.policy = policy; PA.deltaw = deltaw; PA.gap = cm->gap; PA.maxc = maxc;
@@ -183,45 +187,69 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   { ProfScope ps("lin_plan", st); launch_lin_plan(PA, st); }
   CK(cudaGetLastError());
 
-  // Host: DM offsets, scratch size, and a longest-first pair order.
-  std::vector<int64_t> hw((size_t)n);
-  std::vector<int32_t> hwd((size_t)n + 1);
-  CK(cudaMemcpyAsync(hw.data(), dmw, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(hwd.data(), wdb, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(hwd.data() + n, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  // Pair order (longest first by log2 buckets) and direction-matrix
+  // offsets on the device; one small read-back brings the plan's error bits,
+  // the widest band and the direction-matrix size.
+  int64_t *doff = dmw + n;
+  { ProfScope ps("lin_order", st); launch_lin_order(n, plans, dmw, doff, os, dord, st); }
+  CK(cudaGetLastError());
+  struct {
+    unsigned long long total;
+    int maxwd, err;
+  } tl;
+  static_assert(sizeof(tl) == 16, "order read-back");
+  CK(cudaMemcpyAsync(&tl, &os->total, sizeof tl, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  if (hwd[n] & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
-  if (hwd[n] & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
-  if (hwd[n] & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
-  int maxwd = 1;
-  for (int32_t i = 0; i < n; ++i) maxwd = std::max(maxwd, hwd[i]);
-  // longest first: dm_words ~ strips x band steps is the band area
-  std::vector<int32_t> order;
-  longest_first(hw, order);
-  // Waves: consecutive runs of that order whose direction matrices fit the
-  // device-memory budget, one persistent launch each (one wave when the
-  // whole batch fits, the usual case).  The single-pair protocol (out ==
-  // nullptr) keeps its one matrix for the later backtrack.
+  if (tl.err & 1) return fail(POYD_EINVAL, "sequences must have length >= 1 (the leading gap)");
+  if (tl.err & 2) return fail(POYD_ERANGE, "alignment costs could exceed the 2^24 range of the kernels");
+  if (tl.err & 4) return fail(POYD_EINVAL, "sequence codes must be below 32 (5-bit element masks)");
+  const int maxwd = std::max(1, tl.maxwd);
+  const int64_t need = want_align ? (int64_t)tl.total : 0;
+  // Waves: consecutive runs of a longest-first order whose direction
+  // matrices fit the device-memory budget, one persistent launch each; one
+  // wave, with the device order, when the whole batch fits (the usual
+  // case).  The single-pair protocol (out == nullptr) keeps its one matrix
+  // for the later backtrack.
   int64_t budget = INT64_MAX;
   if (want_align && out) {
-    size_t freeb = 0, totb = 0;
-    cudaMemGetInfo(&freeb, &totb);
-    budget = (int64_t)((double)(freeb + w->size[WS_DM]) * 0.8);
-    if (const char *e = std::getenv("POYD_DM_BUDGET_BYTES")) budget = std::atoll(e);
-    budget = std::max<int64_t>(budget / 4, 1);  // in 32-bit words
-  }
-  std::vector<int32_t> wave_at{0};
-  int64_t wave_words = 0, max_words = 1;
-  for (int32_t p = 0; p < n; ++p) {
-    const int64_t x = want_align ? hw[order[p]] : 0;
-    if (p > wave_at.back() && wave_words + x > budget) {
-      wave_at.push_back(p);
-      wave_words = 0;
+    if (const char *e = std::getenv("POYD_DM_BUDGET_BYTES")) {
+      budget = std::max<int64_t>(std::atoll(e) / 4, 1);
+    } else if ((size_t)need * 4 > w->size[WS_DM]) {
+      size_t freeb = 0, totb = 0;
+      cudaMemGetInfo(&freeb, &totb);
+      budget = std::max<int64_t>((int64_t)((double)(freeb + w->size[WS_DM]) * 0.8) / 4, 1);
     }
-    wave_words += x;
-    max_words = std::max(max_words, wave_words);
   }
-  wave_at.push_back(n);
+  const bool host_waves = need > budget;
+  std::vector<int32_t> order;
+  std::vector<int64_t> hw;
+  std::vector<int32_t> wave_at{0, n};
+  int64_t max_words = std::max<int64_t>(need, 1);
+  if (host_waves) {
+    // too large for one launch: waves of a longest-first order built here
+    hw.resize((size_t)n);
+    CK(cudaMemcpyAsync(hw.data(), dmw, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    longest_first(hw, order);
+    wave_at.assign(1, 0);
+    int64_t wave_words = 0;
+    max_words = 1;
+    for (int32_t p = 0; p < n; ++p) {
+      const int64_t x = hw[order[p]];
+      if (p > wave_at.back() && wave_words + x > budget) {
+        wave_at.push_back(p);
+        wave_words = 0;
+      }
+      wave_words += x;
+      max_words = std::max(max_words, wave_words);
+    }
+    wave_at.push_back(n);
+    CK(cudaMemcpyAsync(dord, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+  } else if (ls) {
+    order.resize((size_t)n);
+    CK(cudaMemcpyAsync(order.data(), dord, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
   if (ls) {  // output slots in DP order
     int64_t o = 0;
     for (int32_t p = 0; p < n; ++p) {
@@ -235,11 +263,6 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     ls->order = order;
     ls->waves = (int)wave_at.size() - 1;
   }
-  int64_t *doff = dmw + n;
-  int32_t *dord = (int32_t *)ws_buffer(w, WS_ORDER, sizeof(int32_t) * (size_t)n);
-  int *counter = (int *)ws_buffer(w, WS_COUNTER, 64);
-  if (!dord || !counter) return fail(POYD_ENOMEM, "order allocation failed");
-  CK(cudaMemcpyAsync(dord, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
   uint32_t *dm = nullptr;
   if (want_align) {
     dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)max_words);
@@ -258,15 +281,17 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * (((size_t)n + kLanes - 1) / kLanes));
     if (!batch_done) return fail(POYD_ENOMEM, "batch counter allocation failed");
   }
-  std::vector<int64_t> off((size_t)n, 0);
+  std::vector<int64_t> off(host_waves ? (size_t)n : 0, 0);
   for (size_t v = 0; v + 1 < wave_at.size(); ++v) {
     const int32_t p0 = wave_at[v], p1 = wave_at[v + 1], m = p1 - p0;
-    int64_t total = 0;
-    for (int32_t p = p0; p < p1; ++p) {
-      off[order[p]] = total;
-      if (want_align) total += hw[order[p]];
+    if (host_waves) {  // this wave's matrices from the start of the buffer
+      int64_t total = 0;
+      for (int32_t p = p0; p < p1; ++p) {
+        off[order[p]] = total;
+        total += hw[order[p]];
+      }
+      CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
     }
-    CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(counter, 0, 4, st));
     if (fuse) CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * (((size_t)m + kLanes - 1) / kLanes), st));
     LinTbArgs TA;
