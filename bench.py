@@ -52,7 +52,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-s", type=float, default=12.0)
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="align", choices=["align", "spr", "learned", "serving"],
+    p.add_argument("--workload", default="align",
+                   choices=["align", "spr", "tbr", "learned", "serving"],
                    help="align (default, the headline line) or one of the other configs")
     p.add_argument("--train-trees", type=int, default=2)
     p.add_argument("--max-passes", type=int, default=8)
@@ -417,7 +418,8 @@ def run_spr(args):
     from poyd_gb300 import align, learned, native, search, simulate
     data = simulate.simulate(args.seed, 200, 1500, n_fitch=2000, n_sank=200)
     be = search.GpuBackend(data, align.CostMatrix.default())
-    t = learned.random_tree(data.n_taxa, args.seed)
+    # a random start, not the generating tree (which the same seed would draw)
+    t = learned.random_tree(data.n_taxa, args.seed + 7)
     search.downpass(t, be)
     S, E = search.spr_candidates(t)
     for _ in range(2):  # warm-up
@@ -461,6 +463,38 @@ def run_spr(args):
                             "sample": "%d of %d candidates" % (k_cpu, n),
                             "bit_exact_on_sample": bool(np.array_equal(out, score[idx]))}
     _emit(line)
+
+
+def run_tbr(args):
+    """TBR pass on the config-2 data (200 taxa x ~1,500 bp + 2,000 Fitch +
+    200 Sankoff): every (clade, re-rooting, join edge) candidate scored in
+    one batch, the re-rootings' medians included."""
+    import torch
+    from poyd_gb300 import align, learned, search, simulate
+    data = simulate.simulate(args.seed, 200, 1500, n_fitch=2000, n_sank=200)
+    be = search.GpuBackend(data, align.CostMatrix.default())
+    # a random start, not the generating tree (which the same seed would draw)
+    t = learned.random_tree(data.n_taxa, args.seed + 7)
+    diag = search.downpass(t, be)
+    search.tbr_candidates(t, be, diag)  # warm-up (buffer growth)
+    be.stats["median_pairs"] = be.stats["distance_pairs"] = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    S, U, E, score, _ = search.tbr_candidates(t, be, diag)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    medians = be.stats["median_pairs"]
+    st = search.tbr_pass(t, be, max_moves=16, diag=diag)
+    _emit({
+        "workload": "TBR pass, 200 taxa x 1500 bp + 2000 Fitch + 200 Sankoff",
+        "metric": "TBR candidate joins scored per second", "value": len(S) / dt,
+        "unit": "joins/s", "candidates": int(len(S)),
+        "rerooted": int((U >= 0).sum()), "clades": int(len(np.unique(S))),
+        "reroot_medians": int(medians), "seconds_scoring": dt,
+        "pass": {"moves_tried": st.moves_tried, "moves_accepted": st.moves_accepted,
+                 "cost_before": st.cost_before, "cost_after": st.cost_after,
+                 "seconds": st.seconds_total},
+    })
 
 
 def run_learned(args):
@@ -556,6 +590,8 @@ def main():
         run_reference(args)
     elif args.workload == "spr":
         run_spr(args)
+    elif args.workload == "tbr":
+        run_tbr(args)
     elif args.workload == "learned":
         run_learned(args)
     elif args.workload == "serving":

@@ -114,6 +114,31 @@ class Tree:
         self.in_tree[p] = False
         return p
 
+    def reroot(self, s: int, u: int):
+        """Re-roots the subtree under s on the edge above u (u inside it,
+        u's parent not s): s keeps its id and becomes the midpoint of that
+        edge, the path from u's parent up to s is reversed and s's old
+        other child hangs from the path's top.  ``Tree_Ops.reroot_fn`` on
+        a clade (ptree.ml:1179-1181)."""
+        path = [u]
+        while self.parent[path[-1]] != s:
+            path.append(int(self.parent[path[-1]]))
+        assert len(path) >= 2, "u must lie below a child of s"
+        top = path[-1]
+        sib = int(self.kids[s][0] if self.kids[s][1] == top else self.kids[s][1])
+        other = []
+        for j in range(1, len(path)):
+            k = self.kids[path[j]]
+            other.append(int(k[0] if k[1] == path[j - 1] else k[1]))
+        self.kids[s] = (path[0], path[1])
+        self.parent[path[0]] = s
+        self.parent[path[1]] = s
+        for j in range(1, len(path)):
+            nxt = path[j + 1] if j + 1 < len(path) else sib
+            self.kids[path[j]] = (other[j - 1], nxt)
+            self.parent[other[j - 1]] = path[j]
+            self.parent[nxt] = path[j]
+
     def nodes(self):
         out, stack = [], [self.root]
         while stack:
@@ -558,6 +583,172 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     return st
 
 
+def tbr_candidates(t: Tree, be, diag: Diagnosis | None = None):
+    """Every TBR candidate of one pass, scored in one batch: (pruned
+    subtree s, re-root node u, join edge e, score, clade cost change).
+    ``tbr_join`` (ptree.ml:1178-1217) breaks the edge above s and runs an
+    SPR round of the clade for each of its re-rootings (``reroot_fn``),
+    joining by the clade's root median.  Here, for every clade together:
+
+    * the medians of the clade seen from inside, looking up towards s
+      (up(w) = median(up(parent), sibling's downpass median)), one batch
+      per depth below s;
+    * the root median of every re-rooting on the edge above w
+      (median(w's downpass median, up(w))), one batch;
+    * the distance of every (re-rooted clade, join edge) pair, one batch.
+
+    The clade cost change is the clade's own cost rooted on the edge above
+    u (the costs of those medians plus the downpass costs below them)
+    minus its cost as rooted now: a re-rooting changes it, a join does not.
+    u = -1 is the clade's own rooting (plain SPR: its sibling edge is
+    excluded).  Medians take their arguments in ``min_child_code`` order.
+    Scratch node ids from 2 * t.n are released on return."""
+    n = t.n
+    diag = downpass(t, be) if diag is None else diag
+    mc = t.min_codes()
+    par = t.parent
+    nodes = np.array(sorted(t.nodes()), np.int64)
+    # downpass cost of every subtree (DO + Fitch)
+    tot = np.zeros(len(par), np.int64)
+    for v in t.nodes()[::-1]:
+        if v >= n:
+            a, b = t.kids[v]
+            tot[v] = tot[a] + tot[b] + diag.do_cost[v] + diag.fitch_cost[v]
+    subs = [int(v) for v in nodes if par[v] >= 0 and par[par[v]] >= 0]
+    nxt = 2 * n
+    cand = []        # (s, u, node holding the clade's root median, clade cost change)
+    fronts = {}      # s -> [(node, id of up(node), min code of up(node), cost of up(node))]
+    for s in subs:
+        cand.append((s, -1, s, 0))
+        if s >= n:
+            k0, k1 = int(t.kids[s][0]), int(t.kids[s][1])
+            fronts[s] = [(k0, k1, int(mc[k1]), int(tot[k1])), (k1, k0, int(mc[k0]), int(tot[k0]))]
+    size = np.zeros(len(par), np.int64)  # nodes per subtree
+    for v in t.nodes()[::-1]:
+        size[v] = 1 if v < n else 1 + size[t.kids[v][0]] + size[t.kids[v][1]]
+    # two medians (up, root) for every clade node below the clade's children
+    be.ensure_nodes(nxt + sum(2 * (int(size[s]) - 3) for s in fronts))
+    roots = []       # (a, b, out, s, u, cost below the root median)
+    while fronts:
+        jobs, meta = [], []
+        for s, front in fronts.items():
+            for u, upid, upmc, upc in front:
+                if u < n:
+                    continue
+                for w in (int(t.kids[u][0]), int(t.kids[u][1])):
+                    x = int(t.kids[u][0] if t.kids[u][1] == w else t.kids[u][1])
+                    jobs.append((upid, x, nxt) if upmc < mc[x] else (x, upid, nxt))
+                    meta.append((s, w, nxt, min(upmc, int(mc[x])), upc + int(tot[x])))
+                    nxt += 1
+        if not jobs:
+            break
+        j = np.array(jobs, np.int64)
+        do, fi = be.medians(j[:, 0], j[:, 1], j[:, 2])
+        fronts = {}
+        for i, (s, w, wid, wmc, below) in enumerate(meta):
+            upc = below + int(do[i]) + int(fi[i])
+            fronts.setdefault(s, []).append((w, wid, wmc, upc))
+            a, b = (w, wid) if mc[w] < wmc else (wid, w)
+            roots.append((a, b, nxt, s, w, int(tot[w]) + upc))
+            nxt += 1
+    if roots:
+        r = np.array([x[:3] for x in roots], np.int64)
+        do, fi = be.medians(r[:, 0], r[:, 1], r[:, 2])
+        for i, (_, _, rid, s, w, below) in enumerate(roots):
+            cand.append((s, w, rid, below + int(do[i]) + int(fi[i]) - int(tot[s])))
+    # join edges: outside the clade, not its parent, not (own rooting) its sibling
+    tin, tout = euler(t)
+    S, U, R, E, D = [], [], [], [], []
+    for s, u, rid, dc in cand:
+        p = par[s]
+        sib = t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1]
+        inside = (tin[nodes] >= tin[s]) & (tin[nodes] < tout[s])
+        keep = ~inside & (nodes != p)
+        if u < 0:
+            keep &= nodes != sib
+        e = nodes[keep]
+        S.append(np.full(len(e), s, np.int64))
+        U.append(np.full(len(e), u, np.int64))
+        R.append(np.full(len(e), rid, np.int64))
+        D.append(np.full(len(e), dc, np.int64))
+        E.append(e)
+    cat = lambda x: np.concatenate(x) if x else np.zeros(0, np.int64)
+    S, U, R, E, D = cat(S), cat(U), cat(R), cat(E), cat(D)
+    score = be.distances(R, E) if len(S) else np.zeros(0, np.int64)
+    be.release_nodes(2 * n)
+    return S, U, E, score, D
+
+
+def tbr_pass(t: Tree, be, max_moves: int = 16, log=None, diag=None):
+    """One TBR pass: every (clade, re-rooting, join edge) candidate scored
+    in one batch (:func:`tbr_candidates`), then the best-scoring move of
+    each clade tried in order of predicted gain, as in :func:`spr_pass`: a
+    move is kept only if the exact re-diagnosed tree cost drops."""
+    t0 = time.perf_counter()
+    st = PassStats()
+    diag = downpass(t, be) if diag is None else diag
+    st.cost_before = diag.total
+    t1 = time.perf_counter()
+    S, U, E, score, dclade = tbr_candidates(t, be, diag)
+    st.candidates = len(S)
+    subs = np.unique(S)
+    cur = np.zeros(len(t.parent), np.int64)
+    if len(subs):
+        p = t.parent[subs]
+        sib = np.where(t.kids[p, 0] == subs, t.kids[p, 1], t.kids[p, 0])
+        cur[subs] = be.distances(subs, sib)
+    st.seconds_scoring = time.perf_counter() - t1
+    if log is not None:
+        log.append((t.copy(), S, U, E, score))
+    gain = cur[S] - score - dclade
+    order = np.lexsort((U, E, S, -gain))  # largest predicted gain first, ties by ids
+    moves, seen = [], set()
+    for i in order:
+        if len(moves) >= max_moves or gain[i] <= 0:
+            break
+        s, e, u = int(S[i]), int(E[i]), int(U[i])
+        if s not in seen:
+            seen.add(s)
+            moves.append((s, e) if u < 0 else (s, e, u))
+    best = diag.total
+    while moves:
+        st.moves_tried += len(moves)
+        detail = {}
+        totals = evaluate_moves(t, be, diag, moves, detail)
+        k = int(np.argmin(totals))
+        if totals[k] >= best:
+            be.release_nodes(2 * t.n)
+            break
+        mv = moves.pop(k)
+        if len(mv) > 2:
+            t.reroot(mv[0], mv[2])
+        w = t.prune(mv[0])
+        t.insert(mv[0], mv[1], w)
+        commit_move(be, diag, detail[k], totals[k])
+        be.release_nodes(2 * t.n)
+        best = int(totals[k])
+        st.moves_accepted += 1
+        moves = [m for m in moves if _valid_tbr_move(t, *m)]
+    if st.moves_accepted:
+        check = downpass(t, be)
+        assert check.total == best, (check.total, best)
+        diag = check
+    st.cost_after = best
+    st.diag = diag
+    st.seconds_total = time.perf_counter() - t0
+    return st
+
+
+def _valid_tbr_move(t: Tree, s: int, e: int, u: int = -1) -> bool:
+    if u < 0:
+        return _valid_move(t, s, e)
+    p = t.parent[s]
+    if p < 0 or t.parent[p] < 0 or not t.in_tree[e]:
+        return False
+    inside = set(t.subtree(s))
+    return e != p and e not in inside and u in inside and u != s and t.parent[u] != s
+
+
 def _valid_move(t: Tree, s: int, e: int) -> bool:
     p = t.parent[s]
     if p < 0 or t.parent[p] < 0 or not t.in_tree[e]:
@@ -574,11 +765,14 @@ def _heights(t: Tree) -> dict:
 
 
 def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarray:
-    """Exact total cost of the tree after each SPR move (s onto the edge above
-    e), computed together: a move changes only the ancestors of the prune
-    point and of the regraft point, so each trial recomputes just those nodes
-    (into scratch node slots), and the dirty nodes of every trial at one
-    height form one batch of medians.
+    """Exact total cost of the tree after each move, computed together.  A
+    move (s, e) is SPR: s onto the edge above e; (s, e, u) is TBR: the
+    subtree under s re-rooted on the edge above u first.  A move changes
+    only the nodes whose children change (in a re-rooted subtree, the path
+    from u's parent up to s) and the ancestors of the prune point and of
+    the regraft point, so each trial recomputes just those nodes (into
+    scratch node slots), and the dirty nodes of every trial at one height
+    form one batch of medians.
 
     With `detail` (a dict), the scratch slots are kept and detail[m] lists
     (node, scratch slot, DO cost, Fitch cost) of trial m's recomputed nodes,
@@ -590,14 +784,21 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
     recs = {}      # level -> list of (trial, a_ref, b_ref, out_tid)
     old = np.zeros(len(moves), np.int64)
     roots = []
-    for m, (s, e) in enumerate(moves):
+    for m, mv in enumerate(moves):
+        s, e = int(mv[0]), int(mv[1])
+        u = int(mv[2]) if len(mv) > 2 else -1
         T = t.copy()
+        changed = []
+        if u >= 0:
+            T.reroot(s, u)
+            changed = [v for v in T.subtree(s)
+                       if v >= T.n and set(T.kids[v].tolist()) != set(t.kids[v].tolist())]
         p = T.parent[s]
         g = T.parent[p]
         w = T.prune(s)
         T.insert(s, e, w)
         dirty = set()
-        for v in (g, w):
+        for v in [g, w] + changed:
             while v >= 0 and v not in dirty:
                 dirty.add(v)
                 v = T.parent[v]

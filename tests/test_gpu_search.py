@@ -71,3 +71,27 @@ def test_final_cost_matches_oracle(sub, indel, go):
     fg = search.final_cost(t, [search.GpuBackend(d, cm) for d in sets])
     fo = search.final_cost(t, [OracleBackend(d, om) for d in sets])
     assert (fg.cost, fg.root_edge, fg.root_cost) == (fo.cost, fo.root_edge, fo.root_cost)
+
+
+@pytest.mark.parametrize("seed,n_fitch,n_sank", [(31, 0, 0), (32, 40, 6)])
+def test_tbr_pass_matches_oracle(seed, n_fitch, n_sank):
+    """A TBR pass (every clade re-rooting scored in one batch, exact
+    evaluation of the best moves) through the CUDA kernels and through the
+    oracle: identical candidates, scores, trees, costs and node medians."""
+    data = simulate.simulate(seed, 18, 250, n_fitch, n_sank)
+    g = search.GpuBackend(data, align.CostMatrix.default())
+    o = OracleBackend(data, O.cm_dna(1, 2, -1))
+    tg, dg = search.wagner(data.n_taxa, g)
+    to, do = search.wagner(data.n_taxa, o)
+    assert tg.newick() == to.newick()
+    cg = search.tbr_candidates(tg, g)
+    co = search.tbr_candidates(to, o)
+    for x, y in zip(cg, co):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
+    sg = search.tbr_pass(tg, g, max_moves=6, diag=dg)
+    so = search.tbr_pass(to, o, max_moves=6, diag=do)
+    assert tg.newick() == to.newick()
+    assert (sg.cost_before, sg.cost_after, sg.moves_accepted) == \
+        (so.cost_before, so.cost_after, so.moves_accepted)
+    assert sg.cost_after <= sg.cost_before
+    _compare_nodes(tg, g, o)
