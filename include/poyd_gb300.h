@@ -149,6 +149,48 @@ int poyd_pack_alignments(int32_t n, const uint8_t *out, const int64_t *out_off,
                          const int32_t *out_len, uint8_t *packed,
                          const int64_t *packed_off, void *stream);
 
+/* Column operations on aligned pairs (a_i and b_i both len[i] bytes, the
+ * output of an alignment), the DP-free externals of sequence.ml:453-758:
+ *   median_2_with_gaps: algn_CAML_median_2_with_gaps (algn.c:4011-4024)
+ *   median_2_no_gaps:   algn_CAML_median_2_no_gaps (algn.c:4031-4046)
+ *   ancestor_2:         algn_CAML_ancestor_2 (algn.c:4126-4147, with the
+ *                       affine block correction algn.c:4080-4119)
+ *   worst_2, verify_2:  algn_CAML_worst_2 / algn_CAML_verify_2, the cost of
+ *                       the alignment under the worst / cost table with gap
+ *                       openings per block (algn.c:3316-3370)
+ * Batched forms: device pointers, asynchronous on `stream`; pair i's result
+ * is right-aligned in out + out_off[i] (capacity len[i] + 1), its length in
+ * out_len[i]; worst/verify write value[i].  Single-pair forms (poyd_algn_*):
+ * host pointers, synchronous; the result is written from out[0]. */
+int poyd_median_2_with_gaps_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                                  const int64_t *a_off, const int64_t *b_off,
+                                  const int32_t *len, uint8_t *out, const int64_t *out_off,
+                                  int32_t *out_len, void *stream);
+int poyd_median_2_no_gaps_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                                const int64_t *a_off, const int64_t *b_off,
+                                const int32_t *len, uint8_t *out, const int64_t *out_off,
+                                int32_t *out_len, void *stream);
+int poyd_ancestor_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                          const int64_t *a_off, const int64_t *b_off, const int32_t *len,
+                          uint8_t *out, const int64_t *out_off, int32_t *out_len,
+                          void *stream);
+int poyd_worst_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                       const int64_t *a_off, const int64_t *b_off, const int32_t *len,
+                       int32_t *value, void *stream);
+int poyd_verify_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                        const int64_t *a_off, const int64_t *b_off, const int32_t *len,
+                        int32_t *value, void *stream);
+int poyd_algn_median_2_with_gaps(const uint8_t *a, const uint8_t *b, int32_t len,
+                                 const poyd_cm *cm, uint8_t *out, int32_t *out_len);
+int poyd_algn_median_2_no_gaps(const uint8_t *a, const uint8_t *b, int32_t len,
+                               const poyd_cm *cm, uint8_t *out, int32_t *out_len);
+int poyd_algn_ancestor_2(const uint8_t *a, const uint8_t *b, int32_t len,
+                         const poyd_cm *cm, uint8_t *out, int32_t *out_len);
+int poyd_algn_worst_2(const uint8_t *a, const uint8_t *b, int32_t len,
+                      const poyd_cm *cm, int32_t *value);
+int poyd_algn_verify_2(const uint8_t *a, const uint8_t *b, int32_t len,
+                       const poyd_cm *cm, int32_t *value);
+
 /* Host-buffer form of poyd_align_2_batch for a caller whose sequences live
  * in host memory (an OCaml stub over seq blocks, which the reference aligns
  * one pair per call, sequence.ml:849-869).  seq, a_off, a_len, b_off, b_len
@@ -211,6 +253,12 @@ int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8_t *s2,
                            int32_t l2, uint8_t *s1p, uint8_t *s2p,
                            int32_t cap, int32_t *len, poyd_matrix *mat,
                            const poyd_cm *cm, int32_t swaped);
+/* algn_CAML_align_2d(s1, s2, cm, mat, s1p, s2p, deltawh, swaped)
+ * (algn.c:3987-3996): poyd_algn_simple_2 then poyd_algn_backtrack_2d. */
+int poyd_algn_align_2d(const uint8_t *s1, int32_t l1, const uint8_t *s2,
+                       int32_t l2, const poyd_cm *cm, poyd_matrix *mat,
+                       uint8_t *s1p, uint8_t *s2p, int32_t cap, int32_t *len,
+                       int32_t deltawh, int32_t swaped, int32_t *cost);
 /* algn_CAML_cost_affine_3(si, sj, cm, mat). */
 int poyd_algn_cost_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
                             int32_t lj, const poyd_cm *cm, int32_t *cost);

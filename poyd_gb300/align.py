@@ -345,3 +345,51 @@ def align_2_pair(s1, s2, cm: CostMatrix):
     b = PairBatch.from_host([np.asarray(s1, np.uint8)], [np.asarray(s2, np.uint8)])
     r = align_2(b, cm).to_host()[0]
     return r["a"], r["b"], r["cost"]
+
+
+# ---- column operations on aligned pairs (no DP) ------------------------------
+
+_COLUMN_SEQ = {"median_2_with_gaps": "poyd_median_2_with_gaps_batch",
+               "median_2_no_gaps": "poyd_median_2_no_gaps_batch",
+               "ancestor_2": "poyd_ancestor_2_batch"}
+_COLUMN_VAL = {"worst_2": "poyd_worst_2_batch", "verify_2": "poyd_verify_2_batch"}
+
+
+def columns(op: str, a_list, b_list, cm: CostMatrix, device="cuda", stream=None):
+    """Batched column operation `op` on aligned pairs (a_i, b_i of equal
+    length): ``median_2_with_gaps``, ``median_2_no_gaps``, ``ancestor_2``
+    (lists of uint8 arrays) or ``worst_2``, ``verify_2`` (int costs)."""
+    assert all(len(x) == len(y) for x, y in zip(a_list, b_list)), "pairs must be aligned"
+    b = PairBatch.from_host(a_list, b_list, device)
+    ln = b.a_len
+    if op in _COLUMN_VAL:
+        val = torch.empty(b.n, dtype=torch.int32, device=device)
+        check(getattr(lib(), _COLUMN_VAL[op])(
+            cm.ref, b.n, b.seq.data_ptr(), b.a_off.data_ptr(), b.b_off.data_ptr(), ln.data_ptr(),
+            val.data_ptr(), _stream_handle(stream)))
+        return [int(x) for x in val.cpu().numpy()]
+    cap = ln.to(torch.int64) + 1
+    off = torch.cumsum(cap, 0) - cap
+    out = torch.empty(max(int(cap.sum()), 16), dtype=torch.uint8, device=device)
+    out_len = torch.empty(b.n, dtype=torch.int32, device=device)
+    check(getattr(lib(), _COLUMN_SEQ[op])(
+        cm.ref, b.n, b.seq.data_ptr(), b.a_off.data_ptr(), b.b_off.data_ptr(), ln.data_ptr(),
+        out.data_ptr(), off.data_ptr(), out_len.data_ptr(), _stream_handle(stream)))
+    o, n, e = out.cpu().numpy(), out_len.cpu().numpy(), (off + cap).cpu().numpy()
+    return [o[int(e[i]) - int(n[i]):int(e[i])].copy() for i in range(b.n)]
+
+
+def column_pair(op: str, a, b, cm: CostMatrix):
+    """Single-pair form with the reference's signature (host buffers)."""
+    a = np.ascontiguousarray(a, np.uint8)
+    b = np.ascontiguousarray(b, np.uint8)
+    assert len(a) == len(b), "pairs must be aligned"
+    p = lambda x: x.ctypes.data_as(C.c_void_p)
+    if op in _COLUMN_VAL:
+        v = C.c_int32()
+        check(getattr(lib(), "poyd_algn_" + op)(p(a), p(b), len(a), cm.ref, C.byref(v)))
+        return int(v.value)
+    out = np.zeros(len(a) + 1, np.uint8)
+    n = C.c_int32()
+    check(getattr(lib(), "poyd_algn_" + op)(p(a), p(b), len(a), cm.ref, p(out), C.byref(n)))
+    return out[:n.value].copy()

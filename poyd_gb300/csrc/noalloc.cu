@@ -141,6 +141,7 @@ extern "C" int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uin
                                ((uint32_t)(cm->cost[(16 << 5) | b] & 0xffff) << 16);
   std::memcpy(h.median, cm->median, sizeof(h.median));
   std::memcpy(h.cost, cm->cost, sizeof(h.cost));
+  std::memcpy(h.worst, cm->worst, sizeof(h.worst));
   NA_CK(cudaMemcpyAsync(tabs, &h, sizeof(DevTables), cudaMemcpyHostToDevice, st));
   NA_CK(cudaMemsetAsync(base, 0, kNaHeader, st));
 

@@ -77,6 +77,7 @@ struct DevTables {
   uint32_t packed[1024];
   uint8_t median[1024];
   int32_t cost[1024];
+  int32_t worst[1024];
 };
 
 struct Workspace;

@@ -145,6 +145,7 @@ int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *str
                                  ((uint32_t)(cm->cost[(16 << 5) | b] & 0xffff) << 16);
     std::memcpy(h.median, cm->median, sizeof(h.median));
     std::memcpy(h.cost, cm->cost, sizeof(h.cost));
+    std::memcpy(h.worst, cm->worst, sizeof(h.worst));
     CK(cudaMemcpyAsync(d, &h, sizeof(DevTables), cudaMemcpyHostToDevice, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     w->last_cm = *cm;
@@ -513,6 +514,15 @@ extern "C" int poyd_algn_backtrack_2d(const uint8_t *s1, int32_t l1, const uint8
   CK(cudaMemcpy(s2p + cap - hl[0], out + 2 * slot - hl[0], (size_t)hl[0], cudaMemcpyDeviceToHost));
   *len = hl[0];
   return POYD_OK;
+}
+
+extern "C" int poyd_algn_align_2d(const uint8_t *s1, int32_t l1, const uint8_t *s2, int32_t l2,
+                                  const poyd_cm *cm, poyd_matrix *mat, uint8_t *s1p,
+                                  uint8_t *s2p, int32_t cap, int32_t *len, int32_t deltawh,
+                                  int32_t swaped, int32_t *cost) {
+  const int rc = poyd_algn_simple_2(s1, l1, s2, l2, cm, mat, deltawh, cost);
+  if (rc) return rc;
+  return poyd_algn_backtrack_2d(s1, l1, s2, l2, s1p, s2p, cap, len, mat, cm, swaped);
 }
 
 static int affine_one(const uint8_t *si, int32_t li, const uint8_t *sj, int32_t lj,

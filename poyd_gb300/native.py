@@ -58,6 +58,19 @@ SIGNATURES = [
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("poyd_align_2_host", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                     C.c_int64, _vp, _vp, _i32]),
+    ("poyd_algn_align_2d", C.c_int, [_vp, _i32, _vp, _i32, _cmp, _vp, _vp, _vp, _i32, _vp, _i32,
+                                     _i32, _vp]),
+    ("poyd_median_2_with_gaps_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                                _vp]),
+    ("poyd_median_2_no_gaps_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("poyd_ancestor_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("poyd_worst_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("poyd_verify_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("poyd_algn_median_2_with_gaps", C.c_int, [_vp, _vp, _i32, _cmp, _vp, _vp]),
+    ("poyd_algn_median_2_no_gaps", C.c_int, [_vp, _vp, _i32, _cmp, _vp, _vp]),
+    ("poyd_algn_ancestor_2", C.c_int, [_vp, _vp, _i32, _cmp, _vp, _vp]),
+    ("poyd_algn_worst_2", C.c_int, [_vp, _vp, _i32, _cmp, _vp]),
+    ("poyd_algn_verify_2", C.c_int, [_vp, _vp, _i32, _cmp, _vp]),
     ("poyd_closest_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _i32, _vp]),
     ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -54,6 +54,15 @@ def test_simple_2_then_backtrack_both_priorities():
                                             o2.ctypes.data_as(O.u8p))
                 assert n.value == k
                 assert np.array_equal(r1[cap - k:], o1[:k]) and np.array_equal(r2[cap - k:], o2[:k])
+                # algn_CAML_align_2d: the two calls in one
+                q1 = np.zeros(cap, np.uint8)
+                q2 = np.zeros(cap, np.uint8)
+                m, c2 = C.c_int32(), C.c_int32()
+                assert L.poyd_algn_align_2d(P(s1), len(s1), P(s2), len(s2), cm.ref,
+                                            C.c_void_p(mat), P(q1), P(q2), cap, C.byref(m), dw,
+                                            swaped, C.byref(c2)) == 0, L.poyd_last_error()
+                assert c2.value == c_ref and m.value == k
+                assert np.array_equal(q1, r1) and np.array_equal(q2, r2)
     finally:
         L.poyd_matrix_free(C.c_void_p(mat))
 
