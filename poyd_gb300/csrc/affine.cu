@@ -116,7 +116,7 @@ __global__ void k_aff_plan(AffPlanArgs A) {
   P.swap = swap;
   P.nstrips = (leni + 1 + 31) / 32;
   const int S = P.wd + 62;
-  const int Spad = (S + 31) / 32 * 32;
+  const int Spad = (S + 15) / 16 * 16;  // whole 16-step half blocks
   P.sblocks = Spad / 4;
   P.empty = 0;
   if (A.dos_empty) {
@@ -330,6 +330,8 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int hs = s0 + 16 * h;
+        if (hs >= Spad) break;  // a strip may end on a half block; its lane 31
+                                // positions past the band are not copied out
         R.uL = sL - hs;
         R.uR = sR - hs;
         R.uF = sF - hs;
