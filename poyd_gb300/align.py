@@ -259,12 +259,14 @@ class PackedAlignments:
 
 
 def align_2(batch: PairBatch, cm: CostMatrix, dos_empty: bool = False,
-            band_cells: bool = False, stream=None) -> AlignResult:
+            band_cells: bool = False, stream=None, layout=None) -> AlignResult:
     """Batched ``DOS.median`` pieces (seqCS.ml:747-776): ``align_2``,
     ``ancestor_2`` and ``median_2_with_gaps`` for the linear model, or
-    ``align_affine_3`` for an affine matrix."""
+    ``align_affine_3`` for an affine matrix.  `layout` may bring the
+    output layout (out_off, total, cap) the caller computed from host
+    copies of the lengths, saving the device read-back of the total."""
     dev = batch.seq.device
-    out_off, total, cap = batch.out_layout()
+    out_off, total, cap = batch.out_layout() if layout is None else layout
     out = torch.empty(max(total, 16), dtype=torch.uint8, device=dev)
     cost = torch.empty(batch.n, dtype=torch.int32, device=dev)
     out_len = torch.empty(2 * batch.n, dtype=torch.int32, device=dev)

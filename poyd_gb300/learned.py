@@ -178,21 +178,29 @@ def learned_scorer(prop: Proposal, be, frac: float = 0.03, min_k: int = 64, stat
 
 
 def run_search(t: search.Tree, be, scorer=None, max_passes: int = 30, max_moves: int = 16,
-               fallback: bool = True):
+               fallback: bool = True, times=None):
     """SPR passes until a pass accepts nothing (with an exhaustive fallback
-    pass when `scorer` is the learned proposal).  Returns (history, seconds)."""
+    pass when `scorer` is the learned proposal).  Returns (history, seconds);
+    `times` (a list) receives the elapsed seconds after every pass."""
     hist = []
     t0 = time.perf_counter()
     diag = None
+
+    def mark(st):
+        hist.append(st.cost_after)
+        if times is not None:
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+
     for _ in range(max_passes):
         st = search.spr_pass(t, be, max_moves=max_moves, scorer=scorer, diag=diag)
         diag = st.diag
-        hist.append(st.cost_after)
+        mark(st)
         if st.moves_accepted == 0:
             if scorer is not None and fallback:
                 st = search.spr_pass(t, be, max_moves=max_moves, diag=diag)
                 diag = st.diag
-                hist.append(st.cost_after)
+                mark(st)
                 if st.moves_accepted == 0:
                     break
             else:

@@ -252,6 +252,25 @@ class GpuBackend:
         return align.PairBatch(self.pool, t(self.off[a], np.int64), t(self.len[a], np.int32),
                                t(self.off[b], np.int64), t(self.len[b], np.int32))
 
+    def _batch_indexed(self, a, b, out):
+        """The pair batch of nodes (a_i, b_i), the node ids a, b and out on
+        the device and the output layout, from two uploads of host arrays
+        (no device read-back)."""
+        a = np.asarray(a, np.int64)
+        b = np.asarray(b, np.int64)
+        n = len(a)
+        la, lb = self.len[a].astype(np.int64), self.len[b].astype(np.int64)
+        cap = (la + lb + 2 + 3) // 4 * 4
+        off = np.cumsum(4 * cap) - 4 * cap
+        h64 = np.concatenate([self.off[a], self.off[b], off, cap, np.asarray(out, np.int64)])
+        h32 = np.concatenate([la, lb, a, b]).astype(np.int32)
+        d64 = torch.from_numpy(h64).to(self.dev)
+        d32 = torch.from_numpy(h32).to(self.dev)
+        batch = align.PairBatch(self.pool, d64[:n], d32[:n], d64[n:2 * n], d32[n:2 * n])
+        total = int(4 * cap.sum()) if n else 0
+        return batch, d32[2 * n:3 * n], d32[3 * n:], d64[4 * n:], \
+            (d64[2 * n:3 * n], total, d64[3 * n:4 * n])
+
     # -- batched operations -------------------------------------------------
     def medians(self, a: np.ndarray, b: np.ndarray, out: np.ndarray):
         """Downpass medians of (a_i, b_i) into nodes out_i; returns the DO
@@ -259,9 +278,8 @@ class GpuBackend:
         n = len(a)
         st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         L = native.lib()
-        ia = torch.from_numpy(np.asarray(a, np.int32)).to(self.dev)
-        ib = torch.from_numpy(np.asarray(b, np.int32)).to(self.dev)
-        res = align.align_2(self._batch(a, b), self.cm, dos_empty=True)
+        batch, ia, ib, oi, layout = self._batch_indexed(a, b, out)
+        res = align.align_2(batch, self.cm, dos_empty=True, layout=layout)
         tmp_f = torch.empty((n, self.stride), dtype=torch.uint8, device=self.dev)
         added = torch.zeros(n, dtype=torch.int64, device=self.dev)
         if self.nf:
@@ -272,7 +290,6 @@ class GpuBackend:
             native.check(L.poyd_sank_median_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
                                                   _p(ia), _p(ib), _p(tmp_s), None, None, st))
         do_cost, f_cost = self._store(res, out, added)
-        oi = torch.from_numpy(np.asarray(out, np.int64)).to(self.dev)
         if self.nf:
             self.fitch[oi] = tmp_f
         if self.ns:
@@ -293,8 +310,8 @@ class GpuBackend:
         if n and lens.min() < 0:
             raise native.PoydError(-3, "traceback failed (code %d)" % int(lens.min()))
         src = res.out_off + 4 * res.cap - ln
-        dst_off = np.array([self._reserve(int(x)) for x in lens], np.int64)
         total = int(lens.sum())
+        dst_off = self._reserve(total) + np.cumsum(lens) - lens
         seg = torch.repeat_interleave(torch.arange(n, device=self.dev), ln)
         starts = torch.cumsum(ln, 0) - ln
         pos = torch.arange(total, device=self.dev) - starts[seg]
@@ -388,6 +405,15 @@ class GpuBackend:
         """Forget scratch node ids >= first (their pool bytes are reclaimed
         at the next compaction)."""
         self.len[first:] = 0
+
+    def sank_costs(self, vs) -> np.ndarray:
+        """Sankoff root costs of several nodes, one read-back."""
+        vs = np.asarray(vs, np.int64)
+        if not self.ns or len(vs) == 0:
+            return np.zeros(len(vs), np.int64)
+        s = self.sank[torch.from_numpy(vs).to(self.dev)]
+        c = torch.clamp(s.min(dim=2).values, max=native.SANK_INF).to(torch.int64).sum(dim=1)
+        return c.cpu().numpy()
 
     def sank_cost(self, v: int) -> int:
         if not self.ns:
@@ -834,8 +860,7 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
             for i in range(len(r)):
                 detail.setdefault(int(r[i, 0]), []).append(
                     (int(r[i, 4]), int(r[i, 3]), int(do[i]), int(fi[i])))
-    totals = np.array([diag.total - old[m] + new[m] - base_sank + be.sank_cost(roots[m])
-                       for m in range(len(moves))], np.int64)
+    totals = diag.total - old + new - base_sank + be.sank_costs(roots)
     if detail is None:
         be.release_nodes(2 * t.n)
     return totals
@@ -961,7 +986,7 @@ def _all_directions(tree: Tree, be) -> _AllDir | None:
     do, fi = be.medians(np.array(a, np.int64), np.array(b, np.int64), out)
     other = np.array(bfi, np.int64) + fi
     if getattr(be, "ns", 0):
-        other = other + np.array([be.sank_cost(int(v)) for v in out], np.int64)
+        other = other + be.sank_costs(out)
     return _AllDir(adj, info, edges, out, np.array(bdo, np.int64) + do, other,
                    nxt + len(edges))
 

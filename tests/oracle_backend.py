@@ -70,6 +70,9 @@ class OracleBackend:
                 out.append(O.cost_2(s1, s2, self.om, max(abs(len(s1) - len(s2)), 8)))
         return np.array(out, np.int64)
 
+    def sank_costs(self, vs):
+        return np.array([self.sank_cost(v) for v in vs], np.int64)
+
     def sank_cost(self, v):
         if not self.ns:
             return 0
