@@ -5,8 +5,8 @@ candidate join (pruned subtree s onto the edge above e) changes the cost
 relative to s's current attachment.  The exact search logs its own
 (candidate, exact delta) pairs for training; at search time the network
 orders all candidates, only the best-predicted fraction is scored with the
-exact DP, and the exact downpass remains the sole judge of every accepted
-tree.  When a learned pass accepts nothing, an exhaustive pass is the
+exact DP, and the exact downpass alone decides whether a tree is
+accepted.  When a learned pass accepts nothing, an exhaustive pass is the
 fallback, so the search stops at the same kind of local optimum.
 
 Features (32, computed on the device): clade sizes, depths, sequence and
