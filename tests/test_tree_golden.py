@@ -101,3 +101,42 @@ def test_formats():
     part = formats.parse_tree("(t1 (t2 t4))", names)
     assert sorted(part.nodes())[:3] == [0, 1, 3] and not part.in_tree[2]
     assert search.Tree.min_codes(t)[t.root] == 0
+
+
+def _rooted_on(adj, n, u, v):
+    """A Tree over the unrooted adjacency `adj`, rooted on edge (u, v)."""
+    t = search.Tree(n)
+    nxt = [n]
+
+    def build(x, frm):
+        if x < n:
+            return x
+        kids = [build(c, x) for c in adj[x] if c != frm]
+        w = nxt[0]
+        nxt[0] += 1
+        t.kids[w] = kids
+        t.parent[kids[0]] = t.parent[kids[1]] = w
+        return w
+
+    a, b = build(u, v), build(v, u)
+    r = nxt[0]
+    t.kids[r] = (a, b)
+    t.parent[a] = t.parent[b] = r
+    t.parent[r] = -1
+    t.root = r
+    t.free = []
+    t.in_tree[t.nodes()] = True
+    return t
+
+
+def test_root_costs_equal_downpass_of_every_rooting():
+    """Each edge's root cost equals the ordinary downpass total of the tree
+    rooted on that edge (Fitch and Sankoff characters included)."""
+    data = simulate.simulate(4, 9, 90, 12, 3)
+    om = O.cm_dna(1, 2, -1)
+    t, _ = search.wagner(data.n_taxa, OracleBackend(data, om))
+    rc = search.root_costs(t, OracleBackend(data, om))
+    adj = search.unrooted_adjacency(t)
+    for (u, v), c in zip(rc.edges.tolist(), rc.costs.tolist()):
+        T = _rooted_on(adj, t.n, u, v)
+        assert search.downpass(T, OracleBackend(data, om)).total == c, (u, v)
