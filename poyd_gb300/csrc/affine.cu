@@ -10,13 +10,15 @@
 // The band of row i is columns [max(1, i-39), min(e0+i-1, lenj)] with a
 // vertical boundary cell just left of it and, while the band has not
 // reached lenj, a HIGH_NUM boundary cell just right of it.  In diagonal
-// coordinates d = j - i that is d in [-40, e0] for every row, so one warp
-// sweeps it exactly like the linear kernel: lane k owns row 32*strip+k and
-// handles diagonal d at step d + 40 + 2k.  The four states (EH, EV, EB, CB)
-// of row i-1 at column j arrive from lane k-1 by shuffles, with the column
-// characters (sj[j], sj[j-1]); lane 0 reads the previous strip's last row
-// from a per-warp global slab of 16-byte records.  The bt variant packs the
-// bits backtrace_affine reads into one byte per cell (4 cells per word).
+// coordinates d = j - i that is d in [-40, e0] for every row.  A half warp
+// sweeps one pair's band (a warp runs two pairs side by side): lane k of
+// the half owns row 16*strip+k and handles diagonal d at step d + 40 + 2k.
+// The four states (EH, EV, EB, CB) of row i-1 at column j arrive from lane
+// k-1 by shuffles; the column quantities come from a shared window staged
+// per 32-step block; lane 0 of the half reads the previous strip's last row
+// from a per-half global slab of 16-byte records.  The bt variant packs
+// the bits backtrace_affine reads into one byte per cell (4 cells per
+// word, 16 words per strip row group).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -33,6 +35,10 @@ constexpr unsigned kFullA = 0xffffffffu;
 constexpr int kHigh = 1000000;  // HIGH_NUM (algn.c:38)
 constexpr int kStart = 40;      // start_v (algn.c:2291)
 constexpr int kDlo = -40;
+// Rows per strip: one per lane of a half warp; a warp runs two pairs side
+// by side, one per half (the strips' pipeline ramp is 2 * (kAffRows - 1)
+// steps, against an ~85-diagonal band).
+constexpr int kAffRows = 16;
 
 // One-byte direction code: bits 0-1 the m_todo choice (0 H, 1 A, 2 V, 3 D:
 // DO_HORIZONTAL > DO_ALIGN > DO_VERTICAL > DO_DIAGONAL, algn.c:2005-2012),
@@ -114,8 +120,8 @@ __global__ void k_aff_plan(AffPlanArgs A) {
   P.leni = leni; P.lenj = lenj; P.e0 = e0;
   P.wd = e0 - kDlo + 1;
   P.swap = swap;
-  P.nstrips = (leni + 1 + 31) / 32;
-  const int S = P.wd + 62;
+  P.nstrips = (leni + 1 + kAffRows - 1) / kAffRows;
+  const int S = P.wd + 2 * (kAffRows - 1);
   const int Spad = (S + 15) / 16 * 16;  // whole 16-step half blocks
   P.sblocks = Spad / 4;
   P.empty = 0;
@@ -127,7 +133,7 @@ __global__ void k_aff_plan(AffPlanArgs A) {
   }
   for (int t = 0; t < 4; ++t) P.pad_[t] = 0;
   A.plans[id] = P;
-  A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * 32;
+  A.dm_words[id] = (int64_t)P.nstrips * P.sblocks * kAffRows;
   A.wd_out[id] = P.wd;
   if (A.cells) {
     long long c = lenj + 1;
@@ -152,9 +158,9 @@ __global__ void k_aff_plan(AffPlanArgs A) {
 struct AffSmem {
   uint32_t tab[1024];            // packed {cost[a][b], cost[gap][b]}
   uint16_t cost[1024];           // cost[a][b]
-  int4 col[8][64];               // per warp: the 64 columns of a 32-step block (AffCol)
-  int4 ring_in[8][32];           // per warp: lane 0's inputs of the block
-  int4 ring_out[8][32];          // per warp: lane 31's states of the block
+  int4 col[8][2][64];            // per half warp: the columns of a 32-step block (AffCol)
+  int4 ring_in[8][2][32];        // per half warp: its first lane's inputs of the block
+  int4 ring_out[8][2][32];       // per half warp: its last lane's states of the block
 };
 
 // Column quantities of column j (algn.c:2321-2328 / 2451-2457), computed
@@ -170,7 +176,8 @@ __device__ __forceinline__ int4 aff_column(const uint32_t *tab, int jc, int jp, 
   return make_int4(hext, sj_open + sj_ext, sj_open, jc);
 }
 
-// 16 steps of one strip: cells (i, j = i + d) with d = kDlo + s - 2 * lane at
+// 16 steps of one strip of a half warp (`lane` is the lane in the half, the
+// row in the strip): cells (i, j = i + d) with d = kDlo + s - 2 * lane at
 // step s = s0 + u.  The four states of row i-1 at column j come from lane
 // k-1 by shuffles (lane 0: from ring_in, the previous strip's last row), the
 // column characters from the block's window, and lane 31's states go to
@@ -202,10 +209,10 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
   const int v_open = R.si_open + R.si_ext;
 #pragma unroll
   for (int u = 0; u < 16; ++u) {
-    int u_eh = __shfl_up_sync(kFullA, S.m_eh, 1);
-    int u_ev = __shfl_up_sync(kFullA, S.m_ev, 1);
-    int u_eb = __shfl_up_sync(kFullA, S.m_eb, 1);
-    int u_cb = __shfl_up_sync(kFullA, S.m_cb, 1);
+    int u_eh = __shfl_up_sync(kFullA, S.m_eh, 1, kAffRows);
+    int u_ev = __shfl_up_sync(kFullA, S.m_ev, 1, kAffRows);
+    int u_eb = __shfl_up_sync(kFullA, S.m_eb, 1, kAffRows);
+    int u_cb = __shfl_up_sync(kFullA, S.m_cb, 1, kAffRows);
     if (lane == 0) {
       const int4 v = rin[u];
       u_eh = v.x; u_ev = v.y; u_eb = v.z; u_cb = v.w;
@@ -258,37 +265,48 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
     if (ENDS && u == R.uF) S.result = f;
     if (BT) {
       S.word = (S.word << 8) | code;
-      if ((u & 3) == 3) dmb[(u >> 2) * 32] = S.word;
+      if ((u & 3) == 3 && dmb) dmb[(u >> 2) * kAffRows] = S.word;
     }
     S.m_eh = eh; S.m_ev = ev; S.m_eb = eb; S.m_cb = cb;
-    if (lane == 31) rout[u] = make_int4(eh, ev, eb, cb);
+    if (lane == kAffRows - 1) rout[u] = make_int4(eh, ev, eb, cb);
     S.eh_d = u_eh; S.ev_d = u_ev; S.eb_d = u_eb; S.cb_d = u_cb;
     S.eh_l = eh; S.cb_l = cb;
   }
 }
 
+// Two pairs per warp, one per half warp (16 lanes, 16-row strips).  Both
+// halves run the same strip / block / half-block loop, to the larger pair's
+// bounds; a half whose pair has no strip or step left computes cells that
+// nothing reads and writes no direction word, boundary record or cost.
 template <bool BT>
 __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int warp,
-                                         const AffPlan &P, int64_t dm_off, int id, int4 *bnd,
-                                         int lane) {
+                                         const AffPlan &P, bool has, int64_t dm_off, int id,
+                                         int4 *bnd, int lane) {
+  const int h = lane >> 4, k = lane & (kAffRows - 1);
   const uint8_t *si = A.seq + P.si_off;
   const uint8_t *sj = A.seq + P.sj_off;
   const int leni = P.leni, lenj = P.lenj, e0 = P.e0, wd = P.wd, go = A.go;
-  const int Spad = P.sblocks * 4;
-  int4 *win = sm.col[warp];
-  int4 *rin = sm.ring_in[warp], *rout = sm.ring_out[warp];
-  // this lane's column j at block step u is window index 32 + u - lane
-  const int4 *wl = win + 32 - lane;
+  const int Th = has ? P.nstrips : 0, Sh = has ? P.sblocks * 4 : 0;
+  const int To = __shfl_xor_sync(kFullA, Th, kAffRows);  // the other half's pair
+  const int So = __shfl_xor_sync(kFullA, Sh, kAffRows);
+  const int T = max(Th, To);
+  int4 *win = sm.col[warp][h];
+  int4 *rin = sm.ring_in[warp][h], *rout = sm.ring_out[warp][h];
+  // this lane's column j at block step u is window index 16 + u - k
+  const int4 *wl = win + kAffRows - k;
   const int4 kHigh4 = make_int4(kHigh, kHigh, kHigh, kHigh);
   AffState S;
   S.result = 0;
   uint32_t *dm = BT ? A.dm + dm_off : nullptr;
 
-  for (int strip = 0; strip < P.nstrips; ++strip) {
-    const int r0 = strip * 32;
+  for (int strip = 0; strip < T; ++strip) {
+    const bool act = strip < Th;
+    const int Spad = max(act ? Sh : 0, strip < To ? So : 0);  // the same in both halves
+    const bool ends = strip == 0 || strip == Th - 1 || strip == To - 1;
+    const int r0 = strip * kAffRows;
     AffRow R;
-    R.i = r0 + lane;
-    const bool rowok = R.i <= leni;
+    R.i = r0 + k;
+    const bool rowok = act && R.i <= leni;
     R.ic = rowok ? si[R.i] : 0;
     R.ip = (rowok && R.i > 0) ? si[R.i - 1] : 0;
     R.si_ext = (int)(sm.tab[(R.ic << 5) | 16] & 0xffffu);
@@ -298,60 +316,63 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
     R.icg = (R.ic & 16) ? -1 : 0;
     const int d_lb = (-R.i > kDlo) ? -R.i : kDlo;
     const bool has_rb = e0 <= lenj - R.i;
-    const int sL = d_lb - kDlo + 2 * lane;
-    const int sR = has_rb ? e0 - kDlo + 2 * lane : -1000000;
-    const int sF = (R.i == leni) ? (lenj - leni) - kDlo + 2 * lane : -1000000;
+    const int sL = d_lb - kDlo + 2 * k;
+    const int sR = has_rb ? e0 - kDlo + 2 * k : -1000000;
+    const int sF = (act && R.i == leni) ? (lenj - leni) - kDlo + 2 * k : -1000000;
 
     S.eh_l = kHigh; S.cb_l = kHigh;
     S.eh_d = kHigh; S.ev_d = kHigh; S.eb_d = kHigh; S.cb_d = kHigh;
     S.m_eh = kHigh; S.m_ev = kHigh; S.m_eb = kHigh; S.m_cb = kHigh;
     S.word = 0;
-    if (lane == 0 && strip > 0) {
+    if (k == 0 && act && strip > 0) {
       const int4 v = bnd[0];
       S.eh_d = v.x; S.ev_d = v.y; S.eb_d = v.z; S.cb_d = v.w;
     }
     for (int s0 = 0; s0 < Spad; s0 += 32) {
-      // stage the block: lane 0's inputs bnd[s + 1], the 64 columns
-      // r0 - 40 + s0 - 32 + x (x = 0..63), lane 31's states go to ring_out
+      // stage the block: the first lane's inputs bnd[s + 1], the 64 columns
+      // r0 - 40 + s0 - 16 + x (x = 0..63); the last lane's states go to ring_out
       __syncwarp();
       {
-        const int x = s0 + lane + 1;
-        rin[lane] = (strip > 0 && x < wd) ? bnd[x] : kHigh4;
-        // columns jb and jb + 32, each with its predecessor
-        const int jb = r0 + kDlo + s0 - 32 + lane;
         auto chr = [&](int j) { return (j >= 0 && j <= lenj) ? (int)sj[j] : 0; };
-        const int c0 = chr(jb), c1 = chr(jb + 32);
+        const int jb = r0 + kDlo + s0 - kAffRows;
+#pragma unroll
+        for (int e = k; e < 32; e += kAffRows) {
+          const int x = s0 + e + 1;
+          rin[e] = (act && strip > 0 && x < wd) ? bnd[x] : kHigh4;
+        }
         // window index 0 is read only as the predecessor of index 1
-        win[lane] = aff_column(sm.tab, c0, chr(jb - 1), jb, go);
-        win[lane + 32] = aff_column(sm.tab, c1, chr(jb + 31), jb + 32, go);
+#pragma unroll
+        for (int x = k; x < 64; x += kAffRows)
+          win[x] = aff_column(sm.tab, chr(jb + x), chr(jb + x - 1), jb + x, go);
       }
       __syncwarp();
-      uint32_t *dmb = BT ? dm + ((int64_t)strip * P.sblocks + (s0 >> 2)) * 32 + lane : nullptr;
+      uint32_t *dmb = (BT && act) ? dm + ((int64_t)strip * P.sblocks + (s0 >> 2)) * kAffRows + k
+                                  : nullptr;
 #pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
-        const int hs = s0 + 16 * h;
-        if (hs >= Spad) break;  // a strip may end on a half block; its lane 31
-                                // positions past the band are not copied out
+      for (int hh = 0; hh < 2; ++hh) {
+        const int hs = s0 + 16 * hh;
+        if (hs >= Spad) break;  // a strip may end on a half block; the last
+                                // lane's positions past the band are not copied out
         R.uL = sL - hs;
         R.uR = sR - hs;
         R.uF = sF - hs;
-        if (strip == 0 || strip == P.nstrips - 1)
-          aff_half<BT, true>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
-                             BT ? dmb + 4 * 32 * h : nullptr, lane);
+        uint32_t *dmh = (dmb && hs < Sh) ? dmb + 4 * kAffRows * hh : nullptr;
+        if (ends)
+          aff_half<BT, true>(S, R, sm, wl + 16 * hh, rin + 16 * hh, rout + 16 * hh, hs, go, dmh, k);
         else
-          aff_half<BT, false>(S, R, sm, wl + 16 * h, rin + 16 * h, rout + 16 * h, hs, go,
-                              BT ? dmb + 4 * 32 * h : nullptr, lane);
+          aff_half<BT, false>(S, R, sm, wl + 16 * hh, rin + 16 * hh, rout + 16 * hh, hs, go, dmh, k);
       }
       __syncwarp();
-      {
-        const int x = s0 + lane - 62;  // lane 31's band index at block step lane
-        if (x >= 0 && x < wd) bnd[x] = rout[lane];
+#pragma unroll
+      for (int e = k; e < 32; e += kAffRows) {
+        const int x = s0 + e - 2 * (kAffRows - 1);  // the last lane's band index at block step e
+        if (act && x >= 0 && x < wd) bnd[x] = rout[e];
       }
     }
     __syncwarp();
   }
-  S.result = __shfl_sync(kFullA, S.result, leni & 31);
-  if (lane == 0) A.cost[id] = S.result;
+  const int r = __shfl_sync(kFullA, S.result, h * kAffRows + (leni & (kAffRows - 1)));
+  if (k == 0 && has) A.cost[id] = r;
 }
 
 template <bool BT>
@@ -365,19 +386,28 @@ __global__ void __launch_bounds__(256, 3) k_aff_dp(AffDpArgs A) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int4 *bnd = A.scratch + gw * A.slab;
+  const int h = lane >> 4;
+  int4 *bnd = A.scratch + (gw * 2 + h) * A.slab;  // one boundary slab per half warp
   for (;;) {
     int p = 0;
-    if (lane == 0) p = atomicAdd(A.counter, 1);
+    if (lane == 0) p = atomicAdd(A.counter, 2);  // consecutive pairs: similar sizes
     p = __shfl_sync(kFullA, p, 0);
     if (p >= A.n) break;
-    const int id = A.order ? A.order[p] : p;
-    const AffPlan P = A.plans[id];
-    if (P.empty) {
-      if (lane == 0) A.cost[id] = 0;
-      continue;
+    const int ph = p + h;
+    bool has = ph < A.n;
+    const int id = has ? (A.order ? A.order[ph] : ph) : 0;
+    AffPlan P = {};
+    P.leni = P.lenj = -1;
+    if (has) {
+      const AffPlan Q = A.plans[id];
+      if (Q.empty) {
+        if ((lane & (kAffRows - 1)) == 0) A.cost[id] = 0;
+        has = false;
+      } else {
+        P = Q;
+      }
     }
-    aff_pair<BT>(A, sm, warp, P, BT ? A.dm_off[id] : 0, id, bnd, lane);
+    aff_pair<BT>(A, sm, warp, P, has, (BT && has) ? A.dm_off[id] : 0, id, bnd, lane);
   }
 }
 
@@ -429,9 +459,9 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
     const int d = j - i;
     const int d_lb = (-i > kDlo) ? -i : kDlo;
     if (d < d_lb || d > e0 || (d == e0 && !(e0 <= lenj - i))) { bad = true; break; }
-    const int k = i & 31, strip = i >> 5;
+    const int k = i & (kAffRows - 1), strip = i / kAffRows;
     const int s = d - kDlo + 2 * k;
-    const uint32_t w = dm[((int64_t)strip * sb + (s >> 2)) * 32 + k];
+    const uint32_t w = dm[((int64_t)strip * sb + (s >> 2)) * kAffRows + k];
     const uint32_t c = (w >> (8 * (3 - (s & 3)))) & 0xffu;
     if (mode == 0) {
       const uint32_t t = c & 3u;
@@ -570,7 +600,7 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
   }
   const int blocks = aff_blocks(want_align);
   const int64_t slab = maxwd + 8;
-  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH, sizeof(int4) * (size_t)slab * (size_t)blocks * 8);
+  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH, sizeof(int4) * (size_t)slab * (size_t)blocks * 8 * 2);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
   AffDpArgs DA;
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
