@@ -164,9 +164,11 @@ def learned_scorer(prop: Proposal, be, frac: float = 0.03, min_k: int = 64, stat
     def scorer(t, S, E):
         cur = current_attachment(t, be, S)
         X = features(t, be, S, E, cur)
-        pred = prop.predict(X).cpu().numpy()
+        pred = prop.predict(X)
         k = min(len(S), max(min_k, int(frac * len(S))))
-        top = np.argsort(pred, kind="stable")[:k]
+        # best-predicted first, ties by candidate index (a stable sort on
+        # the device; only the chosen indices come back)
+        top = torch.sort(pred, stable=True).indices[:k].cpu().numpy()
         out = np.full(len(S), np.iinfo(np.int64).max // 4, np.int64)
         out[top] = be.distances(S[top], E[top])
         if stats is not None:
