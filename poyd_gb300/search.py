@@ -365,7 +365,9 @@ class GpuBackend:
             self.sank[d] = self.sank[s]
 
     def distances(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
-        """Candidate-join distance d(a_i, b_i) = DOS.distance + Fitch + Sankoff."""
+        """Candidate-join distance d(a_i, b_i) = DOS.distance + Fitch + Sankoff,
+        with the join cost's missing distance 0 for an all-gap sequence
+        (``Node.Standard.distance 0.``, allDirChar.ml:1305-1316)."""
         n = len(a)
         st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         L = native.lib()
@@ -373,6 +375,13 @@ class GpuBackend:
         ib = torch.from_numpy(np.asarray(b, np.int32)).to(self.dev)
         do, cells = align.cost_2(self._batch(a, b), self.cm, deltaw="dos", band_cells=True)
         tot = do.to(torch.int64)
+        u, inv = np.unique(np.concatenate([np.asarray(a, np.int64), np.asarray(b, np.int64)]),
+                           return_inverse=True)
+        e = self._empty(u)
+        if e.any():
+            e = e[inv]
+            keep = ~(e[:n] | e[n:])
+            tot = tot * torch.from_numpy(keep.astype(np.int64)).to(self.dev)
         if self.nf:
             fd = torch.empty(n, dtype=torch.int64, device=self.dev)
             native.check(L.poyd_nonadd8_distance_batch(_p(self.fitch), C.c_int64(self.stride), self.nf,

@@ -95,3 +95,20 @@ def test_tbr_pass_matches_oracle(seed, n_fitch, n_sank):
         (so.cost_before, so.cost_after, so.moves_accepted)
     assert sg.cost_after <= sg.cost_before
     _compare_nodes(tg, g, o)
+
+
+def test_search_with_an_empty_leaf_matches_oracle():
+    """An all-gap leaf sequence (an empty '#' fragment): the DOS.median and
+    join-cost empty rules through the CUDA kernels equal the oracle's."""
+    data = simulate.simulate(41, 16, 200, 20, 3)
+    data.seqs[5] = np.array([16], np.uint8)
+    g = search.GpuBackend(data, align.CostMatrix.default())
+    o = OracleBackend(data, O.cm_dna(1, 2, -1))
+    tg, dg = search.wagner(data.n_taxa, g)
+    to, do = search.wagner(data.n_taxa, o)
+    assert tg.newick() == to.newick() and dg.total == do.total
+    sg = search.spr_pass(tg, g, max_moves=6, diag=dg)
+    so = search.spr_pass(to, o, max_moves=6, diag=do)
+    assert tg.newick() == to.newick() and sg.cost_after == so.cost_after
+    _compare_nodes(tg, g, o)
+    assert search.final_cost(tg, g).cost == search.final_cost(to, o).cost

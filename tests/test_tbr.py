@@ -95,3 +95,17 @@ def test_tbr_pass_lowers_or_keeps_cost():
     assert st.cost_after <= st.cost_before
     assert search.downpass(t, be).total == st.cost_after
     assert sorted(v for v in t.nodes() if v < t.n) == list(range(t.n))
+
+
+def test_join_distance_of_an_empty_sequence_is_zero():
+    """A join with an all-gap sequence costs nothing on the DO character
+    (the join cost's missing distance, Node.Standard.distance 0.)."""
+    data = simulate.simulate(9, 6, 80, 10, 2)
+    data.seqs[2] = np.array([16], np.uint8)
+    be = OracleBackend(data, O.cm_dna(1, 2, -1))
+    full = be.distances([2, 0], [0, 1])
+    fitch_sank = [O.nonadd_distance(be.fitch[2], be.fitch[0]) +
+                  int(sum(O.sank_elt_distance(be.tcm, be.sank[2][c], be.sank[0][c])
+                          for c in range(be.ns)))]
+    assert int(full[0]) == fitch_sank[0]
+    assert int(full[1]) > 0
