@@ -10,15 +10,16 @@
 // The band of row i is columns [max(1, i-39), min(e0+i-1, lenj)] with a
 // vertical boundary cell just left of it and, while the band has not
 // reached lenj, a HIGH_NUM boundary cell just right of it.  In diagonal
-// coordinates d = j - i that is d in [-40, e0] for every row.  A half warp
-// sweeps one pair's band (a warp runs two pairs side by side): lane k of
-// the half owns row 16*strip+k and handles diagonal d at step d + 40 + 2k.
-// The four states (EH, EV, EB, CB) of row i-1 at column j arrive from lane
-// k-1 by shuffles; the column quantities come from a shared window staged
-// per 32-step block; lane 0 of the half reads the previous strip's last row
-// from a per-half global slab of 16-byte records.  The bt variant packs
-// the bits backtrace_affine reads into one byte per cell (4 cells per
-// word, 16 words per strip row group).
+// coordinates d = j - i that is d in [-40, e0] for every row.  A group of
+// kAffRows lanes sweeps one pair's band (a warp runs 32 / kAffRows pairs
+// side by side): lane k of the group owns row kAffRows*strip+k and handles
+// diagonal d at step d + 40 + 2k.  The four states (EH, EV, EB, CB) of row
+// i-1 at column j arrive from lane k-1 by shuffles; the column quantities
+// come from a shared window staged per 32-step block; lane 0 of the group
+// reads the previous strip's last row from a per-group global slab of
+// 16-byte records.  The bt variant packs the bits backtrace_affine reads
+// into one byte per cell (4 cells per word, kAffRows words per strip and
+// 4-step column).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -35,10 +36,12 @@ constexpr unsigned kFullA = 0xffffffffu;
 constexpr int kHigh = 1000000;  // HIGH_NUM (algn.c:38)
 constexpr int kStart = 40;      // start_v (algn.c:2291)
 constexpr int kDlo = -40;
-// Rows per strip: one per lane of a half warp; a warp runs two pairs side
-// by side, one per half (the strips' pipeline ramp is 2 * (kAffRows - 1)
-// steps, against an ~85-diagonal band).
-constexpr int kAffRows = 16;
+// Rows per strip: one per lane of a lane group; a warp runs kAffGroups
+// pairs side by side, one per group (the strips' pipeline ramp is
+// 2 * (kAffRows - 1) steps, against an ~85-diagonal band).
+constexpr int kAffRows = 8;
+constexpr int kAffGroups = 32 / kAffRows;  // pairs per warp
+constexpr int kAffWarps = 4;                // warps per block (24 per SM)
 
 // One-byte direction code: bits 0-1 the m_todo choice (0 H, 1 A, 2 V, 3 D:
 // DO_HORIZONTAL > DO_ALIGN > DO_VERTICAL > DO_DIAGONAL, algn.c:2005-2012),
@@ -158,9 +161,9 @@ __global__ void k_aff_plan(AffPlanArgs A) {
 struct AffSmem {
   uint32_t tab[1024];            // packed {cost[a][b], cost[gap][b]}
   uint16_t cost[1024];           // cost[a][b]
-  int4 col[8][2][64];            // per half warp: the columns of a 32-step block (AffCol)
-  int4 ring_in[8][2][32];        // per half warp: its first lane's inputs of the block
-  int4 ring_out[8][2][32];       // per half warp: its last lane's states of the block
+  int4 col[kAffWarps][kAffGroups][64];   // per lane group: the columns of a 32-step block (AffCol)
+  int4 ring_in[kAffWarps][kAffGroups][32];   // per lane group: its first lane's inputs of the block
+  int4 ring_out[kAffWarps][kAffGroups][32];  // per lane group: its last lane's states of the block
 };
 
 // Column quantities of column j (algn.c:2321-2328 / 2451-2457), computed
@@ -176,8 +179,8 @@ __device__ __forceinline__ int4 aff_column(const uint32_t *tab, int jc, int jp, 
   return make_int4(hext, sj_open + sj_ext, sj_open, jc);
 }
 
-// 16 steps of one strip of a half warp (`lane` is the lane in the half, the
-// row in the strip): cells (i, j = i + d) with d = kDlo + s - 2 * lane at
+// 16 steps of one strip of a lane group (`lane` is the lane in the group,
+// the row in the strip): cells (i, j = i + d) with d = kDlo + s - 2 * lane at
 // step s = s0 + u.  The four states of row i-1 at column j come from lane
 // k-1 by shuffles (lane 0: from ring_in, the previous strip's last row), the
 // column characters from the block's window, and lane 31's states go to
@@ -274,22 +277,21 @@ __device__ __forceinline__ void aff_half(AffState &S, const AffRow &R, const Aff
   }
 }
 
-// Two pairs per warp, one per half warp (16 lanes, 16-row strips).  Both
-// halves run the same strip / block / half-block loop, to the larger pair's
-// bounds; a half whose pair has no strip or step left computes cells that
-// nothing reads and writes no direction word, boundary record or cost.
+// kAffGroups pairs per warp, one per group of kAffRows lanes (kAffRows-row
+// strips).  Every group runs the same strip / block / half-block loop, to
+// the largest pair's bounds; a group whose pair has no strip or step left
+// computes cells that nothing reads and writes no direction word, boundary
+// record or cost.
 template <bool BT>
 __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int warp,
                                          const AffPlan &P, bool has, int64_t dm_off, int id,
                                          int4 *bnd, int lane) {
-  const int h = lane >> 4, k = lane & (kAffRows - 1);
+  const int h = lane / kAffRows, k = lane & (kAffRows - 1);
   const uint8_t *si = A.seq + P.si_off;
   const uint8_t *sj = A.seq + P.sj_off;
   const int leni = P.leni, lenj = P.lenj, e0 = P.e0, wd = P.wd, go = A.go;
   const int Th = has ? P.nstrips : 0, Sh = has ? P.sblocks * 4 : 0;
-  const int To = __shfl_xor_sync(kFullA, Th, kAffRows);  // the other half's pair
-  const int So = __shfl_xor_sync(kFullA, Sh, kAffRows);
-  const int T = max(Th, To);
+  const int T = __reduce_max_sync(kFullA, Th);  // the largest pair of the warp
   int4 *win = sm.col[warp][h];
   int4 *rin = sm.ring_in[warp][h], *rout = sm.ring_out[warp][h];
   // this lane's column j at block step u is window index 16 + u - k
@@ -301,8 +303,8 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
 
   for (int strip = 0; strip < T; ++strip) {
     const bool act = strip < Th;
-    const int Spad = max(act ? Sh : 0, strip < To ? So : 0);  // the same in both halves
-    const bool ends = strip == 0 || strip == Th - 1 || strip == To - 1;
+    const int Spad = __reduce_max_sync(kFullA, act ? Sh : 0);  // the same in every group
+    const bool ends = __any_sync(kFullA, strip == 0 || strip == Th - 1);
     const int r0 = strip * kAffRows;
     AffRow R;
     R.i = r0 + k;
@@ -376,7 +378,7 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
 }
 
 template <bool BT>
-__global__ void __launch_bounds__(256, 3) k_aff_dp(AffDpArgs A) {
+__global__ void __launch_bounds__(kAffWarps * 32, 24 / kAffWarps) k_aff_dp(AffDpArgs A) {
   __shared__ AffSmem sm;
   for (int t = threadIdx.x; t < 1024; t += blockDim.x) {
     sm.tab[t] = A.tables->packed[t];
@@ -386,11 +388,11 @@ __global__ void __launch_bounds__(256, 3) k_aff_dp(AffDpArgs A) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int h = lane >> 4;
-  int4 *bnd = A.scratch + (gw * 2 + h) * A.slab;  // one boundary slab per half warp
+  const int h = lane / kAffRows;
+  int4 *bnd = A.scratch + (gw * kAffGroups + h) * A.slab;  // one boundary slab per lane group
   for (;;) {
     int p = 0;
-    if (lane == 0) p = atomicAdd(A.counter, 2);  // consecutive pairs: similar sizes
+    if (lane == 0) p = atomicAdd(A.counter, kAffGroups);  // consecutive pairs: similar sizes
     p = __shfl_sync(kFullA, p, 0);
     if (p >= A.n) break;
     const int ph = p + h;
@@ -526,8 +528,8 @@ int aff_blocks(bool bt) {
   int &c = cache[bt ? 1 : 0][dev & 63];
   if (!c) {
     int per_sm = 0, sms = 0;
-    if (bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<true>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<false>, 256, 0);
+    if (bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<true>, kAffWarps * 32, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<false>, kAffWarps * 32, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   }
@@ -600,7 +602,9 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
   }
   const int blocks = aff_blocks(want_align);
   const int64_t slab = maxwd + 8;
-  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH, sizeof(int4) * (size_t)slab * (size_t)blocks * 8 * 2);
+  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH,
+                                    sizeof(int4) * (size_t)slab * (size_t)blocks * kAffWarps *
+                                        kAffGroups);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
   AffDpArgs DA;
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
@@ -608,8 +612,8 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
   DA.cost = cost;
   {
     ProfScope ps(want_align ? "aff_dp_dm" : "aff_dp_cost", st);
-    if (want_align) k_aff_dp<true><<<blocks, 256, 0, st>>>(DA);
-    else k_aff_dp<false><<<blocks, 256, 0, st>>>(DA);
+    if (want_align) k_aff_dp<true><<<blocks, kAffWarps * 32, 0, st>>>(DA);
+    else k_aff_dp<false><<<blocks, kAffWarps * 32, 0, st>>>(DA);
   }
   CKA(cudaGetLastError());
   if (want_align) {
