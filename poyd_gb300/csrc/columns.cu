@@ -177,15 +177,16 @@ int columns_host(int op, const uint8_t *a, const uint8_t *b, int32_t len, const 
   int64_t *meta = (int64_t *)ws_buffer(w, WS_META, 64);
   if (!buf || !meta) return fail(POYD_ENOMEM, "column operation: workspace");
   const int64_t hm[3] = {0, (int64_t)L, (int64_t)(2 * L)};
-  cudaMemcpy(buf, a, L, cudaMemcpyHostToDevice);
-  cudaMemcpy(buf + L, b, L, cudaMemcpyHostToDevice);
-  cudaMemcpy(meta, hm, sizeof hm, cudaMemcpyHostToDevice);
   int32_t *m32 = (int32_t *)(meta + 3);
-  cudaMemcpy(m32, &len, sizeof len, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemcpy(buf, a, L, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(buf + L, b, L, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(meta, hm, sizeof hm, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m32, &len, sizeof len, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "column operation upload");
   int rc = columns(op, cm, 1, buf, meta, meta + 1, m32, buf, meta + 2, m32 + 1, m32 + 2, nullptr);
   if (rc) return rc;
   int32_t res[2] = {0, 0};
-  cudaError_t e = cudaMemcpy(res, m32 + 1, sizeof res, cudaMemcpyDeviceToHost);
+  e = cudaMemcpy(res, m32 + 1, sizeof res, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "column operation");
   if (op <= kAncestor) {
     *out_len = res[0];
