@@ -109,3 +109,27 @@ def test_join_distance_of_an_empty_sequence_is_zero():
                           for c in range(be.ns)))]
     assert int(full[0]) == fitch_sank[0]
     assert int(full[1]) > 0
+
+
+def test_tbr_candidate_enumeration():
+    """Every clade (parent not the root) appears with its own rooting and
+    with each re-rooting below its children, joined to every node outside
+    it except its parent (and, for its own rooting, its sibling)."""
+    data, be, t, diag = _setup(seed=8, n=10, length=60)
+    S, U, E, score, dclade = search.tbr_candidates(t, be, diag)
+    nodes = set(t.nodes())
+    want = set()
+    for s in nodes:
+        p = t.parent[s]
+        if p < 0 or t.parent[p] < 0:
+            continue
+        inside = set(t.subtree(s))
+        sib = int(t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1])
+        reroots = [-1] + [u for u in inside if u != s and t.parent[u] != s]
+        for u in reroots:
+            for e in nodes - inside - {int(p)}:
+                if u < 0 and e == sib:
+                    continue
+                want.add((s, u, e))
+    got = set(zip(S.tolist(), U.tolist(), E.tolist()))
+    assert len(got) == len(S) and got == want
