@@ -576,10 +576,13 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     if log is not None:
         log.append((t.copy(), S, E, score))
     gain = cur[S] - score
-    order = np.lexsort((E, S, -gain))  # largest predicted gain first, ties by ids
+    # largest predicted gain first, ties by ids; only improving candidates
+    # can become moves, so only they are sorted
+    pos = np.nonzero(gain > 0)[0]
+    order = pos[np.lexsort((E[pos], S[pos], -gain[pos]))]
     moves, seen = [], set()
     for i in order:
-        if len(moves) >= max_moves or gain[i] <= 0:
+        if len(moves) >= max_moves:
             break
         s, e = int(S[i]), int(E[i])
         if s not in seen:
@@ -736,10 +739,12 @@ def tbr_pass(t: Tree, be, max_moves: int = 16, log=None, diag=None):
     if log is not None:
         log.append((t.copy(), S, U, E, score))
     gain = cur[S] - score - dclade
-    order = np.lexsort((U, E, S, -gain))  # largest predicted gain first, ties by ids
+    # largest predicted gain first, ties by ids; only improving candidates
+    pos = np.nonzero(gain > 0)[0]
+    order = pos[np.lexsort((U[pos], E[pos], S[pos], -gain[pos]))]
     moves, seen = [], set()
     for i in order:
-        if len(moves) >= max_moves or gain[i] <= 0:
+        if len(moves) >= max_moves:
             break
         s, e, u = int(S[i]), int(E[i]), int(U[i])
         if s not in seen:
