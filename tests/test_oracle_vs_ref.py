@@ -94,3 +94,94 @@ def test_fitch_vs_reference(R):
         c2, r2 = O.nonadd_median(a, b)
         assert c1 == c2 and np.array_equal(r1, r2)
         assert R.ref_nonadd8_distance(P(a), P(b), n) == O.nonadd_distance(a, b)
+
+
+# A 5x5 input (A, C, G, T, gap) that breaks the triangle inequality
+# (A-C costs more than A-G + G-C), so the tables take the bitwise fill
+# (cost_matrix.ml:520-538) rather than the metric one.
+NONMETRIC = np.array([[0, 7, 2, 3, 4],
+                      [7, 0, 2, 5, 4],
+                      [2, 2, 0, 1, 3],
+                      [3, 5, 1, 0, 4],
+                      [4, 4, 3, 4, 0]], np.int32)
+
+
+def _cm(model):
+    if model == "nonmetric":
+        m = O.OrCM()
+        O.lib().or_cm_of_matrix5(C.byref(m), NONMETRIC.ctypes.data_as(O.i32p), -1)
+        assert not m.is_metric
+        return m
+    return O.cm_dna(*model)
+
+
+def _aligned(m, seed, n, lmax):
+    A, B = _pairs(seed, n, lmax)
+    out = []
+    for a, b in zip(A, B):
+        if m.cost_model == 1:
+            _, _, _, ra, rb = O.align_affine_3(a, b, m)
+        else:
+            _, ra, rb = O.align_2(a, b, m)
+        out.append((ra, rb))
+    # gap-and-base codes on both sides of a column, and a lone gap column
+    out.append((np.array([16, 17, 18, 1, 16, 31], np.uint8),
+                np.array([16, 16, 24, 20, 2, 15], np.uint8)))
+    out.append((np.array([16], np.uint8), np.array([16], np.uint8)))
+    return out
+
+
+@pytest.mark.parametrize("model", [(1, 2, -1), (3, 1, -1), "nonmetric", (1, 2, 3), (2, 1, 1)])
+def test_column_ops_vs_reference(R, model):
+    """median_2_with_gaps, median_2_no_gaps, ancestor_2, worst_2 and
+    verify_2 (algn.c) on aligned pairs, the oracle against the reference."""
+    m = _cm(model)
+    rc = R.ref_cm_new(C.byref(m))
+    for ra, rb in _aligned(m, 31, 40, 900):
+        n = len(ra)
+        for name, want in (("ref_median_2_with_gaps", O.median_2_with_gaps(ra, rb, m)),
+                           ("ref_median_2_no_gaps", O.median_2(ra, rb, m)),
+                           ("ref_ancestor_2", O.ancestor_2(ra, rb, m))):
+            t = np.zeros(n + 2, np.uint8)
+            k = getattr(R, name)(P(ra), P(rb), n, rc, P(t))
+            assert np.array_equal(want, t[:k]), name
+        assert R.ref_worst_2(P(ra), P(rb), n, rc) == O.worst_2(ra, rb, m)
+        assert R.ref_verify_2(P(ra), P(rb), n, rc) == O.verify_2(ra, rb, m)
+    R.ref_cm_free(rc)
+
+
+def test_nonmetric_align_vs_reference(R):
+    m = _cm("nonmetric")
+    rc = R.ref_cm_new(C.byref(m))
+    for a, b in zip(*_pairs(77, 40, 1000)):
+        dw = O.deltaw(a, b, m)
+        cap = len(a) + len(b) + 2
+        o1, o2 = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+        n = C.c_int()
+        c_ref = R.ref_align_2(P(a), len(a), P(b), len(b), rc, dw, P(o1), P(o2), C.byref(n))
+        c, ra, rb = O.align_2(a, b, m)
+        assert c == c_ref
+        assert np.array_equal(ra, o1[:n.value]) and np.array_equal(rb, o2[:n.value])
+    R.ref_cm_free(rc)
+
+
+@pytest.mark.parametrize("dw", [0, 1, 5, 40, 400])
+def test_explicit_band_vs_reference(R, dw):
+    """simple_2 with a caller-chosen band width (the ?deltaw argument of
+    Sequence.Align.cost_2): the cost depends on the band, and both agree."""
+    m = O.cm_dna(1, 2, -1)
+    rc = R.ref_cm_new(C.byref(m))
+    for a, b in zip(*_pairs(dw + 3, 30, 700)):
+        s1, s2 = (a, b) if len(a) >= len(b) else (b, a)
+        assert O.simple_2(s1, s2, m, dw) == R.ref_simple_2(P(s1), len(s1), P(s2), len(s2), rc, dw)
+    R.ref_cm_free(rc)
+
+
+def test_fitch_median_3_vs_reference(R):
+    rng = np.random.default_rng(12)
+    for _ in range(20):
+        n = int(rng.integers(1, 3000))
+        A, N, D1, D2 = (rng.integers(1, 256, n).astype(np.uint8) for _ in range(4))
+        f = np.zeros(n, np.uint8)
+        R.ref_nonadd8_median_3(P(A), P(N), P(D1), P(D2), n, P(f))
+        assert np.array_equal(O.nonadd_median_3(A, N, D1, D2), f)
