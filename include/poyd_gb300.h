@@ -15,6 +15,17 @@
  *
  * Device pointers are CUDA global-memory pointers; `stream` is a
  * cudaStream_t (NULL = legacy default stream).
+ *
+ * Threads: the library keeps one grow-only scratch workspace per (device,
+ * stream).  Calls from several host threads are safe when each thread uses
+ * its own stream; calls that share a stream must not overlap in time (the
+ * same rule as a cuBLAS handle).  The single-pair affine and column entry
+ * points (poyd_algn_*_affine_3, poyd_algn_median_2_*, ancestor_2, worst_2,
+ * verify_2) run on the legacy default stream and count as calls on it.
+ * poyd_algn_simple_2 / backtrack_2d / align_2d work in the poyd_matrix they
+ * are given, so two threads need two matrices, as two OCaml domains would
+ * need two Matrix.m.  poyd_align_2_host serialises itself per device.  The
+ * message of poyd_last_error() is per thread.
  */
 #ifndef POYD_GB300_H
 #define POYD_GB300_H

@@ -74,6 +74,18 @@ struct Trace {
   }
 };
 
+// Waits for both streams when the call returns, whichever way: an early
+// error return must not leave a download still writing into the caller's
+// buffers, or the DP still writing into the pipe's buffers.
+struct Drain {
+  Pipe &P;
+  ~Drain() {
+    if (!P.ready) return;
+    cudaStreamSynchronize(P.dp);
+    cudaStreamSynchronize(P.copy);
+  }
+};
+
 #define CKH(call)                                        \
   do {                                                   \
     cudaError_t e_ = (call);                             \
@@ -106,6 +118,7 @@ extern "C" int poyd_align_2_host(const poyd_cm *cm, int32_t n, const uint8_t *se
     CKH(cudaStreamCreateWithFlags(&P.copy, cudaStreamNonBlocking));
     P.ready = true;
   }
+  Drain drain{P};
   int64_t lo = INT64_MAX, hi = 0, slots = 0;
   for (int32_t i = 0; i < n; ++i) {
     if (a_len[i] < 1 || b_len[i] < 1)
