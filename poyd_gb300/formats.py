@@ -1,4 +1,5 @@
-"""Reading POY inputs: unaligned DNA FASTA files and parenthetical trees.
+"""Reading POY inputs: unaligned DNA FASTA files, Hennig86 matrices of
+static characters and parenthetical trees.
 
 FASTA: every '#'-separated fragment of a taxon's sequence is its own
 dynamic (DO) character (``split_frag``, parser.ml:262); residues are
@@ -11,10 +12,16 @@ Trees: POY's parenthetical format, ``(a ((b c) d))`` with whitespace (or
 commas) between siblings and an optional bracketed cost after the tree
 (``[865.]``).  Taxon codes follow the order in which the FASTA file names
 the taxa; they are the leaf ids of :class:`poyd_gb300.search.Tree`.
+
+Hennig86 (xread): the static characters' state sets per taxon, their
+additive / non-additive, active and weight flags from ccode commands, and
+the tread trees (:func:`read_hennig`).  The non-additive characters give
+the 8-bit Fitch lanes of the GPU path (:meth:`HennigMatrix.fitch_matrix`).
 """
 from __future__ import annotations
 
 import re
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -129,3 +136,174 @@ def parse_tree(text: str, names):
     t.root = r
     t.in_tree[t.nodes()] = True
     return t
+
+
+# --------------------------------------------------------------------------
+# Hennig86 / TNT files (xread, ccode, tread)
+# --------------------------------------------------------------------------
+
+# state symbols in order (hennig_upto, parser.ml:3813-3833)
+HENNIG_STATES = "0123456789ABCDEFGHIJKLMNOPQRSTUV"
+
+
+@dataclass
+class HennigMatrix:
+    """A Hennig86 file as POY reads it (Parser.Hennig.of_channel,
+    parser.ml:3895-3990).
+
+    ``cells[t][c]`` is the set of raw states of taxon t at character c as a
+    bitmask over HENNIG_STATES (bit s = state s); 0 means missing ('?' or
+    '-').  Every character starts additive, active and of weight 1
+    (default_hennig, parser.ml:3790-3811) until a ccode command changes it
+    (parser.ml:3929-3951)."""
+    names: list
+    cells: np.ndarray      # [n_taxa, n_chars] uint32 state masks, 0 = missing
+    additive: np.ndarray   # [n_chars] bool
+    active: np.ndarray     # [n_chars] bool
+    weight: np.ndarray     # [n_chars] int64
+    trees: list            # parenthetical tree texts, taxa by name
+
+    def observed(self, c: int) -> list:
+        """Raw states of character c seen in some taxon, ascending."""
+        m = int(np.bitwise_or.reduce(self.cells[:, c])) if len(self.cells) else 0
+        return [s for s in range(32) if m >> s & 1]
+
+    def fitch_matrix(self):
+        """The active non-additive characters as 8-bit Fitch state masks:
+        (uint8 [n_taxa, k] masks, int64 [k] character indices, int64 [k]
+        weights).  As in POY's non-additive encoding, bit i stands for the
+        i-th observed state of the character and a missing cell holds every
+        observed state.  A character with more than 8 observed states does
+        not fit the 8-bit lanes and raises ValueError."""
+        cols = [c for c in range(self.cells.shape[1]) if self.active[c] and not self.additive[c]]
+        out = np.zeros((len(self.names), len(cols)), np.uint8)
+        for j, c in enumerate(cols):
+            obs = self.observed(c)
+            if len(obs) > 8:
+                raise ValueError("character %d has %d states; 8-bit lanes hold 8" % (c, len(obs)))
+            full = (1 << max(len(obs), 1)) - 1
+            for t in range(len(self.names)):
+                m = int(self.cells[t, c])
+                out[t, j] = full if m == 0 else sum(1 << i for i, s in enumerate(obs) if m >> s & 1)
+        cols = np.array(cols, np.int64)
+        return out, cols, self.weight[cols]
+
+    def additive_intervals(self):
+        """The active additive characters as [min, max] state intervals:
+        (uint8 [n_taxa, k] lows, uint8 [n_taxa, k] highs, int64 [k]
+        character indices); a missing cell spans the observed states."""
+        cols = [c for c in range(self.cells.shape[1]) if self.active[c] and self.additive[c]]
+        lo = np.zeros((len(self.names), len(cols)), np.uint8)
+        hi = np.zeros_like(lo)
+        for j, c in enumerate(cols):
+            obs = self.observed(c) or [0]
+            for t in range(len(self.names)):
+                m = int(self.cells[t, c])
+                st = [s for s in range(32) if m >> s & 1] or obs
+                lo[t, j], hi[t, j] = min(st), max(st)
+        return lo, hi, np.array(cols, np.int64)
+
+
+def _hennig_cell(tok: str) -> int:
+    if tok in ("?", "-"):
+        return 0
+    m = 0
+    for ch in tok.strip("[]"):
+        if ch in " .":
+            continue
+        s = HENNIG_STATES.find(ch.upper())
+        if s < 0:
+            raise ValueError("illegal Hennig state %r" % ch)
+        m |= 1 << s
+    return m
+
+
+def _hennig_ccode(body: str, flags, n_chars: int) -> None:
+    """One ccode command: verbs '+' additive, '-' non-additive, '[' active,
+    ']' inactive, '/w' weight w (default 1), '*' reset, each applying to the
+    character ranges after it ('a.b'; a missing bound is 0 or the last
+    character) (process_ccode, parser.ml:1209-1260)."""
+    additive, active, weight = flags
+    verbs = {}
+    for tok in re.findall(r"/\s*\d*|[-+\[\]*]|\d*\.\d*|\d+", body):
+        if tok[0] == "/":
+            verbs["w"] = int(tok[1:].strip() or 1)
+        elif tok == "+":
+            verbs["add"] = True
+        elif tok == "-":
+            verbs["add"] = False
+        elif tok == "[":
+            verbs["act"] = True
+        elif tok == "]":
+            verbs["act"] = False
+        elif tok == "*":
+            verbs = {}
+        else:
+            a, dot, b = tok.partition(".")
+            lo = int(a) if a else 0
+            hi = (int(b) if b else n_chars - 1) if dot else lo
+            for c in range(lo, min(hi, n_chars - 1) + 1):
+                if "add" in verbs:
+                    additive[c] = verbs["add"]
+                if "act" in verbs:
+                    active[c] = verbs["act"]
+                if "w" in verbs:
+                    weight[c] = verbs["w"]
+
+
+def read_hennig(path: str) -> HennigMatrix:
+    """Reads the xread matrix, ccode ('cc') commands and tread trees of a
+    Hennig86 file; other commands (cn, proc, ...) are skipped.  In the
+    matrix, spaces and '.' between cells are ignored and '[...]' is a
+    polymorphic cell (read_data_xread, parser.ml:1365-1400).  Numeric taxon
+    references in trees become taxon names (parser.ml:3952-3966)."""
+    text = re.sub(r"'[^']*'", " ", open(path).read())  # titles and comments
+    names, rows, trees = [], [], []
+    flags = None
+    n_chars = 0
+    for m in re.finditer(r"[^;]*;", text, re.S):
+        cmd = m.group(0)[:-1]
+        cmd = re.sub(r"^[\s#$]+", "", cmd)
+        word = re.match(r"[A-Za-z]*", cmd).group(0).lower()
+        body = cmd[len(word):]
+        if word == "xread":
+            # the two counts come first
+            head = re.match(r"\s*(\d+)\s+(\d+)", body)
+            if not head:
+                raise ValueError("xread without character and taxon counts")
+            n_chars, n_taxa = int(head.group(1)), int(head.group(2))
+            rest = body[head.end():]
+            words = re.findall(r"\[[^\]]*\]|[^\s\[]+", rest)
+            i = 0
+            while i < len(words) and len(names) < n_taxa:
+                names.append(words[i])
+                i += 1
+                cells = []
+                while len(cells) < n_chars:
+                    if i >= len(words):
+                        raise ValueError("taxon %r has fewer than %d cells" % (names[-1], n_chars))
+                    w = words[i]
+                    i += 1
+                    if w.startswith("["):
+                        cells.append(_hennig_cell(w))
+                    else:
+                        cells.extend(_hennig_cell(ch) for ch in w if ch != ".")
+                if len(cells) != n_chars:
+                    raise ValueError("taxon %r has %d cells, not %d" % (names[-1], len(cells), n_chars))
+                rows.append(cells)
+            if len(names) != n_taxa:
+                raise ValueError("xread names %d taxa, not %d" % (len(names), n_taxa))
+            flags = (np.ones(n_chars, bool), np.ones(n_chars, bool), np.ones(n_chars, np.int64))
+        elif word in ("cc", "ccode") and flags is not None:
+            _hennig_ccode(body, flags, n_chars)
+        elif word == "tread":
+            for tree in body.split("*"):
+                if tree.strip():
+                    trees.append(re.sub(r"(?<![\w.])(\d+)(?![\w.])",
+                                        lambda d: names[int(d.group(1))]
+                                        if int(d.group(1)) < len(names) else d.group(1), tree))
+    if flags is None:
+        raise ValueError("no xread matrix in %s" % path)
+    additive, active, weight = flags
+    return HennigMatrix(names=names, cells=np.array(rows, np.uint32).reshape(len(names), n_chars),
+                        additive=additive, active=active, weight=weight, trees=trees)

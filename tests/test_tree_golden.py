@@ -140,3 +140,69 @@ def test_root_costs_equal_downpass_of_every_rooting():
     for (u, v), c in zip(rc.edges.tolist(), rc.costs.tolist()):
         T = _rooted_on(adj, t.n, u, v)
         assert search.downpass(T, OracleBackend(data, om)).total == c, (u, v)
+
+
+def _static_cost(h, tree_text):
+    """Whole-tree cost of a Hennig matrix's static characters on a fixed
+    tree: the oracle's Fitch medians (nonaddCSc.c:422-462) for the
+    non-additive characters plus, for the additive ones, the interval rule
+    of add_item (add.c:559-600) restated here as a test helper (additive
+    characters are not on the GPU path).  Both totals are root-invariant."""
+    F, _, w = h.fitch_matrix()
+    assert (w == 1).all()
+    lo, hi, _ = h.additive_intervals()
+    t = formats.parse_tree(tree_text, h.names)
+    total = 0
+    state = {}
+    for v in t.nodes()[::-1]:   # reversed preorder: children before parents
+        if v < t.n:
+            state[v] = (F[v], lo[v].astype(np.int64), hi[v].astype(np.int64))
+            continue
+        a, b = (state[int(k)] for k in t.kids[v])
+        c, med = O.nonadd_median(a[0], b[0])
+        lo_v, hi_v = np.maximum(a[1], b[1]), np.minimum(a[2], b[2])
+        gap = lo_v > hi_v
+        total += c + int((lo_v - hi_v)[gap].sum())
+        state[v] = (med, np.where(gap, hi_v, lo_v), np.where(gap, lo_v, hi_v))
+    return total
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
+                    reason="reference test files not present")
+def test_static_poly_cost():
+    """test/cost_tests' static_poly.poy: the Hennig matrix
+    test/polymorphic.ss (non-additive characters with polymorphic and
+    missing cells, two additive characters) on the tree its tread gives;
+    the expected cost is read from test/cost_tests."""
+    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
+    want = int(line.split("-cost")[1].split()[0])
+    h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
+    assert len(h.trees) == 1
+    assert _static_cost(h, h.trees[0]) == want
+
+
+def test_read_hennig(tmp_path):
+    p = tmp_path / "m.ss"
+    p.write_text("xread\n'title; with a semicolon'\n5 4\n"
+                 "a 0 1 2 [01] ?\nb 1 1 0 2 A\nc 0.0-0 V\nd 1 [1 2] 1 3 0\n;\n"
+                 "cc - 0.2;\ncc + 3 ] 4;\nccode /3 1.;\n"
+                 "cn {0 first x y ;\n"
+                 "tread (a (b (c d)))*(0 (3 (1 2)));\nproc/;\n")
+    h = formats.read_hennig(str(p))
+    assert h.names == ["a", "b", "c", "d"]
+    assert h.cells[:, 3].tolist() == [0b11, 0b100, 0b1, 0b1000]
+    assert h.cells[2].tolist() == [1, 1, 0, 1, 1 << 31]
+    assert h.cells[3, 1] == 0b110 and h.cells[1, 4] == 1 << 10
+    assert h.additive.tolist() == [False, False, False, True, True]
+    assert h.active.tolist() == [True, True, True, True, False]
+    assert h.weight.tolist() == [1, 3, 3, 3, 3]
+    assert h.trees[1].split() == ["(a", "(d", "(b", "c)))"]
+    F, cols, w = h.fitch_matrix()
+    assert cols.tolist() == [0, 1, 2] and w.tolist() == [1, 3, 3]
+    # character 2 observes states {0, 1, 2}: bit i is its i-th state
+    # (c is missing there, so it holds all three)
+    assert F[:, 2].tolist() == [0b100, 0b001, 0b111, 0b010]
+    assert F[:, 1].tolist() == [0b010, 0b010, 0b001, 0b110]
+    lo, hi, acols = h.additive_intervals()
+    assert acols.tolist() == [3] and lo[:, 0].tolist() == [0, 2, 0, 3]
+    assert hi[:, 0].tolist() == [1, 2, 0, 3]
