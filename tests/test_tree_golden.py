@@ -206,3 +206,42 @@ def test_read_hennig(tmp_path):
     lo, hi, acols = h.additive_intervals()
     assert acols.tolist() == [3] and lo[:, 0].tolist() == [0, 2, 0, 3]
     assert hi[:, 0].tolist() == [1, 2, 0, 3]
+
+
+def _sankoff_tree_cost(t, leaves, tcm):
+    """Root cost of a Sankoff downpass (the oracle's elt_median,
+    sankCS.ml:302-338) with leaf cost vectors leaves[v] [n_chars, k]."""
+    s = {}
+    for v in t.nodes()[::-1]:
+        if v < t.n:
+            s[v] = leaves[v]
+            continue
+        a, b = (s[int(k)] for k in t.kids[v])
+        s[v] = np.array([O.sank_elt_median(tcm, a[c], b[c])[0] for c in range(len(a))])
+    return int(s[t.root].min(axis=1).sum())
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
+                    reason="reference test files not present")
+def test_static_poly_cost_through_sankoff():
+    """Sankoff with a 0/1 matrix is Fitch, and with |i - j| costs it is the
+    additive rule: the Sankoff oracle on polymorphic.ss, non-additive
+    characters under the unit matrix and additive ones under the linear
+    matrix (a cell's leaf vector 0 on its states, infinite elsewhere), must
+    give the same whole-tree cost as the reference's static_poly test."""
+    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
+    want = int(line.split("-cost")[1].split()[0])
+    h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
+    t = formats.parse_tree(h.trees[0], h.names)
+    k = 8
+    F, _, _ = h.fitch_matrix()
+    lo, hi, _ = h.additive_intervals()
+    bit = (F[:, :, None] >> np.arange(k)) & 1
+    unit = np.where(bit == 1, 0, O.SANK_INF).astype(np.int64)
+    st = np.arange(k)
+    inside = (st >= lo[:, :, None]) & (st <= hi[:, :, None])
+    ordered = np.where(inside, 0, O.SANK_INF).astype(np.int64)
+    tcm_unit = 1 - np.eye(k, dtype=np.int64)
+    tcm_lin = np.abs(st[:, None] - st[None, :]).astype(np.int64)
+    got = (_sankoff_tree_cost(t, unit, tcm_unit) + _sankoff_tree_cost(t, ordered, tcm_lin))
+    assert got == want
