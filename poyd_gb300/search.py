@@ -190,6 +190,23 @@ class Tree:
 # ---------------------------------------------------------------------------
 # GPU backend
 # ---------------------------------------------------------------------------
+def either_empty(a, b, n_slots: int, empty) -> np.ndarray:
+    """Per pair whether node a_i or b_i is all gaps.  ``empty(v)`` answers
+    for an ascending array of distinct node ids and is asked once per node
+    the pairs name, found with a mark array over the n_slots node ids
+    rather than a sort of the 2n ids."""
+    a = np.asarray(a, np.int64)
+    b = np.asarray(b, np.int64)
+    seen = np.zeros(n_slots, bool)
+    seen[a] = True
+    seen[b] = True
+    u = np.flatnonzero(seen)
+    e = np.zeros(n_slots, bool)
+    if len(u):
+        e[u] = empty(u)
+    return e[a] | e[b]
+
+
 def _p(t):
     return C.c_void_p(t.data_ptr())
 
@@ -345,10 +362,9 @@ class GpuBackend:
         a = np.asarray(a, np.int64)
         b = np.asarray(b, np.int64)
         do, _ = align.cost_2(self._batch(a, b), self.cm, deltaw="dos")
+        e = either_empty(a, b, len(self.len), self._empty)
         do = do.to(torch.int64).cpu().numpy()
-        u, inv = np.unique(np.concatenate([a, b]), return_inverse=True)
-        e = self._empty(u)[inv]
-        do[e[:len(a)] | e[len(a):]] = 0
+        do[e] = 0
         return do
 
     def rebind_nodes(self, dst: np.ndarray, src: np.ndarray):
@@ -375,13 +391,9 @@ class GpuBackend:
         ib = torch.from_numpy(np.asarray(b, np.int32)).to(self.dev)
         do, cells = align.cost_2(self._batch(a, b), self.cm, deltaw="dos", band_cells=True)
         tot = do.to(torch.int64)
-        u, inv = np.unique(np.concatenate([np.asarray(a, np.int64), np.asarray(b, np.int64)]),
-                           return_inverse=True)
-        e = self._empty(u)
+        e = either_empty(a, b, len(self.len), self._empty)
         if e.any():
-            e = e[inv]
-            keep = ~(e[:n] | e[n:])
-            tot = tot * torch.from_numpy(keep.astype(np.int64)).to(self.dev)
+            tot = tot * torch.from_numpy((~e).astype(np.int64)).to(self.dev)
         if self.nf:
             fd = torch.empty(n, dtype=torch.int64, device=self.dev)
             native.check(L.poyd_nonadd8_distance_batch(_p(self.fitch), C.c_int64(self.stride), self.nf,
@@ -694,24 +706,19 @@ def tbr_candidates(t: Tree, be, diag: Diagnosis | None = None):
         do, fi = be.medians(r[:, 0], r[:, 1], r[:, 2])
         for i, (_, _, rid, s, w, below) in enumerate(roots):
             cand.append((s, w, rid, below + int(do[i]) + int(fi[i]) - int(tot[s])))
-    # join edges: outside the clade, not its parent, not (own rooting) its sibling
+    # join edges: outside the clade, not its parent, not (own rooting) its
+    # sibling; one (candidate x node) mask, rows in candidate order
     tin, tout = euler(t)
-    S, U, R, E, D = [], [], [], [], []
-    for s, u, rid, dc in cand:
-        p = par[s]
-        sib = t.kids[p][0] if t.kids[p][1] == s else t.kids[p][1]
-        inside = (tin[nodes] >= tin[s]) & (tin[nodes] < tout[s])
-        keep = ~inside & (nodes != p)
-        if u < 0:
-            keep &= nodes != sib
-        e = nodes[keep]
-        S.append(np.full(len(e), s, np.int64))
-        U.append(np.full(len(e), u, np.int64))
-        R.append(np.full(len(e), rid, np.int64))
-        D.append(np.full(len(e), dc, np.int64))
-        E.append(e)
-    cat = lambda x: np.concatenate(x) if x else np.zeros(0, np.int64)
-    S, U, R, E, D = cat(S), cat(U), cat(R), cat(E), cat(D)
+    cs, cu, cr, cd = (np.array([c[i] for c in cand], np.int64).reshape(-1) for i in range(4))
+    p = par[cs]
+    sib = np.where(t.kids[p, 0] == cs, t.kids[p, 1], t.kids[p, 0])
+    tn = tin[nodes][None, :]
+    keep = ~((tn >= tin[cs][:, None]) & (tn < tout[cs][:, None]))
+    keep &= nodes[None, :] != p[:, None]
+    keep &= ~((cu < 0)[:, None] & (nodes[None, :] == sib[:, None]))
+    cnt = keep.sum(axis=1)
+    S, U, R, D = (np.repeat(x, cnt) for x in (cs, cu, cr, cd))
+    E = np.broadcast_to(nodes, keep.shape)[keep]
     score = be.distances(R, E) if len(S) else np.zeros(0, np.int64)
     be.release_nodes(2 * n)
     return S, U, E, score, D

@@ -133,3 +133,27 @@ def test_tbr_candidate_enumeration():
                 want.add((s, u, e))
     got = set(zip(S.tolist(), U.tolist(), E.tolist()))
     assert len(got) == len(S) and got == want
+
+
+def test_either_empty_matches_a_sort():
+    """The GPU backend's all-gap test per pair asks once per distinct node
+    and agrees with the sort-based formulation."""
+    rng = np.random.default_rng(3)
+    empty_nodes = set(rng.choice(300, 40, replace=False).tolist())
+    asked = []
+
+    def empty(v):
+        asked.append(v.copy())
+        return np.array([int(x) in empty_nodes for x in v], bool)
+    for n in (0, 1, 17, 5000):
+        a = rng.integers(0, 300, n)
+        b = rng.integers(0, 300, n)
+        asked.clear()
+        got = search.either_empty(a, b, 300, empty)
+        u, inv = np.unique(np.concatenate([a, b]).astype(np.int64), return_inverse=True)
+        e = np.array([int(x) in empty_nodes for x in u], bool)[inv]
+        assert np.array_equal(got, e[:n] | e[n:])
+        if n:
+            assert len(asked) == 1 and np.array_equal(asked[0], u)
+        else:
+            assert not asked
