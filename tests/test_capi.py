@@ -71,3 +71,63 @@ def test_errors_are_reported_without_a_gpu(lib):
                                None, None)
     assert rc == -5
     assert b"alphabet" in lib.poyd_last_error()
+
+
+def _dna(lib, gap_open=-1):
+    m = native.PoydCM()
+    assert lib.poyd_cm_dna(C.byref(m), 1, 2, gap_open) == 0
+    return m
+
+
+def test_argument_checks_without_a_gpu(lib):
+    """Checks that return before any CUDA call, with the reference's
+    failure cases (failwith in the OCaml stubs) as negative codes."""
+    L = C.CDLL(native.LIB_PATH)   # own handle: argtypes set here stay local
+    vp, i32 = C.c_void_p, C.c_int32
+    cmp = C.POINTER(native.PoydCM)
+    L.poyd_algn_simple_2.argtypes = [vp, i32, vp, i32, cmp, vp, i32, vp]
+    L.poyd_algn_cost_affine_3.argtypes = [vp, i32, vp, i32, cmp, vp]
+    L.poyd_last_error.restype = C.c_char_p
+    lin, aff = _dna(lib), _dna(lib, 3)
+    s = np.array([16, 1, 2, 4], np.uint8)
+    p = s.ctypes.data
+    cost = C.c_int32()
+    L.poyd_matrix_create.restype = vp
+    L.poyd_matrix_free.argtypes = [vp]
+    mat = L.poyd_matrix_create()  # host allocation only
+    EINVAL, ERANGE, EUNSUP = -1, -3, -5
+    # simple_2 wants len(s1) >= len(s2) >= 1, the linear model and a matrix
+    assert L.poyd_algn_simple_2(p, 2, p, 3, C.byref(lin), mat, 0, C.byref(cost)) == EINVAL
+    assert L.poyd_algn_simple_2(p, 3, p, 0, C.byref(lin), mat, 0, C.byref(cost)) == EINVAL
+    assert L.poyd_algn_simple_2(p, 4, p, 4, C.byref(aff), mat, 0, C.byref(cost)) == EINVAL
+    assert L.poyd_algn_simple_2(p, 4, p, 4, C.byref(lin), None, 0, C.byref(cost)) == EINVAL
+    assert b"null argument" in L.poyd_last_error()
+    # the affine entry points want an affine matrix
+    assert L.poyd_algn_cost_affine_3(p, 4, p, 4, C.byref(lin), C.byref(cost)) == EINVAL
+    assert b"affine" in L.poyd_last_error()
+    # matrices the GPU path does not implement, or costs out of range
+    bad = _dna(lib)
+    bad.tail[1] += 1
+    assert L.poyd_algn_cost_affine_3(p, 4, p, 4, C.byref(bad), C.byref(cost)) == EUNSUP
+    bad = _dna(lib)
+    bad.cost[(1 << 5) | 2] = -1
+    assert L.poyd_algn_simple_2(p, 4, p, 4, C.byref(bad), mat, 0, C.byref(cost)) == ERANGE
+    bad = _dna(lib)
+    bad.cost[(1 << 5) | 2] = 1 << 16
+    assert L.poyd_algn_simple_2(p, 4, p, 4, C.byref(bad), mat, 0, C.byref(cost)) == ERANGE
+    L.poyd_matrix_free(mat)
+    bad = _dna(lib, 3)
+    bad.gap_open = 1 << 16
+    assert L.poyd_algn_cost_affine_3(p, 4, p, 4, C.byref(bad), C.byref(cost)) == ERANGE
+    # host-buffer batch: a null matrix, a negative count or a null buffer
+    assert lib.poyd_align_2_host(None, 1, p, None, None, None, None, None, None, 0, None, None,
+                                 0) == EINVAL
+    assert lib.poyd_align_2_host(C.byref(lin), -1, p, None, None, None, None, None, None, 0,
+                                 None, None, 0) == EINVAL
+    assert lib.poyd_align_2_host(C.byref(lin), 1, None, None, None, None, None, None, None, 0,
+                                 None, None, 0) == EINVAL
+    assert lib.poyd_align_2_host(C.byref(lin), 0, None, None, None, None, None, None, None, 0,
+                                 None, None, 0) == 0   # an empty batch is a no-op
+    # single-pair column operations: null outputs
+    assert lib.poyd_algn_median_2_with_gaps(p, p, 4, C.byref(lin), None, None) == EINVAL
+    assert lib.poyd_algn_worst_2(p, p, 4, C.byref(lin), None) == EINVAL
