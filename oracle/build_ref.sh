@@ -12,6 +12,11 @@ OUT="$HERE/_ref"
 [ -f "$REF/algn.c" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
 mkdir -p "$OUT"
 CF="-O2 -fPIC -w -I$HERE -I$REF"
+LIB=libporef.so
+# POYD_REF_C_PATH=1 (x86-64 only): leave __MMX__ undefined so that algn.c
+# compiles its plain-C cell path (algn.c:375-453), the one an arm64 build
+# uses, instead of the inline-asm one; written to libporef_cpath.so.
+if [ "${POYD_REF_C_PATH:-0}" = 1 ]; then CF="$CF -mno-mmx"; LIB=libporef_cpath.so; fi
 gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/algn.c" -o "$OUT/algn.o"
 gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/avl.c" -o "$OUT/avl.o"
 gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/zarr.c" -o "$OUT/zarr.o"
@@ -19,6 +24,6 @@ gcc -std=gnu89 -fgnu89-inline $CF -c "$REF/zarr.c" -o "$OUT/zarr.o"
 sed -e 's/nonadd_/nonadd8_/g' -e 's/NONADDSIZE/8/g' "$REF/nonaddCSc.c" | \
     gcc -std=gnu89 -fgnu89-inline $CF -DCHARSIZE=8 -x c - -c -o "$OUT/nonadd8.o"
 gcc -std=gnu99 $CF -c "$HERE/ref_driver.c" -o "$OUT/ref_driver.o"
-gcc -shared -o "$OUT/libporef.so" "$OUT/algn.o" "$OUT/avl.o" "$OUT/zarr.o" \
+gcc -shared -o "$OUT/$LIB" "$OUT/algn.o" "$OUT/avl.o" "$OUT/zarr.o" \
     "$OUT/nonadd8.o" "$OUT/ref_driver.o" -lm
-echo "$OUT/libporef.so"
+echo "$OUT/$LIB"

@@ -3,6 +3,8 @@ source (oracle/build_ref.sh) on seeded random inputs.  Skipped where the
 reference sources are absent (the compiled reference does not travel)."""
 import ctypes as C
 import os
+import platform
+import subprocess
 
 import numpy as np
 import pytest
@@ -185,3 +187,34 @@ def test_fitch_median_3_vs_reference(R):
         f = np.zeros(n, np.uint8)
         R.ref_nonadd8_median_3(P(A), P(N), P(D1), P(D2), n, P(f))
         assert np.array_equal(O.nonadd_median_3(A, N, D1, D2), f)
+
+
+@pytest.mark.skipif(platform.machine() != "x86_64",
+                    reason="the asm/C switch of algn.c exists on x86-64 only")
+def test_reference_c_cell_path_vs_oracle():
+    """algn.c has an inline-asm cell path (x86-64 with MMX) and a plain-C
+    one (algn.c:375-453, the one an arm64 build compiles).  The C path,
+    built with POYD_REF_C_PATH=1, agrees with the oracle as the asm path
+    does."""
+    env = dict(os.environ, POYD_REF_C_PATH="1")
+    subprocess.check_call(["sh", os.path.join(os.path.dirname(O.REF_PATH), "..", "build_ref.sh"),
+                           REF_SRC], stdout=subprocess.DEVNULL, env=env)
+    Rc = C.CDLL(os.path.join(os.path.dirname(O.REF_PATH), "libporef_cpath.so"))
+    Rc.ref_cm_new.argtypes = [C.POINTER(O.OrCM)]
+    Rc.ref_cm_new.restype = C.c_void_p
+    Rc.ref_cm_free.argtypes = [C.c_void_p]
+    Rc.ref_align_2.argtypes = [O.u8p, C.c_int, O.u8p, C.c_int, C.c_void_p, C.c_int, O.u8p,
+                               O.u8p, C.POINTER(C.c_int)]
+    for model in [(1, 2), (3, 1)]:
+        m = O.cm_dna(model[0], model[1], -1)
+        rc = Rc.ref_cm_new(C.byref(m))
+        for a, b in zip(*_pairs(90 + model[0], 30, 1200)):
+            cap = len(a) + len(b) + 2
+            o1, o2 = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+            n = C.c_int()
+            c_ref = Rc.ref_align_2(P(a), len(a), P(b), len(b), rc, O.deltaw(a, b, m), P(o1), P(o2),
+                                   C.byref(n))
+            c, ra, rb = O.align_2(a, b, m)
+            assert c == c_ref
+            assert np.array_equal(ra, o1[:n.value]) and np.array_equal(rb, o2[:n.value])
+        Rc.ref_cm_free(rc)
