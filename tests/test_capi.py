@@ -131,3 +131,9 @@ def test_argument_checks_without_a_gpu(lib):
     # single-pair column operations: null outputs
     assert lib.poyd_algn_median_2_with_gaps(p, p, 4, C.byref(lin), None, None) == EINVAL
     assert lib.poyd_algn_worst_2(p, p, 4, C.byref(lin), None) == EINVAL
+
+
+def test_integration_guide_lists_every_entry_point():
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [s for s in declared_symbols() if s not in doc]
+    assert not missing, missing
