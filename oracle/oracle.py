@@ -108,6 +108,12 @@ def lib():
         L.or_nonadd_median_3.argtypes = [u8p, u8p, u8p, u8p, C.c_int, u8p]
         L.or_nonadd_dist_2.argtypes = [u8p, u8p, u8p, C.c_int]
         L.or_nonadd_dist_2.restype = C.c_int64
+        for w in (16, 32):
+            getattr(L, "or_nonadd%d_median" % w).argtypes = [C.c_void_p] * 2 + [C.c_int, C.c_void_p]
+            getattr(L, "or_nonadd%d_median" % w).restype = C.c_int64
+            getattr(L, "or_nonadd%d_distance" % w).argtypes = [C.c_void_p] * 2 + [C.c_int]
+            getattr(L, "or_nonadd%d_distance" % w).restype = C.c_int64
+            getattr(L, "or_nonadd%d_median_3" % w).argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
         L.or_sank_elt_median.argtypes = [C.c_int, i64p, i64p, i64p, i64p, i64p, i64p]
         L.or_sank_elt_distance.argtypes = [C.c_int, i64p, i64p, i64p]
         L.or_sank_elt_distance.restype = C.c_double
@@ -139,6 +145,12 @@ def ref():
         R.ref_nonadd8_distance.argtypes = [u8p, u8p, C.c_int]
         R.ref_nonadd8_distance.restype = C.c_long
         R.ref_nonadd8_median_3.argtypes = [u8p, u8p, u8p, u8p, C.c_int, u8p]
+        for w in (16, 32):
+            getattr(R, "ref_nonadd%d_median" % w).argtypes = [C.c_void_p] * 2 + [C.c_int, C.c_void_p]
+            getattr(R, "ref_nonadd%d_median" % w).restype = C.c_long
+            getattr(R, "ref_nonadd%d_distance" % w).argtypes = [C.c_void_p] * 2 + [C.c_int]
+            getattr(R, "ref_nonadd%d_distance" % w).restype = C.c_long
+            getattr(R, "ref_nonadd%d_median_3" % w).argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
         _ref = R
     return _ref
 
@@ -299,6 +311,42 @@ def nonadd_median_3(A, N, D1, D2):
 
 
 SANK_INF = ((1 << 62) - 1) // 4
+
+
+_WIDE = {8: np.uint8, 16: np.uint16, 32: np.uint32}
+
+
+def _wide(x, width):
+    return np.ascontiguousarray(x, dtype=_WIDE[width])
+
+
+def nonadd_median_w(a, b, width: int):
+    """Fitch median of width-bit state sets (NonaddCS8/16/32): (added
+    cost, median)."""
+    if width == 8:
+        return nonadd_median(a, b)
+    a, b = _wide(a, width), _wide(b, width)
+    res = np.zeros_like(a)
+    c = getattr(lib(), "or_nonadd%d_median" % width)(a.ctypes.data, b.ctypes.data, len(a),
+                                                     res.ctypes.data)
+    return int(c), res
+
+
+def nonadd_distance_w(a, b, width: int) -> int:
+    if width == 8:
+        return nonadd_distance(a, b)
+    a, b = _wide(a, width), _wide(b, width)
+    return int(getattr(lib(), "or_nonadd%d_distance" % width)(a.ctypes.data, b.ctypes.data, len(a)))
+
+
+def nonadd_median_3_w(A, N, D1, D2, width: int):
+    if width == 8:
+        return nonadd_median_3(A, N, D1, D2)
+    A, N, D1, D2 = (_wide(x, width) for x in (A, N, D1, D2))
+    F = np.zeros_like(A)
+    getattr(lib(), "or_nonadd%d_median_3" % width)(A.ctypes.data, N.ctypes.data, D1.ctypes.data,
+                                                   D2.ctypes.data, len(A), F.ctypes.data)
+    return F
 
 
 def sank_elt_median(tcm, a_s, b_s):

@@ -875,6 +875,48 @@ int64_t or_nonadd_dist_2(const uint8_t *a, const uint8_t *b, const uint8_t *c, i
     return d;
 }
 
+/* NonaddCS16 / NonaddCS32: the same three rules on 16- and 32-bit state
+ * sets (nonaddCSc.c built with CHARSIZE 16 / 32 under the nonadd16_ /
+ * nonadd32_ names, myocamlbuild.ml.in:262-289).  Arrays hold len elements
+ * of the width in host byte order. */
+#define OR_NONADD_WIDE(W, T)                                                     \
+int64_t or_nonadd##W##_median(const T *a, const T *b, int len, T *res) {          \
+    int64_t cost = 0;                                                            \
+    int i;                                                                       \
+    for (i = 0; i < len; i++) {                                                  \
+        T in = (T)(a[i] & b[i]);                                                 \
+        if (!in) { cost++; res[i] = (T)(a[i] | b[i]); }                          \
+        else res[i] = in;                                                        \
+    }                                                                            \
+    return cost;                                                                 \
+}                                                                                \
+int64_t or_nonadd##W##_distance(const T *a, const T *b, int len) {                \
+    int64_t cost = 0;                                                            \
+    int i;                                                                       \
+    for (i = 0; i < len; i++) if (!(a[i] & b[i])) cost++;                        \
+    return cost;                                                                 \
+}                                                                                \
+void or_nonadd##W##_median_3(const T *A, const T *N, const T *D1, const T *D2,    \
+                             int len, T *F) {                                    \
+    int i;                                                                       \
+    for (i = 0; i < len; i++) {                                                  \
+        T a = A[i], n = N[i], d1 = D1[i], d2 = D2[i];                            \
+        T inter = (T)(n | (a & (d1 | d2)));                                      \
+        T temp = inter;                                                          \
+        T was_union = (T)((d1 & d2) == 0 ? ~(T)0 : 0);                           \
+        T contained, f;                                                          \
+        inter = (T)((inter | a) & was_union);                                    \
+        temp |= inter;                                                           \
+        contained = (T)(((a & n) == a) ? ~(T)0 : 0);                             \
+        f = (T)(contained & a);                                                  \
+        contained = (T)(contained == 0 ? ~(T)0 : 0);                             \
+        temp &= contained;                                                       \
+        F[i] = (T)(f | temp);                                                    \
+    }                                                                            \
+}
+OR_NONADD_WIDE(16, uint16_t)
+OR_NONADD_WIDE(32, uint32_t)
+
 /* ------------------------------------------------------------------------ */
 /* Sankoff (sankCS.ml)                                                       */
 /* ------------------------------------------------------------------------ */

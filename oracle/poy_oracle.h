@@ -158,6 +158,14 @@ int64_t or_nonadd_distance(const uint8_t *a, const uint8_t *b, int len);
 void or_nonadd_median_3(const uint8_t *A, const uint8_t *N, const uint8_t *D1,
                         const uint8_t *D2, int len, uint8_t *F);
 int64_t or_nonadd_dist_2(const uint8_t *a, const uint8_t *b, const uint8_t *c, int len);
+int64_t or_nonadd16_median(const uint16_t *a, const uint16_t *b, int len, uint16_t *res);
+int64_t or_nonadd16_distance(const uint16_t *a, const uint16_t *b, int len);
+void or_nonadd16_median_3(const uint16_t *A, const uint16_t *N, const uint16_t *D1,
+                          const uint16_t *D2, int len, uint16_t *F);
+int64_t or_nonadd32_median(const uint32_t *a, const uint32_t *b, int len, uint32_t *res);
+int64_t or_nonadd32_distance(const uint32_t *a, const uint32_t *b, int len);
+void or_nonadd32_median_3(const uint32_t *A, const uint32_t *N, const uint32_t *D1,
+                          const uint32_t *D2, int len, uint32_t *F);
 
 /* ---- Sankoff characters (sankCS.ml) ---- */
 #define OR_SANK_INF ((int64_t)(((uint64_t)1 << 62) - 1) / 4) /* max_int/4, 63-bit */

@@ -33,6 +33,12 @@ value algn_CAML_verify_2(value s1, value s2, value c);
 value char_nonadd8_CAML_basic_median(value v, value a, value b);
 value char_nonadd8_CAML_distance(value a, value b);
 value char_nonadd8_CAML_median_3(value v, value vA, value vN, value vD1, value vD2);
+value char_nonadd16_CAML_basic_median(value v, value a, value b);
+value char_nonadd16_CAML_distance(value a, value b);
+value char_nonadd16_CAML_median_3(value v, value vA, value vN, value vD1, value vD2);
+value char_nonadd32_CAML_basic_median(value v, value a, value b);
+value char_nonadd32_CAML_distance(value a, value b);
+value char_nonadd32_CAML_median_3(value v, value vA, value vN, value vD1, value vD2);
 
 /* ---- runtime stand-ins declared by the stub headers ---- */
 value oracle_alloc_custom(struct custom_operations *ops, uintptr_t size, uintptr_t mem, uintptr_t max) {
@@ -201,14 +207,16 @@ int ref_verify_2(const uint8_t *s1, const uint8_t *s2, int len, void *cm) {
 /* ---- Fitch (8-bit), struct _naca_t layout (nonaddCSc.c:293-300) ---- */
 struct ref_naca { long len, heur, code, added_cost; void *data; };
 
-static value make_naca(const uint8_t *d, int len) {
-    size_t sz = sizeof(struct ref_naca) + (size_t)len + 64;
+/* len elements of eb bytes each */
+static value make_naca_w(const void *d, int len, int eb) {
+    size_t sz = sizeof(struct ref_naca) + (size_t)len * eb + 64;
     struct ref_naca *n = (struct ref_naca *)calloc(1, sz);
     n->len = len;
     n->data = (void *)(n + 1);
-    if (d) memcpy(n + 1, d, (size_t)len);
+    if (d) memcpy(n + 1, d, (size_t)len * eb);
     return (value)n;
 }
+static value make_naca(const uint8_t *d, int len) { return make_naca_w(d, len, 1); }
 
 long ref_nonadd8_median(const uint8_t *a, const uint8_t *b, int len, uint8_t *res) {
     value va = make_naca(a, len), vb = make_naca(b, len), vr = make_naca(NULL, len);
@@ -235,3 +243,34 @@ void ref_nonadd8_median_3(const uint8_t *A, const uint8_t *N, const uint8_t *D1,
     memcpy(F, (struct ref_naca *)vf + 1, (size_t)len);
     free((void *)va); free((void *)vn); free((void *)v1); free((void *)v2); free((void *)vf);
 }
+
+/* ---- Fitch on 16- and 32-bit state sets (nonaddCSc.c with CHARSIZE 16 / 32) ---- */
+#define REF_NONADD_WIDE(W, EB)                                                        \
+long ref_nonadd##W##_median(const void *a, const void *b, int len, void *res) {       \
+    value va = make_naca_w(a, len, EB), vb = make_naca_w(b, len, EB),                 \
+          vr = make_naca_w(NULL, len, EB);                                            \
+    long c;                                                                           \
+    char_nonadd##W##_CAML_basic_median(vr, va, vb);                                   \
+    memcpy(res, (struct ref_naca *)vr + 1, (size_t)len * EB);                         \
+    c = ((struct ref_naca *)vr)->added_cost;                                          \
+    free((void *)va); free((void *)vb); free((void *)vr);                             \
+    return c;                                                                         \
+}                                                                                     \
+long ref_nonadd##W##_distance(const void *a, const void *b, int len) {                \
+    value va = make_naca_w(a, len, EB), vb = make_naca_w(b, len, EB);                 \
+    long c = Long_val(char_nonadd##W##_CAML_distance(va, vb));                        \
+    free((void *)va); free((void *)vb);                                               \
+    return c;                                                                         \
+}                                                                                     \
+void ref_nonadd##W##_median_3(const void *A, const void *N, const void *D1,           \
+                              const void *D2, int len, void *F) {                     \
+    value va = make_naca_w(A, len, EB), vn = make_naca_w(N, len, EB),                 \
+          v1 = make_naca_w(D1, len, EB), v2 = make_naca_w(D2, len, EB),               \
+          vf = make_naca_w(NULL, len, EB);                                            \
+    char_nonadd##W##_CAML_median_3(vf, va, vn, v1, v2);                               \
+    memcpy(F, (struct ref_naca *)vf + 1, (size_t)len * EB);                           \
+    free((void *)va); free((void *)vn); free((void *)v1); free((void *)v2);           \
+    free((void *)vf);                                                                 \
+}
+REF_NONADD_WIDE(16, 2)
+REF_NONADD_WIDE(32, 4)

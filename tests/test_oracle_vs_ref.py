@@ -218,3 +218,35 @@ def test_reference_c_cell_path_vs_oracle():
             assert c == c_ref
             assert np.array_equal(ra, o1[:n.value]) and np.array_equal(rb, o2[:n.value])
         Rc.ref_cm_free(rc)
+
+
+def _sparse_sets(rng, n, width):
+    """n non-empty state sets of 1-3 states out of `width`, so that about
+    half of the pairs do not intersect."""
+    out = np.zeros(n, np.uint64)
+    for _ in range(3):
+        bit = rng.integers(0, width, n).astype(np.uint64)
+        keep = rng.random(n) < 0.6
+        out |= np.where(keep, np.uint64(1) << bit, np.uint64(0))
+    out[out == 0] = np.uint64(1) << rng.integers(0, width, int((out == 0).sum())).astype(np.uint64)
+    return out.astype({16: np.uint16, 32: np.uint32}[width])
+
+
+@pytest.mark.parametrize("width", [16, 32])
+def test_wide_fitch_vs_reference(R, width):
+    """NonaddCS16 / NonaddCS32 (nonaddCSc.c at CHARSIZE 16 / 32): median,
+    distance and median_3 of the oracle against the reference."""
+    rng = np.random.default_rng(width)
+    med = getattr(R, "ref_nonadd%d_median" % width)
+    dist = getattr(R, "ref_nonadd%d_distance" % width)
+    med3 = getattr(R, "ref_nonadd%d_median_3" % width)
+    for n in (1, 7, 8, 9, 31, 200, 1999):
+        a, b, c, d = (_sparse_sets(rng, n, width) for _ in range(4))
+        r = np.zeros_like(a)
+        c_ref = med(a.ctypes.data, b.ctypes.data, n, r.ctypes.data)
+        c_or, r_or = O.nonadd_median_w(a, b, width)
+        assert c_ref == c_or and np.array_equal(r, r_or), n
+        assert dist(a.ctypes.data, b.ctypes.data, n) == O.nonadd_distance_w(a, b, width)
+        f = np.zeros_like(a)
+        med3(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, f.ctypes.data)
+        assert np.array_equal(f, O.nonadd_median_3_w(a, b, c, d, width)), n
