@@ -245,3 +245,40 @@ def test_static_poly_cost_through_sankoff():
     tcm_lin = np.abs(st[:, None] - st[None, :]).astype(np.int64)
     got = (_sankoff_tree_cost(t, unit, tcm_unit) + _sankoff_tree_cost(t, ordered, tcm_lin))
     assert got == want
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
+                    reason="reference test files not present")
+def test_static_poly_fitch_through_the_search_module():
+    """The search module's own accounting (downpass, best rooting, reported
+    cost) over polymorphic.ss's non-additive characters, with an empty DO
+    character beside them, gives the static_poly cost less its additive
+    part."""
+    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
+    want = int(line.split("-cost")[1].split()[0])
+    h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
+    t = formats.parse_tree(h.trees[0], h.names)
+    F, _, _ = h.fitch_matrix()
+    n = len(h.names)
+    data = simulate.Dataset(names=h.names, seqs=[np.array([16], np.uint8)] * n, fitch=F,
+                            fitch_states=np.array([len(h.observed(c)) for c in
+                                                   np.flatnonzero(~h.additive)], np.int64),
+                            sank=np.zeros((n, 0, 4), np.int32), sank_tcm=np.zeros((4, 4), np.int32))
+    additive = _static_cost(h, h.trees[0]) - _static_cost_fitch_only(h, h.trees[0])
+    be = OracleBackend(data, O.cm_dna(1, 2, -1))
+    assert search.downpass(t, be).total == want - additive
+    assert search.root_costs(t, be).best()[0] == want - additive
+    assert search.final_cost(t, be).cost == want - additive
+
+
+def _static_cost_fitch_only(h, tree_text):
+    F, _, _ = h.fitch_matrix()
+    t = formats.parse_tree(tree_text, h.names)
+    total, state = 0, {}
+    for v in t.nodes()[::-1]:
+        if v < t.n:
+            state[v] = F[v]
+            continue
+        c, state[v] = O.nonadd_median(*(state[int(k)] for k in t.kids[v]))
+        total += c
+    return total
