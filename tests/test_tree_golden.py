@@ -282,3 +282,23 @@ def _static_cost_fitch_only(h, tree_text):
         c, state[v] = O.nonadd_median(*(state[int(k)] for k in t.kids[v]))
         total += c
     return total
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
+                    reason="reference test files not present")
+def test_static_poly_sankoff_through_the_search_module():
+    """The same characters as Sankoff characters under a 0/1 matrix (which
+    makes Sankoff equal Fitch) through the search module: the same cost."""
+    h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
+    t = formats.parse_tree(h.trees[0], h.names)
+    F, _, _ = h.fitch_matrix()
+    n, k = len(h.names), 8
+    bit = (F[:, :, None] >> np.arange(k)) & 1
+    sank = np.where(bit == 1, 0, simulate.SANK_INF).astype(np.int32)
+    data = simulate.Dataset(names=h.names, seqs=[np.array([16], np.uint8)] * n,
+                            fitch=np.zeros((n, 0), np.uint8), fitch_states=np.zeros(0, np.int64),
+                            sank=sank, sank_tcm=(1 - np.eye(k)).astype(np.int32))
+    be = OracleBackend(data, O.cm_dna(1, 2, -1))
+    want = _static_cost_fitch_only(h, h.trees[0])
+    assert search.downpass(t, be).total == want
+    assert search.final_cost(t, be).cost == want
