@@ -145,6 +145,8 @@ def ref():
         R.ref_nonadd8_distance.argtypes = [u8p, u8p, C.c_int]
         R.ref_nonadd8_distance.restype = C.c_long
         R.ref_nonadd8_median_3.argtypes = [u8p, u8p, u8p, u8p, C.c_int, u8p]
+        R.ref_nonadd8_dist_2.argtypes = [u8p, u8p, u8p, C.c_int]
+        R.ref_nonadd8_dist_2.restype = C.c_long
         for w in (16, 32):
             getattr(R, "ref_nonadd%d_median" % w).argtypes = [C.c_void_p] * 2 + [C.c_int, C.c_void_p]
             getattr(R, "ref_nonadd%d_median" % w).restype = C.c_long
@@ -301,6 +303,12 @@ def nonadd_median(a, b):
 def nonadd_distance(a, b):
     a, b = _u8(a), _u8(b)
     return lib().or_nonadd_distance(_ptr(a), _ptr(b), len(a))
+
+
+def nonadd_dist_2(a, b, c) -> int:
+    """char_nonadd_CAML_dist_2: characters where a meets neither b nor c."""
+    a, b, c = _u8(a), _u8(b), _u8(c)
+    return int(lib().or_nonadd_dist_2(_ptr(a), _ptr(b), _ptr(c), len(a)))
 
 
 def nonadd_median_3(A, N, D1, D2):

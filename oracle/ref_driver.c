@@ -33,6 +33,7 @@ value algn_CAML_verify_2(value s1, value s2, value c);
 value char_nonadd8_CAML_basic_median(value v, value a, value b);
 value char_nonadd8_CAML_distance(value a, value b);
 value char_nonadd8_CAML_median_3(value v, value vA, value vN, value vD1, value vD2);
+value char_nonadd8_CAML_dist_2(value va, value vb, value vc);
 value char_nonadd16_CAML_basic_median(value v, value a, value b);
 value char_nonadd16_CAML_distance(value a, value b);
 value char_nonadd16_CAML_median_3(value v, value vA, value vN, value vD1, value vD2);
@@ -242,6 +243,13 @@ void ref_nonadd8_median_3(const uint8_t *A, const uint8_t *N, const uint8_t *D1,
     char_nonadd8_CAML_median_3(vf, va, vn, v1, v2);
     memcpy(F, (struct ref_naca *)vf + 1, (size_t)len);
     free((void *)va); free((void *)vn); free((void *)v1); free((void *)v2); free((void *)vf);
+}
+
+long ref_nonadd8_dist_2(const uint8_t *a, const uint8_t *b, const uint8_t *c, int len) {
+    value va = make_naca(a, len), vb = make_naca(b, len), vc = make_naca(c, len);
+    long d = Long_val(char_nonadd8_CAML_dist_2(va, vb, vc));
+    free((void *)va); free((void *)vb); free((void *)vc);
+    return d;
 }
 
 /* ---- Fitch on 16- and 32-bit state sets (nonaddCSc.c with CHARSIZE 16 / 32) ---- */

@@ -229,7 +229,7 @@ def _sparse_sets(rng, n, width):
         keep = rng.random(n) < 0.6
         out |= np.where(keep, np.uint64(1) << bit, np.uint64(0))
     out[out == 0] = np.uint64(1) << rng.integers(0, width, int((out == 0).sum())).astype(np.uint64)
-    return out.astype({16: np.uint16, 32: np.uint32}[width])
+    return out.astype({8: np.uint8, 16: np.uint16, 32: np.uint32}[width])
 
 
 @pytest.mark.parametrize("width", [16, 32])
@@ -250,3 +250,11 @@ def test_wide_fitch_vs_reference(R, width):
         f = np.zeros_like(a)
         med3(a.ctypes.data, b.ctypes.data, c.ctypes.data, d.ctypes.data, n, f.ctypes.data)
         assert np.array_equal(f, O.nonadd_median_3_w(a, b, c, d, width)), n
+
+
+def test_fitch_dist_2_vs_reference(R):
+    """char_nonadd8_CAML_dist_2 (nonaddCSc.c:1349-1376)."""
+    rng = np.random.default_rng(13)
+    for n in (1, 15, 16, 17, 500, 3001):
+        a, b, c = (_sparse_sets(rng, n, 8) for _ in range(3))
+        assert R.ref_nonadd8_dist_2(P(a), P(b), P(c), n) == O.nonadd_dist_2(a, b, c)
