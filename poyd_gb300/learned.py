@@ -119,7 +119,7 @@ def features(t: search.Tree, be, S: np.ndarray, E: np.ndarray, cur: dict) -> tor
 def current_attachment(t: search.Tree, be, S: np.ndarray) -> np.ndarray:
     """Exact distance of every pruned subtree to its current sibling, indexed by node id."""
     cur = np.zeros(len(t.parent), np.int64)
-    subs = np.unique(S)
+    subs = search.distinct_nodes(S, len(t.parent))
     if len(subs):
         _, _, _, sib = node_info(t, be)
         cur[subs] = be.distances(subs, sib[subs])

@@ -190,6 +190,15 @@ class Tree:
 # ---------------------------------------------------------------------------
 # GPU backend
 # ---------------------------------------------------------------------------
+def distinct_nodes(ids, n_slots: int) -> np.ndarray:
+    """The distinct node ids among `ids`, ascending (what np.unique gives),
+    from a mark array over the n_slots node ids instead of a sort: the
+    candidate lists of a pass name each node many times."""
+    seen = np.zeros(n_slots, bool)
+    seen[np.asarray(ids, np.int64)] = True
+    return np.flatnonzero(seen)
+
+
 def either_empty(a, b, n_slots: int, empty) -> np.ndarray:
     """Per pair whether node a_i or b_i is all gaps.  ``empty(v)`` answers
     for an ascending array of distinct node ids and is asked once per node
@@ -545,19 +554,18 @@ def spr_candidates(t: Tree):
     pruning s, except s's old parent and sibling (the unchanged tree)."""
     nodes = np.array(sorted(t.nodes()), np.int64)
     par = t.parent
-    ok = np.array([par[v] >= 0 and par[par[v]] >= 0 for v in nodes], bool)
-    subs = nodes[ok]
+    pn = par[nodes]
+    subs = nodes[(pn >= 0) & (par[np.maximum(pn, 0)] >= 0)]
     if len(subs) == 0:
         return np.zeros(0, np.int64), np.zeros(0, np.int64)
     tin, tout = euler(t)
     p = par[subs]
     sib = np.where(t.kids[p, 0] == subs, t.kids[p, 1], t.kids[p, 0])
-    S = np.repeat(subs, len(nodes))
-    E = np.tile(nodes, len(subs))
-    ps, ss = np.repeat(p, len(nodes)), np.repeat(sib, len(nodes))
-    inside = (tin[E] >= tin[S]) & (tin[E] < tout[S])
-    keep = ~inside & (E != ps) & (E != ss)
-    return S[keep], E[keep]
+    # one (subtree x node) mask; rows in subtree order, nodes ascending
+    tn = tin[nodes][None, :]
+    keep = ~((tn >= tin[subs][:, None]) & (tn < tout[subs][:, None]))
+    keep &= (nodes[None, :] != p[:, None]) & (nodes[None, :] != sib[:, None])
+    return np.repeat(subs, keep.sum(axis=1)), np.broadcast_to(nodes, keep.shape)[keep]
 
 
 def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None):
@@ -578,7 +586,7 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     else:
         score = scorer(t, S, E)
     # the cost of each subtree where it is now: distance to its sibling
-    subs = np.unique(S)
+    subs = distinct_nodes(S, len(t.parent))
     cur = np.zeros(len(t.parent), np.int64)
     if len(subs):
         p = t.parent[subs]
@@ -736,7 +744,7 @@ def tbr_pass(t: Tree, be, max_moves: int = 16, log=None, diag=None):
     t1 = time.perf_counter()
     S, U, E, score, dclade = tbr_candidates(t, be, diag)
     st.candidates = len(S)
-    subs = np.unique(S)
+    subs = distinct_nodes(S, len(t.parent))
     cur = np.zeros(len(t.parent), np.int64)
     if len(subs):
         p = t.parent[subs]
