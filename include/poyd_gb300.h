@@ -304,6 +304,36 @@ int poyd_nonadd8_median_3_batch(const uint8_t *nodes, int64_t stride,
                                 const int32_t *prelim, const int32_t *d1,
                                 const int32_t *d2, uint8_t *out, void *stream);
 
+/* Fitch on 16- and 32-bit state sets (NonaddCS16 / NonaddCS32: nonaddCSc.c
+ * built with CHARSIZE 16 / 32, characters of 9-16 / 17-32 states).  The
+ * same three operations and arguments as the 8-bit batches, with node rows
+ * of `len` characters of 2 / 4 bytes (host byte order): stride a multiple
+ * of 16 bytes and at least len x 2 (x 4) rounded up to 16. */
+int poyd_nonadd16_distance_batch(const void *nodes, int64_t stride,
+                                 int32_t len, int32_t n, const int32_t *a_idx,
+                                 const int32_t *b_idx, int64_t *dist,
+                                 void *stream);
+int poyd_nonadd16_median_batch(const void *nodes, int64_t stride, int32_t len,
+                               int32_t n, const int32_t *a_idx,
+                               const int32_t *b_idx, void *out,
+                               int64_t *added_cost, void *stream);
+int poyd_nonadd16_median_3_batch(const void *nodes, int64_t stride,
+                                 int32_t len, int32_t n, const int32_t *anc,
+                                 const int32_t *prelim, const int32_t *d1,
+                                 const int32_t *d2, void *out, void *stream);
+int poyd_nonadd32_distance_batch(const void *nodes, int64_t stride,
+                                 int32_t len, int32_t n, const int32_t *a_idx,
+                                 const int32_t *b_idx, int64_t *dist,
+                                 void *stream);
+int poyd_nonadd32_median_batch(const void *nodes, int64_t stride, int32_t len,
+                               int32_t n, const int32_t *a_idx,
+                               const int32_t *b_idx, void *out,
+                               int64_t *added_cost, void *stream);
+int poyd_nonadd32_median_3_batch(const void *nodes, int64_t stride,
+                                 int32_t len, int32_t n, const int32_t *anc,
+                                 const int32_t *prelim, const int32_t *d1,
+                                 const int32_t *d2, void *out, void *stream);
+
 /* ---------------------------------------------------------------------
  * Sankoff characters (SankCS, sankCS.ml:302-377).  k states per character
  * (k <= 8), nchar characters per node; per-node data int32
