@@ -16,7 +16,8 @@ the taxa; they are the leaf ids of :class:`poyd_gb300.search.Tree`.
 Hennig86 (xread): the static characters' state sets per taxon, their
 additive / non-additive, active and weight flags from ccode commands, and
 the tread trees (:func:`read_hennig`).  The non-additive characters give
-the 8-bit Fitch lanes of the GPU path (:meth:`HennigMatrix.fitch_matrix`).
+the 8-, 16- and 32-bit Fitch lanes of the GPU path
+(:meth:`HennigMatrix.fitch_groups`).
 """
 from __future__ import annotations
 
@@ -168,25 +169,51 @@ class HennigMatrix:
         m = int(np.bitwise_or.reduce(self.cells[:, c])) if len(self.cells) else 0
         return [s for s in range(32) if m >> s & 1]
 
+    def _fitch_masks(self, cols, dtype) -> np.ndarray:
+        # bit i = the i-th observed state; a missing cell holds them all
+        out = np.zeros((len(self.names), len(cols)), dtype)
+        for j, c in enumerate(cols):
+            obs = self.observed(c)
+            full = (1 << max(len(obs), 1)) - 1
+            for t in range(len(self.names)):
+                m = int(self.cells[t, c])
+                out[t, j] = full if m == 0 else sum(1 << i for i, s in enumerate(obs) if m >> s & 1)
+        return out
+
     def fitch_matrix(self):
         """The active non-additive characters as 8-bit Fitch state masks:
         (uint8 [n_taxa, k] masks, int64 [k] character indices, int64 [k]
         weights).  As in POY's non-additive encoding, bit i stands for the
         i-th observed state of the character and a missing cell holds every
         observed state.  A character with more than 8 observed states does
-        not fit the 8-bit lanes and raises ValueError."""
+        not fit the 8-bit lanes and raises ValueError (see fitch_groups)."""
         cols = [c for c in range(self.cells.shape[1]) if self.active[c] and not self.additive[c]]
-        out = np.zeros((len(self.names), len(cols)), np.uint8)
-        for j, c in enumerate(cols):
-            obs = self.observed(c)
-            if len(obs) > 8:
-                raise ValueError("character %d has %d states; 8-bit lanes hold 8" % (c, len(obs)))
-            full = (1 << max(len(obs), 1)) - 1
-            for t in range(len(self.names)):
-                m = int(self.cells[t, c])
-                out[t, j] = full if m == 0 else sum(1 << i for i, s in enumerate(obs) if m >> s & 1)
+        for c in cols:
+            if len(self.observed(c)) > 8:
+                raise ValueError("character %d has %d states; 8-bit lanes hold 8"
+                                 % (c, len(self.observed(c))))
         cols = np.array(cols, np.int64)
-        return out, cols, self.weight[cols]
+        return self._fitch_masks(cols, np.uint8), cols, self.weight[cols]
+
+    def fitch_groups(self) -> dict:
+        """The active non-additive characters grouped by lane width the way
+        POY groups them by observed states (data.ml:1962-1989): 2-8 states
+        in 8-bit lanes, 9-16 in 16-bit, 17-32 in 32-bit; characters of 0 or 1
+        observed state never cost anything and are left out.  Returns
+        {width: (masks [n_taxa, k] of that width, int64 character indices,
+        int64 weights)} for the widths present, for the nonadd8 / nonadd16 /
+        nonadd32 batches."""
+        groups = {8: [], 16: [], 32: []}
+        for c in range(self.cells.shape[1]):
+            if not self.active[c] or self.additive[c]:
+                continue
+            k = len(self.observed(c))
+            if k >= 2:
+                groups[8 if k <= 8 else 16 if k <= 16 else 32].append(c)
+        dt = {8: np.uint8, 16: np.uint16, 32: np.uint32}
+        return {w: (self._fitch_masks(cols, dt[w]), np.array(cols, np.int64),
+                    self.weight[np.array(cols, np.int64)])
+                for w, cols in groups.items() if cols}
 
     def additive_intervals(self):
         """The active additive characters as [min, max] state intervals:

@@ -302,3 +302,59 @@ def test_static_poly_sankoff_through_the_search_module():
     want = _static_cost_fitch_only(h, h.trees[0])
     assert search.downpass(t, be).total == want
     assert search.final_cost(t, be).cost == want
+
+
+def test_hennig_fitch_groups_by_state_count(tmp_path):
+    """Characters of 2-8, 9-16 and 17-32 observed states go to 8-, 16- and
+    32-bit lanes; one-state characters are left out; the grouped Fitch cost
+    on a tree equals a direct per-character Fitch over the raw state sets."""
+    rng = np.random.default_rng(21)
+    sym = formats.HENNIG_STATES
+    n_taxa, spans = 24, [3, 12, 20, 1, 2, 32]   # states per character
+    rows = []
+    for t in range(n_taxa):
+        cells = []
+        for c, k in enumerate(spans):
+            # each state appears somewhere: taxon t takes state t mod k, some
+            # taxa a polymorphic pair, one a missing cell
+            s = {(t + c) % k}
+            if t % 4 == 1 and k > 1:
+                s.add((t + 3) % k)
+            cells.append("?" if t == 7 and c == 1 else
+                         sym[s.pop()] if len(s) == 1 else "[" + "".join(sym[x] for x in s) + "]")
+        rows.append("t%d %s" % (t, " ".join(cells)))
+    p = tmp_path / "g.ss"
+    p.write_text("xread\n%d %d\n%s\n;\ncc - .;\ncc + 4;\n" % (len(spans), n_taxa, "\n".join(rows)))
+    h = formats.read_hennig(str(p))
+    obs = [len(h.observed(c)) for c in range(len(spans))]
+    g = h.fitch_groups()
+    want_w = {c: (8 if k <= 8 else 16 if k <= 16 else 32) for c, k in enumerate(obs)
+              if k >= 2 and c != 4}
+    got_w = {int(c): w for w, (_, cols, _) in g.items() for c in cols}
+    assert got_w == want_w and sorted(g) == [8, 16, 32]
+    t = search.Tree(n_taxa)
+    order = list(rng.permutation(n_taxa))
+    t.start(int(order[0]), int(order[1]))
+    for x in order[2:]:
+        t.insert(int(x), int(rng.choice([v for v in t.nodes()])))
+    grouped = 0
+    for w, (M, _, _) in g.items():
+        state = {}
+        for v in t.nodes()[::-1]:
+            if v < t.n:
+                state[v] = M[v]
+                continue
+            c, state[v] = O.nonadd_median_w(*(state[int(k)] for k in t.kids[v]), w)
+            grouped += c
+    direct = 0
+    for c in want_w:
+        full = sum(1 << s for s in h.observed(c))
+        st = {}
+        for v in t.nodes()[::-1]:
+            if v < t.n:
+                st[v] = int(h.cells[v, c]) or full
+                continue
+            a, b = (st[int(k)] for k in t.kids[v])
+            st[v] = a & b if a & b else a | b
+            direct += not (a & b)
+    assert grouped == direct > 0
