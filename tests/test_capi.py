@@ -128,6 +128,17 @@ def test_argument_checks_without_a_gpu(lib):
                                  None, None, 0) == EINVAL
     assert lib.poyd_align_2_host(C.byref(lin), 0, None, None, None, None, None, None, None, 0,
                                  None, None, 0) == 0   # an empty batch is a no-op
+    # wide Fitch rows: 9 characters of 2 (4) bytes need 32 (48) byte rows
+    buf = np.zeros(64, np.uint8)
+    b16 = buf.ctypes.data + (-buf.ctypes.data) % 16   # 16-byte aligned inside buf
+    assert lib.poyd_nonadd16_distance_batch(C.c_void_p(b16), C.c_int64(16), 9, 1, None, None,
+                                            None, None) == EINVAL
+    assert lib.poyd_nonadd32_median_batch(C.c_void_p(b16), C.c_int64(32), 9, 1, None, None,
+                                          None, None, None) == EINVAL
+    assert lib.poyd_nonadd16_median_3_batch(C.c_void_p(b16 + 8), C.c_int64(32), 9, 1, None,
+                                            None, None, None, None, None) == EINVAL
+    assert lib.poyd_nonadd32_distance_batch(C.c_void_p(b16), C.c_int64(48), 9, 0, None, None,
+                                            None, None) == 0   # nothing to do
     # single-pair column operations: null outputs
     assert lib.poyd_algn_median_2_with_gaps(p, p, 4, C.byref(lin), None, None) == EINVAL
     assert lib.poyd_algn_worst_2(p, p, 4, C.byref(lin), None) == EINVAL
