@@ -136,21 +136,46 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_time_sample(host, idx, cm_o, threads):
+def result_set(res):
+    """Host copies of a batched align_2 result for the oracle's check (the
+    arrays are kept alive by the returned tuple)."""
+    import ctypes as C
+    from oracle import oracle as O
+    arrs = [np.ascontiguousarray(x.cpu().numpy() if hasattr(x, "cpu") else x)
+            for x in (res.cost, res.out, res.out_off, res.out_len)]
+    s = O.OrResultSet(*[a.ctypes.data for a in arrs])
+    return s, arrs
+
+
+def cpu_time_sample(host, idx, cm_o, threads, sets=()):
     """Runs the oracle's DOS.median on pairs idx over `threads` host threads;
-    returns (seconds, band cells)."""
+    returns (seconds, band cells, per-set mismatch counts).  With `sets`
+    (result_set tuples) every output of those batched results on the
+    sampled pairs is compared with the oracle's in the same pass (a
+    memcmp per pair, negligible beside the DP)."""
+    import ctypes as C
     from oracle import oracle as O
     L = O.lib()
     seq, ao, al, bo, bl = host
     chunks = np.array_split(np.asarray(idx, np.int32), threads)
     cells = [0] * threads
+    bads = [None] * threads
+    arr = (O.OrResultSet * max(len(sets), 1))(*[s for s, _ in sets])
 
     def work(t):
         ch = np.ascontiguousarray(chunks[t])
         cost = np.zeros(len(ch), np.int32)
-        cells[t] = L.or_dos_median_many(seq.ctypes.data, ao.ctypes.data, al.ctypes.data,
-                                        bo.ctypes.data, bl.ctypes.data, ch.ctypes.data,
-                                        len(ch), cm_o, cost.ctypes.data)
+        if sets:
+            bad = np.zeros(len(ch), np.int32)
+            cells[t] = L.or_dos_median_check_many(
+                seq.ctypes.data, ao.ctypes.data, al.ctypes.data, bo.ctypes.data,
+                bl.ctypes.data, ch.ctypes.data, len(ch), cm_o, cost.ctypes.data, len(sets),
+                C.cast(arr, C.c_void_p), bad.ctypes.data)
+            bads[t] = bad
+        else:
+            cells[t] = L.or_dos_median_many(seq.ctypes.data, ao.ctypes.data, al.ctypes.data,
+                                            bo.ctypes.data, bl.ctypes.data, ch.ctypes.data,
+                                            len(ch), cm_o, cost.ctypes.data)
 
     ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
     t0 = time.perf_counter()
@@ -158,7 +183,11 @@ def cpu_time_sample(host, idx, cm_o, threads):
         t.start()
     for t in ths:
         t.join()
-    return time.perf_counter() - t0, int(sum(cells))
+    dt = time.perf_counter() - t0
+    if not sets:
+        return dt, int(sum(cells))
+    bad = np.concatenate(bads)
+    return dt, int(sum(cells)), [int(((bad >> k) & 1).sum()) for k in range(len(sets))]
 
 
 def cpu_sample_indices(host, budget_s, threads, cm_o, seed):
@@ -278,6 +307,7 @@ def run_ours(args):
 
     # ---- end-to-end through the public API with host buffers ----
     e2e = None
+    res_e2e = None
     if not args.no_e2e:
         # sequences plus, per pair, offsets and lengths (a, b) and the slot
         # offset
@@ -299,7 +329,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         n_e2e = max(1, args.steps // 2)
         for _ in range(n_e2e):
-            e2e_step()
+            res_e2e = e2e_step()
         dt = (time.perf_counter() - t0) / n_e2e
         d2h = int(e2e_step.d2h)
         _, dt_max = aggregate(cells, dt, dev, world)
@@ -346,13 +376,29 @@ def run_ours(args):
             threads = os.cpu_count() or 1
             idx = cpu_sample_indices(host, args.cpu_sample_s, threads, C.byref(cm_o),
                                      args.seed)
-            dt, c = cpu_time_sample(host, idx, C.byref(cm_o), threads)
+            # the last timed step's results (device-resident run and, when
+            # measured, the host-buffer run) are checked against the oracle
+            # on every sampled pair while the oracle is timed
+            names = ["value"] + (["e2e"] if res_e2e is not None else [])
+            sets = [result_set(res)] + ([result_set(res_e2e)] if res_e2e is not None else [])
+            dt, c, bad = cpu_time_sample(host, idx, C.byref(cm_o), threads, sets)
             line["cpu_baseline"] = {
                 "value": c / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                 "sample": "%d of %d pairs (random, seeded), %.1f s" % (len(idx), args.pairs, dt)}
+            line["parity"] = {
+                "checked": int(len(idx)), "mismatches": int(sum(bad)),
+                "by_run": dict(zip(names, bad)),
+                "fields": ["cost", "aligned a", "aligned b", "median_2_with_gaps",
+                           "ancestor_2 median"],
+                "against": "oracle (C restatement of algn.c / sequence.ml, pinned against "
+                           "the compiled reference)"}
         except Exception as ex:  # the baseline must not hide the GPU line
             line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
+        if line.get("parity", {}).get("mismatches"):
+            sys.stderr.write("bench: %d of %d sampled pairs differ from the oracle\n"
+                             % (line["parity"]["mismatches"], line["parity"]["checked"]))
+            sys.exit(1)
     if world > 1:
         dist.destroy_process_group()
 

@@ -107,16 +107,19 @@ int poyd_cost_2_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
 /* poyd_cost_2_batch for callers that cannot allocate device memory.  It has
  * no counterpart in the reference (whose C code mallocs host scratch per
  * call).  Some callers cannot call cudaMalloc: a C stub running inside a
- * host that owns the CUDA context and its memory pool, code that runs while
- * a CUDA graph is being captured, or a service with a fixed device-memory
- * budget.  This entry point allocates nothing: its scratch (plans, counters,
+ * host that owns the CUDA context and its memory pool, or a service with a
+ * fixed device-memory budget.  This entry point allocates nothing: its
+ * scratch (plans, counters,
  * cost tables, per-warp boundary rows) is one fixed ~24 MiB __device__ array
  * in the library, held by every GPU that loads the library until exit.
  * Linear model only; at most 65,536 pairs per call and bands up to 1,984
  * diagonals, else POYD_ERANGE before any DP kernel runs.  All calls share the
  * array, so calls that overlap on the GPU race and must be serialised by the
- * caller.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * caller.  The call waits for its stream once (it reads the plan's error
+ * flags back before the DP launch), so a stream that is being captured is
+ * refused with POYD_EUNSUP.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture. */
 int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uint8_t *seq,
                               const int64_t *a_off, const int32_t *a_len,
                               const int64_t *b_off, const int32_t *b_len,

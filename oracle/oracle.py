@@ -41,6 +41,14 @@ class OrCM(C.Structure):
     ]
 
 
+class OrResultSet(C.Structure):
+    """Mirror of ``or_result_set`` (poy_oracle.h): host copies of a batched
+    align_2 result (costs, slot bytes, slot offsets, lengths)."""
+
+    _fields_ = [("cost", C.c_void_p), ("out", C.c_void_p), ("off", C.c_void_p),
+                ("len", C.c_void_p)]
+
+
 def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB_PATH):
         subprocess.check_call(["sh", os.path.join(HERE, "build_oracle.sh")],
@@ -48,13 +56,18 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(src_dir: str | None = None) -> str | None:
-    """Compile the reference C kernels when their sources are present."""
-    src = src_dir or os.environ.get("POYD_REFERENCE_SRC", "/root/reference/src")
-    if not os.path.exists(os.path.join(src, "algn.c")):
+def build_ref(src_dir: str | None = None, env: dict | None = None) -> str | None:
+    """Compile the reference C kernels when their sources are present
+    (build_ref.sh finds them: `src_dir`, else POYD_REFERENCE_SRC, else the
+    recipe's default location).  Returns the library path, or None where
+    the sources are absent."""
+    cmd = ["sh", os.path.join(HERE, "build_ref.sh")] + ([src_dir] if src_dir else [])
+    r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True,
+                       env=env)
+    if r.returncode == 2:  # the recipe's "sources not found"
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), src],
-                          stdout=subprocess.DEVNULL)
+    if r.returncode:
+        raise RuntimeError("build_ref.sh failed: " + r.stderr[-2000:])
     return REF_PATH
 
 
@@ -98,6 +111,10 @@ def lib():
                                          C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OrCM),
                                          C.c_void_p]
         L.or_dos_median_many.restype = C.c_int64
+        L.or_dos_median_check_many.argtypes = [C.c_void_p] * 6 + [C.c_int, C.POINTER(OrCM),
+                                                                  C.c_void_p, C.c_int,
+                                                                  C.c_void_p, C.c_void_p]
+        L.or_dos_median_check_many.restype = C.c_int64
         L.or_candidate_scores.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_int, C.c_int,
                                                              C.c_void_p, C.c_void_p, C.c_void_p,
                                                              C.c_int, C.POINTER(OrCM), C.c_void_p]

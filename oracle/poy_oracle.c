@@ -1005,6 +1005,56 @@ int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32
     return cells;
 }
 
+/* One result tail of a right-aligned slot: the last len bytes before end. */
+static int or_tail_eq(const uint8_t *end, int32_t len, const uint8_t *want, int wlen) {
+    return len == wlen && memcmp(end - len, want, (size_t)len) == 0;
+}
+
+/* or_dos_median_many that also checks batches computed elsewhere against
+ * the restatement's outputs.  Each of the nset result sets holds, per pair
+ * i of the batch, the cost cost[i], the lengths len[2i] (aligned pair and
+ * median with gaps) and len[2i+1] (median), and a slot at out + off[i] of
+ * four right-aligned sequences (aligned a, aligned b, median with gaps,
+ * median), each cap = (la + lb + 5) & ~3 bytes: the layout batched align_2
+ * writes.  bad[t] gets a bit per set whose pair idx[t] differs anywhere. */
+int64_t or_dos_median_check_many(const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,
+                                 const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
+                                 int n, const or_cm *m, int32_t *cost, int nset,
+                                 const or_result_set *sets, int32_t *bad) {
+    static __thread uint8_t *buf = NULL;
+    static __thread size_t cap = 0;
+    int64_t cells = 0;
+    int t, k;
+    for (t = 0; t < n; t++) {
+        int i = idx[t];
+        const uint8_t *a = seq + a_off[i], *b = seq + b_off[i];
+        int la = a_len[i], lb = b_len[i], lm = 0, lal = 0;
+        size_t need = (size_t)(la + lb + 4) * 4;
+        int64_t sc = ((int64_t)la + lb + 2 + 3) / 4 * 4;
+        uint8_t *sm, *ra, *rb, *wg;
+        if (need > cap) { free(buf); buf = (uint8_t *)malloc(need); cap = need; }
+        sm = buf; ra = buf + (la + lb + 4); rb = ra + (la + lb + 4); wg = rb + (la + lb + 4);
+        cost[t] = or_dos_median(a, la, b, lb, m, sm, &lm, ra, rb, wg, &lal);
+        bad[t] = 0;
+        for (k = 0; k < nset; k++) {
+            const or_result_set *S = &sets[k];
+            const uint8_t *slot = S->out + S->off[i];
+            int32_t n0 = S->len[2 * i], n1 = S->len[2 * i + 1];
+            int ok = S->cost[i] == cost[t] && n0 == lal && n1 == lm &&
+                     or_tail_eq(slot + sc, n0, ra, lal) && or_tail_eq(slot + 2 * sc, n0, rb, lal) &&
+                     or_tail_eq(slot + 4 * sc, n1, sm, lm);
+            /* the median with gaps is defined for the linear model's
+             * median_2_with_gaps and affine's medianwg alike */
+            if (ok && lal > 0) ok = or_tail_eq(slot + 3 * sc, n0, wg, lal);
+            if (!ok) bad[t] |= 1 << k;
+        }
+        if (m->cost_model == 1) cells += or_band_cells_affine(la, lb);
+        else cells += or_band_cells_linear(la >= lb ? la : lb, la >= lb ? lb : la,
+                                           or_cost2_deltaw(a, la, b, lb, m->gap, 0, 0));
+    }
+    return cells;
+}
+
 /* Candidate-join scores for the CPU timing of a search pass: for pairs
  * (a[t], b[t]) of nodes, DOS.distance (seqCS.ml:819-867) + Fitch distance
  * (nonaddCSc.c:1076-1105) + Sankoff distance (sankCS.ml:371-377).  Node

@@ -146,6 +146,23 @@ int64_t or_dos_median_many(const uint8_t *seq, const int64_t *a_off, const int32
                            const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
                            int n, const or_cm *m, int32_t *cost);
 
+/* Results of a batched align_2 computed elsewhere (host copies): per pair
+ * cost, lengths (aligned, median) and a slot of four right-aligned
+ * sequences at out + off[i]. */
+typedef struct {
+    const int32_t *cost;
+    const uint8_t *out;
+    const int64_t *off;
+    const int32_t *len;
+} or_result_set;
+
+/* or_dos_median_many plus a comparison of every output with nset result
+ * sets; bad[t] has bit k set where set k differs on pair idx[t]. */
+int64_t or_dos_median_check_many(const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,
+                                 const int64_t *b_off, const int32_t *b_len, const int32_t *idx,
+                                 int n, const or_cm *m, int32_t *cost, int nset,
+                                 const or_result_set *sets, int32_t *bad);
+
 /* Candidate-join scores DOS.distance + Fitch + Sankoff (CPU timing driver). */
 void or_candidate_scores(const uint8_t *seq, const int64_t *off, const int32_t *len,
                          const uint8_t *fitch, int nf, const int64_t *sank, int ns, int k,

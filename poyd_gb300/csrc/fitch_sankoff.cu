@@ -236,6 +236,7 @@ extern "C" int poyd_nonadd8_distance_batch(const uint8_t *nodes, int64_t stride,
   int rc = check_rows(nodes, stride, len, n);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!a_idx || !b_idx || !dist) return fail(POYD_EINVAL, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("fitch_distance", st);
   k_fitch_distance<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
@@ -250,6 +251,7 @@ extern "C" int poyd_nonadd8_median_batch(const uint8_t *nodes, int64_t stride, i
   int rc = check_rows(nodes, stride, len, n);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!a_idx || !b_idx) return fail(POYD_EINVAL, "null argument");
   if (!out || ((uintptr_t)out & 15)) return fail(POYD_EINVAL, "output rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("fitch_median", st);
@@ -266,6 +268,7 @@ extern "C" int poyd_nonadd8_median_3_batch(const uint8_t *nodes, int64_t stride,
   int rc = check_rows(nodes, stride, len, n);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!anc || !prelim || !d1 || !d2) return fail(POYD_EINVAL, "null argument");
   if (!out || ((uintptr_t)out & 15)) return fail(POYD_EINVAL, "output rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("fitch_median3", st);

@@ -178,6 +178,7 @@ int wide_distance(const void *nodes, int64_t stride, int32_t len, int32_t n, con
   int rc = check_wide_rows(nodes, stride, len, n, W);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!ai || !bi || !dist) return fail(POYD_EINVAL, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps(W == 16 ? "fitch16_distance" : "fitch32_distance", st);
   k_fitch_wide_distance<W><<<warp_blocks(n), 256, 0, st>>>((const uint8_t *)nodes, stride, len, n,
@@ -192,6 +193,7 @@ int wide_median(const void *nodes, int64_t stride, int32_t len, int32_t n, const
   int rc = check_wide_rows(nodes, stride, len, n, W);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!ai || !bi) return fail(POYD_EINVAL, "null argument");
   if (!out || ((uintptr_t)out & 15)) return fail(POYD_EINVAL, "output rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps(W == 16 ? "fitch16_median" : "fitch32_median", st);
@@ -208,6 +210,7 @@ int wide_median3(const void *nodes, int64_t stride, int32_t len, int32_t n, cons
   int rc = check_wide_rows(nodes, stride, len, n, W);
   if (rc) return rc;
   if (n == 0) return POYD_OK;
+  if (!anc || !pre || !d1 || !d2) return fail(POYD_EINVAL, "null argument");
   if (!out || ((uintptr_t)out & 15)) return fail(POYD_EINVAL, "output rows must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps(W == 16 ? "fitch16_median3" : "fitch32_median3", st);

@@ -2,10 +2,9 @@
 // cannot allocate device memory.
 //
 // Some callers cannot call cudaMalloc at all: an OCaml servant whose C stub
-// runs inside a host that owns the CUDA context and its memory pool, code
-// executing while a CUDA graph is being captured (where allocation calls
-// are not allowed), or a process with a fixed device-memory budget that
-// forbids growth after start-up.  For them this entry point runs the same
+// runs inside a host that owns the CUDA context and its memory pool, or a
+// process with a fixed device-memory budget that forbids growth after
+// start-up.  For them this entry point runs the same
 // plan and band-DP kernels as poyd_cost_2_batch, but every scratch byte
 // those kernels need -- per-pair plans, the launch counter and error
 // flags, the staged cost tables and the per-warp boundary-row slabs --
@@ -20,10 +19,13 @@
 // so callers must serialise them.  The counter and error flags are
 // cleared on every call; the rest is fully rewritten before it is read.
 //
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (the name of a __device__ variable is only a
-// host-side handle, not a device pointer); make that first call outside
-// any stream capture.
+// The call waits for its stream once, to read the plan's error flags back
+// before the DP launch; a stream that is being captured cannot be waited
+// on, so such a stream is refused with POYD_EUNSUP before anything is
+// enqueued.  The first call on each device looks up the array's device
+// address with cudaGetSymbolAddress (the name of a __device__ variable is
+// only a host-side handle, not a device pointer); make that first call
+// outside any stream capture.
 #include <cuda_runtime.h>
 #include <cstring>
 #include <mutex>
@@ -121,10 +123,15 @@ extern "C" int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uin
   if (deltaw_policy == POYD_DELTAW_EXPLICIT && !deltaw)
     return fail(POYD_EINVAL, "explicit deltaw policy needs the deltaw array");
   if (n == 0) return POYD_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  NA_CK(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(POYD_EUNSUP, "poyd_cost_2_batch_noalloc waits for its stream (error flags are "
+                             "read back), which a stream under capture cannot do");
   unsigned char *base = nullptr;
   rc = na_scratch(&base);
   if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
   int *counter = (int *)base;
   int32_t *err = (int32_t *)(base + 64);
   DevTables *tabs = (DevTables *)(base + kNaHeader);

@@ -39,8 +39,31 @@ class PoydCM(C.Structure):
     ]
 
 
-# (name, restype, argtypes) of every exported symbol; tests check that the
-# library exports exactly these.
+# Every entry point the public header declares (include/poyd_gb300.h);
+# tests check the header's declarations against this list and that the
+# library exports each of them.
+EXPORTED = (
+    "poyd_adam_step", "poyd_algn_align_2d", "poyd_algn_align_affine_3", "poyd_algn_ancestor_2",
+    "poyd_algn_backtrack_2d", "poyd_algn_cost_affine_3", "poyd_algn_median_2_no_gaps",
+    "poyd_algn_median_2_with_gaps", "poyd_algn_simple_2", "poyd_algn_verify_2",
+    "poyd_algn_worst_2", "poyd_align_2_batch", "poyd_align_2_host", "poyd_ancestor_2_batch",
+    "poyd_closest_batch", "poyd_cm_dna", "poyd_cm_of_matrix5", "poyd_colsum_bf16",
+    "poyd_cost_2_batch", "poyd_cost_2_batch_noalloc", "poyd_gemm_bf16", "poyd_int32_peak",
+    "poyd_int_pipe_rate", "poyd_last_error", "poyd_launch_count", "poyd_matrix_create",
+    "poyd_matrix_free", "poyd_median_2_no_gaps_batch", "poyd_median_2_with_gaps_batch",
+    "poyd_mlp_head_backward", "poyd_mlp_head_forward", "poyd_nonadd16_distance_batch",
+    "poyd_nonadd16_median_3_batch", "poyd_nonadd16_median_batch",
+    "poyd_nonadd32_distance_batch", "poyd_nonadd32_median_3_batch",
+    "poyd_nonadd32_median_batch", "poyd_nonadd8_distance_batch", "poyd_nonadd8_median_3_batch",
+    "poyd_nonadd8_median_batch", "poyd_pack_alignments", "poyd_profile_enable",
+    "poyd_profile_read", "poyd_relu_grad_bf16", "poyd_sank_distance_batch",
+    "poyd_sank_median_batch", "poyd_to_bf16", "poyd_verify_2_batch", "poyd_version",
+    "poyd_worst_2_batch",
+)
+
+# (name, restype, argtypes) of the entry points the Python mirror calls
+# through typed ctypes signatures (a subset of EXPORTED; the others are set
+# up where they are called).
 _vp, _i32, _i64 = C.c_void_p, C.c_int32, C.c_int64
 _cmp = C.POINTER(PoydCM)
 SIGNATURES = [

@@ -139,12 +139,32 @@ def test_argument_checks_without_a_gpu(lib):
                                             None, None, None, None, None) == EINVAL
     assert lib.poyd_nonadd32_distance_batch(C.c_void_p(b16), C.c_int64(48), 9, 0, None, None,
                                             None, None) == 0   # nothing to do
+    # null index arrays or a null distance output with pairs to do
+    idx = np.zeros(1, np.int32)
+    ip = C.c_void_p(idx.ctypes.data)
+    dist = np.zeros(1, np.int64)
+    dp = C.c_void_p(dist.ctypes.data)
+    v, i64 = C.c_void_p(b16), C.c_int64(16)
+    for W in (8, 16, 32):
+        dist_f = getattr(lib, "poyd_nonadd%d_distance_batch" % W)
+        med_f = getattr(lib, "poyd_nonadd%d_median_batch" % W)
+        med3_f = getattr(lib, "poyd_nonadd%d_median_3_batch" % W)
+        ln = 16 // (W // 8)
+        assert dist_f(v, i64, ln, 1, None, ip, dp, None) == EINVAL
+        assert dist_f(v, i64, ln, 1, ip, None, dp, None) == EINVAL
+        assert dist_f(v, i64, ln, 1, ip, ip, None, None) == EINVAL
+        assert b"null argument" in lib.poyd_last_error()
+        assert med_f(v, i64, ln, 1, ip, None, v, None, None) == EINVAL
+        assert med3_f(v, i64, ln, 1, ip, ip, None, ip, v, None) == EINVAL
+        assert med3_f(v, i64, ln, 1, ip, ip, ip, None, v, None) == EINVAL
     # single-pair column operations: null outputs
     assert lib.poyd_algn_median_2_with_gaps(p, p, 4, C.byref(lin), None, None) == EINVAL
     assert lib.poyd_algn_worst_2(p, p, 4, C.byref(lin), None) == EINVAL
 
 
-def test_integration_guide_lists_every_entry_point():
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [s for s in declared_symbols() if s not in doc]
-    assert not missing, missing
+def test_header_matches_exported_list():
+    """The header's declarations and the loader's list of entry points
+    (native.EXPORTED) are the same set, and every typed signature the
+    loader sets up names one of them."""
+    assert declared_symbols() == sorted(native.EXPORTED)
+    assert {n for n, _, _ in native.SIGNATURES} <= set(native.EXPORTED)

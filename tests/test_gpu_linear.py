@@ -125,10 +125,12 @@ def test_full_size_properties():
         assert O.verify_2(r["a"], r["b"], om) == r["cost"]
         assert np.array_equal(r["a"][r["a"] != 16], a[a != 16])
         assert np.array_equal(r["b"][r["b"] != 16], b[b != 16])
-    # and full oracle parity on a sample
-    for i in range(0, 48, 12):
-        c, ra, rb = O.align_2(A[i], B[i], om)
-        assert res[i]["cost"] == c and np.array_equal(res[i]["a"], ra)
+    # and full oracle parity on every pair
+    for i in range(48):
+        c, med, ra, rb, wg = O.dos_median(A[i], B[i], om)
+        r = res[i]
+        assert r["cost"] == c and np.array_equal(r["a"], ra) and np.array_equal(r["b"], rb), i
+        assert np.array_equal(r["median"], med) and np.array_equal(r["median_wg"], wg), i
 
 
 def test_codes_above_31_rejected():

@@ -4,22 +4,18 @@ reference sources are absent (the compiled reference does not travel)."""
 import ctypes as C
 import os
 import platform
-import subprocess
 
 import numpy as np
 import pytest
 
 from oracle import oracle as O
 from poyd_gb300 import synth
-
-REF_SRC = os.environ.get("POYD_REFERENCE_SRC", "/root/reference/src")
-pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(REF_SRC, "algn.c")),
-                                reason="reference sources not present")
-
+from tests.regimes import band_case, config1_pairs
 
 @pytest.fixture(scope="module")
 def R():
-    O.build_ref(REF_SRC)
+    if O.build_ref() is None:
+        pytest.skip("reference sources not present")
     r = O.ref()
     assert r is not None
     return r
@@ -80,6 +76,55 @@ def test_affine_vs_reference(R, model):
                                      C.byref(lr))
         c, med, mwg, ri, rj = O.align_affine_3(a, b, m)
         assert c == c_ref
+        assert np.array_equal(med, bufs[0][:lm.value]) and np.array_equal(mwg, bufs[1][:lw.value])
+        assert np.array_equal(ri, bufs[2][:lr.value]) and np.array_equal(rj, bufs[3][:lr.value])
+    R.ref_cm_free(rc)
+
+
+@pytest.mark.parametrize("model", [(1, 2), (1, 1), (3, 1), (2, 3)])
+def test_linear_vs_reference_config1_lengths(R, model):
+    """align_2 + ancestor_2 + median_2_with_gaps at 1,500-5,000 bp, every
+    band case of algn_fill_plane_2 included."""
+    m = O.cm_dna(model[0], model[1], -1)
+    rc = R.ref_cm_new(C.byref(m))
+    A, B = config1_pairs(400 + model[0] * 10 + model[1], 40)
+    cases = set()
+    for a, b in zip(A, B):
+        dw = O.deltaw(a, b, m)
+        cases.add(band_case(max(len(a), len(b)), min(len(a), len(b)), dw))
+        cap = len(a) + len(b) + 2
+        o1, o2 = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+        n = C.c_int()
+        c_ref = R.ref_align_2(P(a), len(a), P(b), len(b), rc, dw, P(o1), P(o2), C.byref(n))
+        c, ra, rb = O.align_2(a, b, m)
+        assert c == c_ref, (model, len(a), len(b))
+        assert np.array_equal(ra, o1[:n.value]) and np.array_equal(rb, o2[:n.value])
+        t = np.zeros(len(ra) + 2, np.uint8)
+        k = R.ref_ancestor_2(P(ra), P(rb), len(ra), rc, P(t))
+        assert np.array_equal(O.ancestor_2(ra, rb, m), t[:k])
+        w = np.zeros(len(ra) + 2, np.uint8)
+        k = R.ref_median_2_with_gaps(P(ra), P(rb), len(ra), rc, P(w))
+        assert np.array_equal(O.median_2_with_gaps(ra, rb, m), w[:k])
+    R.ref_cm_free(rc)
+    assert cases == {"full", "narrow", "rows"}
+
+
+@pytest.mark.parametrize("model", [(1, 2, 3), (2, 1, 1), (3, 1, 5)])
+def test_affine_vs_reference_config1_lengths(R, model):
+    """cost_affine_3 and align_affine_3 at 1,500-5,000 bp."""
+    m = O.cm_dna(*model)
+    rc = R.ref_cm_new(C.byref(m))
+    A, B = config1_pairs(500 + sum(model), 40)
+    for a, b in zip(A, B):
+        assert O.cost_affine_3(a, b, m) == R.ref_cost_affine_3(P(a), len(a), P(b), len(b), rc)
+        cap = len(a) + len(b) + 3
+        bufs = [np.zeros(cap, np.uint8) for _ in range(4)]
+        lm, lw, lr = C.c_int(), C.c_int(), C.c_int()
+        c_ref = R.ref_align_affine_3(P(a), len(a), P(b), len(b), rc, P(bufs[0]), C.byref(lm),
+                                     P(bufs[1]), C.byref(lw), P(bufs[2]), P(bufs[3]),
+                                     C.byref(lr))
+        c, med, mwg, ri, rj = O.align_affine_3(a, b, m)
+        assert c == c_ref, (model, len(a), len(b))
         assert np.array_equal(med, bufs[0][:lm.value]) and np.array_equal(mwg, bufs[1][:lw.value])
         assert np.array_equal(ri, bufs[2][:lr.value]) and np.array_equal(rj, bufs[3][:lr.value])
     R.ref_cm_free(rc)
@@ -191,14 +236,12 @@ def test_fitch_median_3_vs_reference(R):
 
 @pytest.mark.skipif(platform.machine() != "x86_64",
                     reason="the asm/C switch of algn.c exists on x86-64 only")
-def test_reference_c_cell_path_vs_oracle():
+def test_reference_c_cell_path_vs_oracle(R):
     """algn.c has an inline-asm cell path (x86-64 with MMX) and a plain-C
     one (algn.c:375-453, the one an arm64 build compiles).  The C path,
     built with POYD_REF_C_PATH=1, agrees with the oracle as the asm path
     does."""
-    env = dict(os.environ, POYD_REF_C_PATH="1")
-    subprocess.check_call(["sh", os.path.join(os.path.dirname(O.REF_PATH), "..", "build_ref.sh"),
-                           REF_SRC], stdout=subprocess.DEVNULL, env=env)
+    assert O.build_ref(env=dict(os.environ, POYD_REF_C_PATH="1")) is not None
     Rc = C.CDLL(os.path.join(os.path.dirname(O.REF_PATH), "libporef_cpath.so"))
     Rc.ref_cm_new.argtypes = [C.POINTER(O.OrCM)]
     Rc.ref_cm_new.restype = C.c_void_p

@@ -15,8 +15,9 @@ and cnc*.poy repeat them with ``weightfactor:-1`` added (cnc*.costs).
 Here the same files go through ``search.final_cost`` (best rooting, then
 single-state assignment and the edge-distance sum) over the oracle's DO
 medians, the backend the CUDA kernels match bit for bit.  The files are
-read where the reference tree is present and the test skips elsewhere;
-nothing of them is stored here."""
+the reference's own, packed unchanged into tests/golden/tree_golden.tar.gz
+by tests/golden/make_tree_golden.py; tests/test_gpu_tree_golden.py runs
+them through the CUDA path."""
 import os
 
 import numpy as np
@@ -24,10 +25,10 @@ import pytest
 
 from oracle import oracle as O
 from poyd_gb300 import formats, search, simulate
+from tests import golden_io
 from tests.oracle_backend import OracleBackend
 
-REF_TEST = os.environ.get("POYD_REFERENCE_TEST", "/root/reference/test")
-have_ref = os.path.exists(os.path.join(REF_TEST, "cc.costs"))
+REF_TEST = golden_io.tree_golden_dir()
 
 MODELS = {"cc": ((1, 2, -1), "tree"), "cc1": ((1, 1, -1), "1.tree"),
           "cc2": ((2, 1, 1), "2.tree"), "cc3": ((3, 1, 5), "3.tree")}
@@ -39,7 +40,6 @@ def diagnose(fas, tree_file, om, weight=1):
     return search.final_cost(t, [OracleBackend(ds, om) for ds in frags], weight)
 
 
-@pytest.mark.skipif(not have_ref, reason="reference test files not present")
 @pytest.mark.parametrize("model", sorted(MODELS))
 def test_golden_tree_costs(model):
     (sub, indel, go), suffix = MODELS[model]
@@ -167,15 +167,12 @@ def _static_cost(h, tree_text):
     return total
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
-                    reason="reference test files not present")
 def test_static_poly_cost():
     """test/cost_tests' static_poly.poy: the Hennig matrix
     test/polymorphic.ss (non-additive characters with polymorphic and
     missing cells, two additive characters) on the tree its tread gives;
     the expected cost is read from test/cost_tests."""
-    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
-    want = int(line.split("-cost")[1].split()[0])
+    want = golden_io.static_poly_cost(REF_TEST)
     h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
     assert len(h.trees) == 1
     assert _static_cost(h, h.trees[0]) == want
@@ -221,16 +218,13 @@ def _sankoff_tree_cost(t, leaves, tcm):
     return int(s[t.root].min(axis=1).sum())
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
-                    reason="reference test files not present")
 def test_static_poly_cost_through_sankoff():
     """Sankoff with a 0/1 matrix is Fitch, and with |i - j| costs it is the
     additive rule: the Sankoff oracle on polymorphic.ss, non-additive
     characters under the unit matrix and additive ones under the linear
     matrix (a cell's leaf vector 0 on its states, infinite elsewhere), must
     give the same whole-tree cost as the reference's static_poly test."""
-    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
-    want = int(line.split("-cost")[1].split()[0])
+    want = golden_io.static_poly_cost(REF_TEST)
     h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
     t = formats.parse_tree(h.trees[0], h.names)
     k = 8
@@ -247,15 +241,12 @@ def test_static_poly_cost_through_sankoff():
     assert got == want
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
-                    reason="reference test files not present")
 def test_static_poly_fitch_through_the_search_module():
     """The search module's own accounting (downpass, best rooting, reported
     cost) over polymorphic.ss's non-additive characters, with an empty DO
     character beside them, gives the static_poly cost less its additive
     part."""
-    line = [x for x in open(os.path.join(REF_TEST, "cost_tests")) if "static_poly.poy" in x][0]
-    want = int(line.split("-cost")[1].split()[0])
+    want = golden_io.static_poly_cost(REF_TEST)
     h = formats.read_hennig(os.path.join(REF_TEST, "polymorphic.ss"))
     t = formats.parse_tree(h.trees[0], h.names)
     F, _, _ = h.fitch_matrix()
@@ -284,8 +275,6 @@ def _static_cost_fitch_only(h, tree_text):
     return total
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_TEST, "polymorphic.ss")),
-                    reason="reference test files not present")
 def test_static_poly_sankoff_through_the_search_module():
     """The same characters as Sankoff characters under a 0/1 matrix (which
     makes Sankoff equal Fitch) through the search module: the same cost."""

@@ -1,6 +1,6 @@
 """poyd_cost_2_batch_noalloc: the batched cost_2 for callers that cannot
 allocate device memory (an OCaml C stub inside a host that owns the CUDA
-memory pool, code running under stream capture, a fixed memory budget).
+memory pool, a service with a fixed device-memory budget).
 
 It must return exactly the costs of the allocating entry point
 (poyd_cost_2_batch) -- integer costs, so the tolerance is zero -- on two
@@ -58,3 +58,20 @@ def test_noalloc_rejects_oversize_batch():
     assert rc == -3  # POYD_ERANGE
     assert b"65536" in native.lib().poyd_last_error()
     assert int(out[0].item()) == -7
+
+
+def test_noalloc_rejects_band_wider_than_scratch():
+    """A pair whose band is wider than the 1,984 diagonals a fixed per-warp
+    boundary row holds (here a full plane: 2,401 x 301 gives 2,701
+    diagonals) is refused with POYD_ERANGE before the DP launch; the cost
+    output is left as it was."""
+    rng = np.random.default_rng(5)
+    A = [synth.with_gap(synth.random_dna(rng, 60)), synth.with_gap(synth.random_dna(rng, 2400))]
+    B = [synth.with_gap(synth.random_dna(rng, 50)), synth.with_gap(synth.random_dna(rng, 300))]
+    batch = align.PairBatch.from_host(A, B)
+    out = torch.full((batch.n,), -7, dtype=torch.int32, device="cuda")
+    rc = _noalloc(batch, align.CostMatrix.default(), native.DELTAW_DEFAULT, out)
+    assert rc == -3  # POYD_ERANGE
+    assert b"1984" in native.lib().poyd_last_error()
+    torch.cuda.synchronize()
+    assert out.cpu().tolist() == [-7, -7]
