@@ -46,20 +46,23 @@ __global__ void __launch_bounds__(128, 16) k_lin_plan(LinPlanArgs A) {
   const int la = A.a_len[id], lb = A.b_len[id];
   const int64_t ao = A.a_off[id], bo = A.b_off[id];
   const int gap = A.gap;
-  unsigned ga = 0, gb = 0, na = 0, nb = 0, wide = 0;
+  unsigned ga = 0, gb = 0, na = 0, nb = 0, wide = 0, zero = 0;
   for (int x = lane; x < la; x += 32) {
     const int c = A.seq[ao + x];
     ga += (c & gap) != 0;
     na += c != gap;
     wide |= (unsigned)c >> 5;
+    zero |= c == 0;
   }
   for (int x = lane; x < lb; x += 32) {
     const int c = A.seq[bo + x];
     gb += (c & gap) != 0;
     nb += c != gap;
     wide |= (unsigned)c >> 5;
+    zero |= c == 0;
   }
   wide = __reduce_or_sync(kFull, wide);
+  zero = __reduce_or_sync(kFull, zero);
   ga = __reduce_add_sync(kFull, ga);
   gb = __reduce_add_sync(kFull, gb);
   na = __reduce_add_sync(kFull, na);
@@ -127,7 +130,23 @@ __global__ void __launch_bounds__(128, 16) k_lin_plan(LinPlanArgs A) {
     }
     A.plans[id] = P;
     // direction-matrix words; also the work estimate used to order pairs
-    A.dm_words[id] = (int64_t)P.nblk * lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
+    int64_t words = (int64_t)P.nblk * lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
+    // The packed kernel (linear4.cu): 128-row strips, period
+    // max(roundup32(wd + 4), 256), eight words per lane and 32-step block.
+    // It holds every value in 16 bits when sc * maxc * (max(l1, l2) + 260)
+    // + 6 < 0xC000 (sc = 4 with backtrack moves), byte costs fit its profile
+    // and no code 0 (whose table entries are unbounded) occurs; else err
+    // bit 16 keeps the batch on this file's kernel.
+    {
+      const int W4 = max((wd + 4 + 31) / 32 * 32, 256), T4 = (l1 + 127) >> 7;
+      const int64_t nblk4 = ((int64_t)(T4 - 1) * W4 + 190 + wd + 31) >> 5;
+      if (A.with_dm == kDpChoice && nblk4 * 256 > words) words = nblk4 * 256;
+      const int sc4 = A.with_dm == kDpChoice ? 4 : 1;
+      const int lim = A.with_dm == kDpChoice ? 31 : 127;
+      const long long need = (long long)sc4 * A.maxc * ((l1 > l2 ? l1 : l2) + 260) + 6;
+      if (zero || A.maxc > lim || need >= 0xC000 || A.with_dm == kDpSets) atomicOr(A.err, 16);
+    }
+    A.dm_words[id] = words;
     A.wd_out[id] = wd;
     if (A.cells) A.cells[id] = cells;
     if (la < 1 || lb < 1) atomicOr(A.err, 1);

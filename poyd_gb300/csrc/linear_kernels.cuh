@@ -90,6 +90,11 @@ void launch_lin_order(int n, const LinPlan *plans, const int64_t *dm_words, int6
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
 int lin_dp_blocks(int mode);
 void launch_lin_dp(const LinDpArgs &A, int mode, int blocks, cudaStream_t st);
+// Packed DP (linear4.cu): four rows per lane in 16-bit halves, kDpCost or
+// kDpChoice, for batches the plan marks eligible (no err bit 16).
+int lin_dp4_blocks(int mode);
+int lin_dp4_warps();
+void launch_lin_dp4(const LinDpArgs &A, int mode, int blocks, cudaStream_t st);
 void launch_lin_traceback(const LinTbArgs &A, cudaStream_t st);
 void launch_pack_alignments(int n, const uint8_t *out, const int64_t *out_off,
                             const int32_t *a_len, const int32_t *b_len,

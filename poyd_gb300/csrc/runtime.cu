@@ -270,9 +270,15 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     if (!dm) return fail(POYD_ENOMEM, "direction matrix allocation (%lld bytes) failed",
                          (long long)(max_words * 4));
   }
-  const int blocks = lin_dp_blocks(mode);
+  // The packed kernel (four rows per lane in 16-bit halves) runs the batch
+  // when the plan found every pair's values to fit (no err bit 16);
+  // POYD_PACKED=0 keeps the 32-bit kernel.
+  bool packed = !(tl.err & 16) && mode != kDpSets;
+  if (const char *e = std::getenv("POYD_PACKED")) packed = packed && std::atoi(e) != 0;
+  const int blocks = packed ? lin_dp4_blocks(mode) : lin_dp_blocks(mode);
+  const int warps = packed ? lin_dp4_warps() : kDpWarps;
   const int64_t slab = maxwd + 64;
-  int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * kDpWarps);
+  int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * warps);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
   // Batched align_2 with backtrack moves: the traceback runs inside the DP
   // kernel, batch by batch as their fills complete.
@@ -305,7 +311,11 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
     DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
     DA.done = (ls && fuse && wave_at.size() == 2) ? ls->done : nullptr;
-    { ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st); launch_lin_dp(DA, mode, blocks, st); }
+    {
+      ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st);
+      if (packed) launch_lin_dp4(DA, mode, blocks, st);
+      else launch_lin_dp(DA, mode, blocks, st);
+    }
     CK(cudaGetLastError());
     if (want_align && out && !fuse) {
       { ProfScope ps("lin_traceback", st); launch_lin_traceback(TA, st); }

@@ -204,27 +204,33 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
             ex, ey = masks_from((1, 2, 4, 5), np.where(t_old >= 0, e, 99))
             ex0, ey0 = masks_from((0, 1, 3, 4), np.where(t_old >= 0, e, 99))
             fx, fy = ex & ~ex0, ey & ~ey0   # exactly e == lam[m]
-            # first strips: rows left of column 0 or not yet started
-            d = G - LANE_LAG * k - t_l * W
-            off0 = -dlo - 128 * t_l - 4 * k
+            # first strips: rows left of column 0 or not yet started, relative
+            # to the block's strip t0 (lanes still in strip t0 - 1 of a later
+            # period are not masked: their cells left of column 0 stay >= INF)
+            t0 = G0 // W
+            d = G - LANE_LAG * k - t0 * W
+            off0 = -dlo - 128 * t0 - 4 * k
             var = np.clip(off0, 0, 3)
             tx = np.zeros(32, np.int64)
             ty = np.zeros(32, np.int64)
-            for vv in range(4):
-                sel = (var == vv) & (t_l <= tri_last)
-                ee = d - off0 if vv == 3 else d
-                mx, my = masks_from(TRI_TH[vv], ee)
-                tx[sel], ty[sel] = mx[sel], my[sel]
+            if t0 <= tri_last:
+                gate = (t0 == 0) | (t_l == t0)
+                for vv in range(4):
+                    sel = (var == vv) & gate
+                    ee = d - off0 if vv == 3 else d
+                    mx, my = masks_from(TRI_TH[vv], ee)
+                    tx[sel], ty[sel] = mx[sel], my[sel]
             if kind == "plain":
                 assert not (fx | fy | tx | ty).any()
-            if kind == "mixed":
+            if kind != "slow":
                 assert not (tx | ty).any()
             tX = (DX + cdX) & 0xFFFFFFFF
             tX = add_min16(X, ci, tX)
             Xn = add_min16(DXp, caX, tX)
             if choice:
                 rX = Xn & 0x00030003
-                dm[blk, :, v // 8] = (dm[blk, :, v // 8] * 4 + rX) & 0xFFFFFFFF
+                wx = 4 * (v // 16) + (v // 8) % 2
+                dm[blk, :, wx] = (dm[blk, :, wx] * 4 + rX) & 0xFFFFFFFF
                 Xn = Xn - rX
             Xn = lop_inf(Xn, fx | tx)
             tY = (Xn + cdY) & 0xFFFFFFFF
@@ -232,7 +238,8 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
             Yn = add_min16(X, caY, tY)
             if choice:
                 rY = Yn & 0x00030003
-                dm[blk, :, 4 + v // 8] = (dm[blk, :, 4 + v // 8] * 4 + rY) & 0xFFFFFFFF
+                wy = 4 * (v // 16) + 2 + (v // 8) % 2
+                dm[blk, :, wy] = (dm[blk, :, wy] * 4 + rY) & 0xFFFFFFFF
                 Yn = Yn - rY
             Yn = lop_inf(Yn, fy | ty)
             if G == Gf:
@@ -269,7 +276,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
         t, kk, mm = r // 128, (r % 128) // 4, r % 4
         G = t * W + LANE_LAG * kk + LAM[mm] + (j - r) - dlo
         vv = G % 32
-        wrd = int(dm[G // 32, kk, 4 * (mm & 1) + vv // 8])
+        wrd = int(dm[G // 32, kk, 4 * (vv // 16) + 2 * (mm & 1) + (vv // 8) % 2])
         code = (wrd >> (2 * (7 - vv % 8) + 16 * (mm >> 1))) & 3
         mv = 0 if code == 0 else (1 if (code == 1) == swaped else 2)
         cr = s1[r] if mv != 1 else gap
