@@ -4,14 +4,16 @@ per lane in two registers of two 16-bit halves.
 A numpy emulation of one warp, step by step, with the kernel's exact
 arithmetic: 32-bit packed registers, per-half wrapping add-min
 (__viaddmin_u16x2), full 32-bit adds (with carries between the halves) for
-the delete candidates, byte permutes for the cost operands, the queue and
+the insert candidates, byte permutes for the cost operands, the queue and
 boundary-slab timing, per-block column windows, the forced out-of-band
 cells and the clamp of the first strips.  Layout:
   * lane k owns rows 128t + 4k + m (m = 0..3) of strip t; row m runs
-    lam[m] = (0, 1, 3, 4) steps behind row 0, lane k runs 6k steps behind
-    lane 0, so row 4k+m is at band index i at step tW + 6k + lam[m] + i;
+    lam[m] = (0, 1, 3, 4) steps behind row 0, lane k runs 7k steps behind
+    lane 0, so row 4k+m is at band index i at step tW + 7k + lam[m] + i
+    (lane k-1's row 3 reaches lane k's row 0 two steps after it is computed:
+    the shuffle that carries it runs a step ahead, off the critical path);
   * X = {row 0, row 2}, Y = {row 1, row 3} (low half, high half);
-  * W = max(roundup32(wd + 4), 256): at least 4 out-of-band steps between
+  * W = max(roundup32(wd + 4), 288): at least 4 out-of-band steps between
     strips, so that every strip-dependent input of a lane (column window,
     cost profile, delete costs) switches at one step, d = 0.
 The emulated costs and the alignments walked back from the emulated moves
@@ -27,8 +29,9 @@ M16 = 0xFFFF
 INF16 = 0xC000
 INF2 = 0xC000C000
 LAM = (0, 1, 3, 4)
-LANE_LAG = 6
+LANE_LAG = 7  # lane k-1's row 3 feeds lane k's row 0 two steps later
 R3_LAG = LANE_LAG * 31 + 4  # lane 31's row 3 relative to lane 0's row 0
+MIN_PERIOD = 288  # lane 31's row-3 values flushed two blocks before lane 0 reads them
 
 
 def band(a, b, m):
@@ -96,7 +99,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
     maxc = int(cost[1:32, 1:32].max())
     assert eligible(L1, L2, maxc, sc)
     T = (L1 + 127) // 128
-    W = max((wd + 4 + 31) // 32 * 32, 256)
+    W = max((wd + 4 + 31) // 32 * 32, MIN_PERIOD)
     Gg = W - wd
     nblk = ((T - 1) * W + R3_LAG + wd + 31) // 32
     rank_i = (1 if swaped else 2) if choice else 0
@@ -129,7 +132,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
     def lookups(t, G):
         """Window word (column char, insert cost) and profile word of lane
         k's row 0 column at step G in strip t."""
-        j = 128 * t + dlo + (G - t * W) - 2 * k
+        j = 128 * t + dlo + (G - t * W) - (LANE_LAG - 4) * k
         c = np.where((j >= 0) & (j < L2), s2[np.clip(j, 0, L2 - 1)], gap)
         return gtab[c], strip_consts(t)[3][c, k]
 
@@ -138,7 +141,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
         o = G0 - t * W
         for tt in (t, t + 1):  # the period of the block and the next one
             if 0 <= tt <= tri_last:
-                end = tt * W + max(-dlo - 128 * tt + 62, R3_LAG)
+                end = tt * W + max(-dlo - 128 * tt + (LANE_LAG - 4) * 31 + 1, R3_LAG)
                 if G0 <= end and G0 + 31 >= tt * W:
                     return "slow"
         if o + 31 >= W - Gg or o <= R3_LAG:
@@ -158,6 +161,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
 
     X = np.full(32, INF2, np.int64)
     Y = X.copy()
+    Yp = X.copy()  # Y two steps back: lane k-1's row 3 for lane k's row 0
     DXp = X.copy()
     DXp[0] = (INF16 << 16) | (bnd[0] >> 16)
     g_prev = np.full(32, 0, np.int64)
@@ -178,7 +182,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
             kinds[kind] = kinds.get(kind, 0) + 1
         for v in range(32):
             G = G0 + v
-            recv = np.roll(Y, 1)
+            recv = np.roll(Yp, 1)
             up = recv.copy()
             up[0] = q[0]
             q = np.roll(q, -1)
@@ -224,31 +228,27 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
                 assert not (fx | fy | tx | ty).any()
             if kind != "slow":
                 assert not (tx | ty).any()
-            tX = (DX + cdX) & 0xFFFFFFFF
-            tX = add_min16(X, ci, tX)
-            Xn = add_min16(DXp, caX, tX)
+            # align and insert terms first (they need no value of this step);
+            # the insert add is one 32-bit add of both halves
+            tX = add_min16(DXp, caX, (X + ci) & 0xFFFFFFFF)
+            tY = add_min16(X, caY, (Y + ci) & 0xFFFFFFFF)
+            Xn = add_min16(DX, cdX, tX)
             if choice:
                 rX = Xn & 0x00030003
                 wx = 4 * (v // 16) + (v // 8) % 2
                 dm[blk, :, wx] = (dm[blk, :, wx] * 4 + rX) & 0xFFFFFFFF
-                Xn = Xn - rX
+                Xn = Xn & 0xFFFCFFFC
             Xn = lop_inf(Xn, fx | tx)
-            tY = (Xn + cdY) & 0xFFFFFFFF
-            tY = add_min16(Y, ci, tY)
-            Yn = add_min16(X, caY, tY)
+            Yn = add_min16(Xn, cdY, tY)
             if choice:
                 rY = Yn & 0x00030003
                 wy = 4 * (v // 16) + 2 + (v // 8) % 2
                 dm[blk, :, wy] = (dm[blk, :, wy] * 4 + rY) & 0xFFFFFFFF
-                Yn = Yn - rY
+                Yn = Yn & 0xFFFCFFFC
             Yn = lop_inf(Yn, fy | ty)
             if G == Gf:
                 reg = Xn if mf in (0, 2) else Yn
                 result = int((reg[kf] >> (16 if mf >= 2 else 0)) & M16)
-            if trace is not None and "lane" in trace and trace["g0"] <= G < trace["g1"]:
-                kk = trace["lane"]
-                print(G, "d", G - LANE_LAG * kk - t_l[kk] * W, "X %08x Y %08x DX %08x ci %08x caX %08x cdX %08x fx %08x tx %08x" %
-                      (Xn[kk], Yn[kk], DX[kk], ci[kk], caX[kk], cdX[kk], fx[kk], tx[kk]))
             if trace is not None:  # cell values by (row, band index), for debugging
                 for mm in range(4):
                     reg = Xn if mm in (0, 2) else Yn
@@ -260,6 +260,7 @@ def emulate4(a, b, m, choice=True, kinds=None, trace=None):
                         if 0 <= rr[kk] < L1 and ii[kk] < wd:
                             trace[(int(rr[kk]), int(ii[kk]))] = int(val[kk])
             q[31] = Yn[31]
+            Yp = Y
             DXp, X, Y, g_prev, pr_prev = DX, Xn, Yn, g, pr
         for L in range(32):  # lane 31's row-3 values of this block: the next boundary row
             p = G0 + L - R3_LAG
