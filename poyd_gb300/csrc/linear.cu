@@ -132,14 +132,14 @@ __global__ void __launch_bounds__(128, 16) k_lin_plan(LinPlanArgs A) {
     // direction-matrix words; also the work estimate used to order pairs
     int64_t words = (int64_t)P.nblk * lin_dm_words(A.with_dm == kDpChoice ? kDpChoice : kDpSets);
     // The packed kernel (linear4.cu): 128-row strips, period
-    // max(roundup32(wd + 4), 256), eight words per lane and 32-step block.
+    // max(roundup32(wd + 4), 288), eight words per lane and 32-step block.
     // It holds every value in 16 bits when sc * maxc * (max(l1, l2) + 260)
     // + 6 < 0xC000 (sc = 4 with backtrack moves), byte costs fit its profile
     // and no code 0 (whose table entries are unbounded) occurs; else err
     // bit 16 keeps the batch on this file's kernel.
     {
-      const int W4 = max((wd + 4 + 31) / 32 * 32, 256), T4 = (l1 + 127) >> 7;
-      const int64_t nblk4 = ((int64_t)(T4 - 1) * W4 + 190 + wd + 31) >> 5;
+      const int W4 = max((wd + 4 + 31) / 32 * 32, 288), T4 = (l1 + 127) >> 7;
+      const int64_t nblk4 = ((int64_t)(T4 - 1) * W4 + 221 + wd + 31) >> 5;
       if (A.with_dm == kDpChoice && nblk4 * 256 > words) words = nblk4 * 256;
       const int sc4 = A.with_dm == kDpChoice ? 4 : 1;
       const int lim = A.with_dm == kDpChoice ? 31 : 127;

@@ -9,17 +9,21 @@
 //
 // Layout.  One warp owns one pair (persistent grid, longest first).  Lane k
 // owns rows 128t + 4k + m (m = 0..3) of strip t.  Row m runs lam[m] =
-// (0, 1, 3, 4) steps behind the lane's row 0 and lane k runs 6k steps
+// (0, 1, 3, 4) steps behind the lane's row 0 and lane k runs 7k steps
 // behind lane 0, so row 4k+m of strip t is at band index i (diagonal
-// dlo + i) at step tW + 6k + lam[m] + i.  Rows 0 and 2 share register X
-// (low, high half), rows 1 and 3 register Y:
+// dlo + i) at step tW + 7k + lam[m] + i.  Lane k-1's row 3 value that lane
+// k's row 0 needs is computed two steps earlier, so the shuffle carrying it
+// is issued a step ahead and stays off the step's dependency chain.  Rows
+// 0 and 2 share register X (low, high half), rows 1 and 3 register Y:
 //   * X's rows never depend on each other within a step (row 2 reads row 1
 //     of the previous steps), so one __viaddmin_u16x2 updates both;
 //   * Y's rows read X's fresh values as their delete predecessors (rows 1
 //     and 3 run one step behind rows 0 and 2), so D_Y = X and A_Y = the
 //     previous X, with no permute;
 //   * X's delete predecessors are {row above row 0 (lane k-1's row 3),
-//     row 1} = one byte permute of the shuffled Y and the lane's own Y.
+//     row 1} = one byte permute of the shuffled Y and the lane's own Y;
+//   * per register, min(align, insert) is formed first (it needs no value
+//     of the step) and the delete term enters with one add-min.
 // Rows 0 and 1 read column c(u) at step u, rows 2 and 3 column c(u-1): one
 // profile word per step holds four byte costs (one per row) and the cost
 // operands are byte permutes of this step's and the previous step's word
@@ -28,7 +32,7 @@
 // two bits in kDpChoice, as in linear.cu.
 //
 // Out-of-band cells.  Strips follow one another with period W =
-// max(roundup32(wd + 4), 256): each row spends W - wd >= 4 steps out of the
+// max(roundup32(wd + 4), 288): each row spends W - wd >= 4 steps out of the
 // band between strips, so every strip-dependent input of a lane (column
 // window, profile, delete costs) can switch at one step.  The cell of each
 // row at band index wd is forced to INF (the reference's right-edge cell
@@ -45,7 +49,7 @@
 // bias + max(r, j) * maxc; the host only launches this kernel when
 // sc * maxc * (max(L1, L2) + 260) + 6 < INF16 = 0xC000 for every pair, so
 // real values never reach INF16 and INF16 plus a cost never wraps.  Adds
-// of two packed halves as one 32-bit add (the delete candidates) carry
+// of two packed halves as one 32-bit add (the insert candidates) carry
 // from the low half only where the low row is past the matrix edge, and
 // then the high row is too.
 #include <cuda_runtime.h>
@@ -59,9 +63,11 @@ namespace {
 
 constexpr unsigned kFull4 = 0xffffffffu;
 constexpr int k4Warps = 8;          // warps per block
-constexpr int k4Lag = 6;            // steps between consecutive lanes
-constexpr int k4R3 = 6 * 31 + 4;    // lane 31's row 3 behind lane 0's row 0
-constexpr int k4MinPeriod = 256;    // boundary row flush-to-prefetch distance
+constexpr int k4Lag = 7;            // steps between consecutive lanes
+constexpr int k4R3 = 7 * 31 + 4;    // lane 31's row 3 behind lane 0's row 0
+constexpr int k4MinPeriod = 288;    // boundary row flush-to-prefetch distance
+constexpr int k4WinBase = 3 * 31;   // window position of lane 31's step-0 column
+constexpr int k4Win = 128;          // window entries per strip (positions 0..124)
 constexpr uint32_t kInf16 = 0xC000u;
 constexpr uint32_t kInf2 = 0xC000C000u;
 constexpr int kEdgeOff = 40, kEdgeN = 112;  // right-edge masks, offsets [-40, 72)
@@ -69,8 +75,8 @@ constexpr int kTriOff = 40, kTriN = 80;     // first-strip masks, offsets [-40, 
 
 // Shared memory, in bytes from a 128-byte aligned base.
 constexpr uint32_t kSmProf = 0;                        // [warp][parity][c][lane] u32
-constexpr uint32_t kSmWin = kSmProf + k4Warps * 8192;  // [warp][new, old][96] u32
-constexpr uint32_t kSmCtab = kSmWin + k4Warps * 768;   // cost[a][b] at a*33+b (u32)
+constexpr uint32_t kSmWin = kSmProf + k4Warps * 8192;  // [warp][new, old][k4Win] uint2
+constexpr uint32_t kSmCtab = kSmWin + k4Warps * 2 * k4Win * 8;  // cost[a][b] at a*33+b (u32)
 constexpr uint32_t kSmGt = kSmCtab + 32 * 33 * 4;      // insert costs [rank 0,1,2][c] (u32)
 constexpr uint32_t kSmEdge = kSmGt + 3 * 32 * 4;       // [kEdgeN] {X mask, Y mask}
 constexpr uint32_t kSmTri = kSmEdge + kEdgeN * 8;      // [4][kTriN] {X mask, Y mask}
@@ -143,7 +149,8 @@ struct Half4 {
 };
 
 struct State4 {
-  uint32_t X, Y, DXp, q, prp, wp, res;
+  uint32_t X, Y, DXp, q, prp, res;
+  uint32_t up;  // the row above of row 0 for the next step (shuffled a step ahead)
 };
 
 // Multiplier constants passed at run time, so that the adds stay
@@ -152,67 +159,95 @@ struct K4 {
   uint32_t one, m1, four;
 };
 
-// 16 steps of one block half.  Per step: one shuffle up (the row above),
-// the queue rotation, the window-word and profile-word loads, four byte
-// permutes, and per register a 32-bit add (delete candidate) and two 16x2
-// add-mins; in kDpChoice the 2-bit ranks of both halves go into the
-// direction words (eight steps per word) and are cleared from the values.
+// 16 steps of one block half.  Per step: the shuffle of the row above for
+// the next step, the queue rotation, the window-word and profile-word
+// loads, four byte permutes, and per register one 32-bit add (insert
+// candidate, both halves) and two 16x2 add-mins: min(align, insert) first,
+// then the delete term.  In kDpChoice the 2-bit ranks of both halves go
+// into the direction words (eight steps per word) and are cleared from the
+// values.
 template <int MODE, int KIND>
 __device__ __forceinline__ void l4_half(State4 &S, const Half4 &H, uint32_t lane4, int lane,
                                          int qsrc, bool capY, const K4 &K, uint32_t &ax0,
                                          uint32_t &ax1, uint32_t &ay0, uint32_t &ay1) {
+  // The shared loads run ahead of their step (the asm loads keep source
+  // order): window words two steps ahead, profile and mask words one.
+  auto waddr = [&](int v) -> uint32_t {
+    return ((KIND == kPlain || v >= H.sw) ? H.wn : H.wo) + 8 * v;
+  };
+  uint2 wq0 = lds64(waddr(0)), wq1 = lds64(waddr(1));
+  uint32_t pq0 = lds32(add_fma(wq0.x, lane4, K.one));
+  uint2 fq = make_uint2(0, 0), tq = make_uint2(0, 0);
+  if (KIND >= kMixed) fq = lds64(H.fe);
+  if (KIND >= kSlow) tq = lds64(H.ft);
 #pragma unroll
   for (int v = 0; v < 16; ++v) {
+    const uint2 w = wq0;
+    const uint32_t pr = pq0;
+    const uint2 fe = fq, ft = tq;
+    wq0 = wq1;
+    if (v + 2 < 16) wq1 = lds64(waddr(v + 2));
+    if (v + 1 < 16) {
+      pq0 = lds32(add_fma(wq0.x, lane4, K.one));
+      if (KIND >= kMixed) fq = lds64(H.fe + 8 * (v + 1));
+      if (KIND >= kSlow) tq = lds64(H.ft + 8 * (v + 1));
+    }
+    const uint32_t up = S.up;
+    // lane k-1's current Y feeds lane k's row 0 at the next step; lane 0
+    // takes the boundary queue's next value after the rotation
     const uint32_t recv = __shfl_up_sync(kFull4, S.Y, 1);
-    const uint32_t up = (lane == 0) ? S.q : recv;
     S.q = __shfl_sync(kFull4, S.q, qsrc);
+    S.up = (lane == 0) ? S.q : recv;
     const bool nw = KIND == kPlain || v >= H.sw;
-    const uint32_t w = lds32((nw ? H.wn : H.wo) + 4 * v);
-    const uint32_t pr = lds32((w & 0xFFFFFFu) | lane4);
-    const uint32_t DX = prmt(up, S.Y, 0x5432);     // {row above row 0, row 1}
     const uint32_t caX = prmt(pr, S.prp, 0xE680);  // {row 0 vs c(u), row 2 vs c(u-1)}
     const uint32_t caY = prmt(pr, S.prp, 0xF791);  // {row 1 vs c(u), row 3 vs c(u-1)}
-    const uint32_t ci = prmt(w, S.wp, 0xF7B3);     // {g(c(u)), g(c(u-1))}
+    const uint32_t ci = w.y;                       // {g(c(u)), g(c(u-1))}
     const uint32_t cdX = nw ? H.cdXn : H.cdXo, cdY = nw ? H.cdYn : H.cdYo;
     uint32_t mX = 0, mY = 0;
     if (KIND >= kMixed) {
-      const uint2 fe = lds64(H.fe + 8 * v);
       mX = fe.x;
       mY = fe.y;
     }
     if (KIND >= kSlow) {
-      const uint2 ft = lds64(H.ft + 8 * v);
       const bool on = v >= H.tg;
       mX |= on ? ft.x : 0u;
       mY |= on ? ft.y : 0u;
     }
     // X = {row 0, row 2}: align from the previous delete operand, insert
-    // from the own previous value, delete from DX
-    uint32_t t = add_fma(DX, cdX, K.one);
-    t = __viaddmin_u16x2(S.X, ci, t);
-    uint32_t Xn = __viaddmin_u16x2(S.DXp, caX, t);
+    // from the own previous value; Y = {row 1, row 3}: align from the
+    // previous X, insert from the own previous value
+    const uint32_t tX = __viaddmin_u16x2(S.DXp, caX, add_fma(S.X, ci, K.one));
+    const uint32_t tY = __viaddmin_u16x2(S.X, caY, add_fma(S.Y, ci, K.one));
+    const uint32_t DX = prmt(up, S.Y, 0x5432);  // {row above row 0, row 1}
+    uint32_t Xn = __viaddmin_u16x2(DX, cdX, tX);
     if (MODE == kDpChoice) {
-      const uint32_t r = Xn & 0x00030003u;
+      // clear the rank bits (one LOP on the dependency chain); the rank
+      // itself, old - cleared, and its accumulation stay on the FMA pipe
+      const uint32_t Xc = Xn & 0xFFFCFFFCu;
+      uint32_t r;
+      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(Xc), "r"(K.m1), "r"(Xn));
       if (v < 8) {
         asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(ax0) : "r"(ax0), "r"(K.four), "r"(r));
       } else {
         asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(ax1) : "r"(ax1), "r"(K.four), "r"(r));
       }
-      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(Xn) : "r"(r), "r"(K.m1), "r"(Xn));
+      Xn = Xc;
     }
     if (KIND >= kMixed) Xn = force_inf(Xn, mX);
-    // Y = {row 1, row 3}: delete from the fresh X, align from the previous X
-    t = add_fma(Xn, cdY, K.one);
-    t = __viaddmin_u16x2(S.Y, ci, t);
-    uint32_t Yn = __viaddmin_u16x2(S.X, caY, t);
+    // Y's delete predecessors are X's fresh values
+    uint32_t Yn = __viaddmin_u16x2(Xn, cdY, tY);
     if (MODE == kDpChoice) {
-      const uint32_t r = Yn & 0x00030003u;
+      // clear the rank bits (one LOP on the dependency chain); the rank
+      // itself, old - cleared, and its accumulation stay on the FMA pipe
+      const uint32_t Yc = Yn & 0xFFFCFFFCu;
+      uint32_t r;
+      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(Yc), "r"(K.m1), "r"(Yn));
       if (v < 8) {
         asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(ay0) : "r"(ay0), "r"(K.four), "r"(r));
       } else {
         asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(ay1) : "r"(ay1), "r"(K.four), "r"(r));
       }
-      asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(Yn) : "r"(r), "r"(K.m1), "r"(Yn));
+      Yn = Yc;
     }
     if (KIND >= kMixed) Yn = force_inf(Yn, mY);
     if (KIND == kSlowCap && v == H.fv) S.res = capY ? Yn : Xn;
@@ -221,7 +256,6 @@ __device__ __forceinline__ void l4_half(State4 &S, const Half4 &H, uint32_t lane
     S.X = Xn;
     S.Y = Yn;
     S.prp = pr;
-    S.wp = w;
   }
 }
 
@@ -262,16 +296,15 @@ __device__ __forceinline__ void build4(uint32_t sb, uint32_t prof0, const uint8_
   cdY = cd[1] | (cd[3] << 16);
 }
 
-// Window word of the column a lane reads at window position p of the
-// block at offset o of period t0, in strip ts (t0 or t0 - 1):
-// {insert cost g(c) in the top byte, shared address of profile row c of
-// the strip's parity buffer}.  Column j = 128 ts + dlo + (t0 - ts) W + o -
-// 63 + p; lane k reads p = v - 2k + 63 at step v.
+// Window entry of the column a lane reads at window position p of the
+// block at offset o of period t0, in strip ts (t0 or t0 - 1): {shared
+// address of profile row c of the strip's parity buffer, the insert costs
+// g(c_p) | g(c_{p-1}) << 16 of this column and the one before, which are
+// the row pairs' insert operands of that step}.  Column j = 128 ts + dlo +
+// (t0 - ts) W + o - 93 + p; lane k reads p = v - 3k + 93 at step v (8-byte
+// entries 24 bytes apart: no bank conflict within a half warp).
 __device__ __forceinline__ int win_col(const Geo4 &g, int ts, int t0, int o, int p) {
-  return 128 * ts + g.dlo + (t0 - ts) * g.W + o - 63 + p;
-}
-__device__ __forceinline__ uint32_t win_word(uint32_t gt, uint32_t prof0, int ts, int c) {
-  return (lds32(gt + 4 * c) << 24) | (prof0 + (uint32_t)(ts & 1) * 4096u + 128u * c);
+  return 128 * ts + g.dlo + (t0 - ts) * g.W + o - k4WinBase + p;
 }
 
 template <int MODE>
@@ -288,7 +321,7 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
   const int rank_d = MODE == kDpChoice ? 3 - rank_i : 0;
   const uint32_t gt = sb + kSmGt + 128u * rank_i;
   const uint32_t prof0 = sb + kSmProf + 8192u * warp;
-  const uint32_t win0 = sb + kSmWin + 768u * warp;
+  const uint32_t win0 = sb + kSmWin + 16u * k4Win * warp;
   const uint32_t lane4 = 4u * lane;
   const int qsrc = (lane + 1) & 31;
   const K4 K{(uint32_t)A.k.one, (uint32_t)A.k.m1, (uint32_t)A.k.four};
@@ -308,24 +341,30 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
     if (x == g.W) x = 0;
     return x < g.wd ? bnd[x] : (kInf16 << 16);
   };
-  // window chars of the block at (t0, o): positions lane, lane+32, lane+64
-  // of the new strip (t0) and of the old one (t0 - 1)
-  auto wchars = [&](int t0, int o, int (&cn)[3], int (&co)[3]) {
+  // window chars of the block at (t0, o): positions lane + 32 i of the new
+  // strip (t0) and of the old one (t0 - 1)
+  // (chars of positions p and p - 1: ch[i][0..1] new strip, ch[i][2..3] old)
+  auto wchars = [&](int t0, int o, int (&ch)[4][4]) {
+    auto col = [&](int j) { return (j >= 0 && j < g.L2) ? (int)s2[j] : gap; };
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 4; ++i) {
       const int p = lane + 32 * i;
       const int jn = win_col(g, t0, t0, o, p), jo = win_col(g, t0 - 1, t0, o, p);
-      cn[i] = (jn >= 0 && jn < g.L2) ? (int)s2[jn] : gap;
-      co[i] = (jo >= 0 && jo < g.L2) ? (int)s2[jo] : gap;
+      ch[i][0] = col(jn);
+      ch[i][1] = col(jn - 1);
+      ch[i][2] = col(jo);
+      ch[i][3] = col(jo - 1);
     }
   };
-  auto wstore = [&](int t0, const int (&cn)[3], const int (&co)[3]) {
+  auto wstore = [&](int t0, const int (&ch)[4][4]) {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
+    for (int i = 0; i < 4; ++i) {
       const int p = lane + 32 * i;
-      if (p < 96) {
-        sts32(win0 + 4u * p, win_word(gt, prof0, t0, cn[i]));
-        sts32(win0 + 384u + 4u * p, win_word(gt, prof0, t0 - 1, co[i]));
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {  // new strip t0, old strip t0 - 1
+        const int c = ch[i][2 * h], cp = ch[i][2 * h + 1];
+        const uint32_t pa = prof0 + (uint32_t)((t0 - h) & 1) * 4096u + 128u * c;
+        sts64(win0 + 8u * (h * k4Win + p), pa, lds32(gt + 4 * c) | (lds32(gt + 4 * cp) << 16));
       }
     }
   };
@@ -334,13 +373,13 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
   S.X = S.Y = kInf2;
   S.DXp = lane == 0 ? ((kInf16 << 16) | (bnd[0] >> 16)) : kInf2;
   S.prp = 0;
-  S.wp = 0;
   S.res = 0;
   S.q = qload(0, 0);
+  S.up = lane == 0 ? S.q : kInf2;
   {
-    int cn[3], co[3];
-    wchars(0, 0, cn, co);
-    wstore(0, cn, co);
+    int ch[4][4];
+    wchars(0, 0, ch);
+    wstore(0, ch);
   }
   __syncwarp();
 
@@ -350,7 +389,7 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
   const int Gf = (rf >> 7) * g.W + k4Lag * kf + lam4(mf) + (g.L2 - 1 - rf - g.dlo);
   const bool capY = (mf & 1) != 0;
   uint32_t *dm = MODE == kDpChoice ? A.dm + dm_off : nullptr;
-  const int slow_end0 = max(-g.dlo + 62, k4R3);
+  const int slow_end0 = max(-g.dlo + (k4Lag - 4) * 31 + 1, k4R3);
 
   int t0 = 0, o = 0;
   for (int b = 0; b < g.nblk; ++b, o += 32) {
@@ -363,13 +402,13 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
       cdYc = cdYn;
     }
     const int G0 = 32 * b;
-    // every lane is in strip t0 from step 186 on: its parity buffer's
+    // every lane is in strip t0 from step 217 on: its parity buffer's
     // other half (strip t0 - 1) is free for strip t0 + 1
-    if (o == 192) build4<MODE>(sb, prof0, s1, g, t0 + 1, lane, gap, rank_d, true, cdXn, cdYn);
+    if (o == 224) build4<MODE>(sb, prof0, s1, g, t0 + 1, lane, gap, rank_d, true, cdXn, cdYn);
     const int o1 = (o + 32 == g.W) ? 0 : o + 32, t1 = (o1 == 0) ? t0 + 1 : t0;
     const uint32_t qn = qload(t1, o1);
-    int cn[3], co[3];
-    wchars(t1, o1, cn, co);
+    int ch[4][4];
+    wchars(t1, o1, ch);
 
     int kind = kPlain;
     if (o + 31 >= g.W - g.G || o <= k4R3) kind = kMixed;
@@ -377,9 +416,9 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
     if ((Gf >> 5) == b) kind = kSlowCap;
 
     Half4 H;
-    H.sw = k4Lag * lane - o;  // t0 W + 6k - G0
-    H.wn = win0 + 4u * (uint32_t)(63 - 2 * lane);
-    H.wo = H.wn + 384u;
+    H.sw = k4Lag * lane - o;  // t0 W + 7k - G0
+    H.wn = win0 + 8u * (uint32_t)(k4WinBase - 3 * lane);
+    H.wo = H.wn + 8u * k4Win;
     H.cdXn = cdXc;
     H.cdYn = cdYc;
     H.cdXo = cdXp;
@@ -418,8 +457,8 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
       H.sw -= 16;
       H.tg -= 16;
       H.fv -= 16;
-      H.wn += 64u;
-      H.wo += 64u;
+      H.wn += 128u;  // 16 window positions
+      H.wo += 128u;
       H.fe += 128u;
       H.ft += 128u;
     }
@@ -432,8 +471,9 @@ __device__ __forceinline__ void lin4_pair(const LinDpArgs &A, uint32_t sb, int w
       if (pstep >= 0 && x < g.wd) bnd[x] = S.q;
     }
     S.q = qn;
+    if (lane == 0) S.up = qn;  // lane 0's first input of the next block
     __syncwarp();
-    wstore(t1, cn, co);
+    wstore(t1, ch);
     __syncwarp();
   }
   const uint32_t res = __shfl_sync(kFull4, S.res, kf);
