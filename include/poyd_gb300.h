@@ -352,6 +352,20 @@ int poyd_sank_median_batch(const int32_t *nodes, int32_t nchar, int32_t k,
                            const int32_t *tcm, int32_t n, const int32_t *a_idx,
                            const int32_t *b_idx, int32_t *out_s,
                            int32_t *out_e, int32_t *out_beta, void *stream);
+/* SankCS.median_3 / elt_median_3 (sankCS.ml:402-452, called by the
+ * uppass, node.ml:478 and allDirChar.ml:1399-1424), per pair i and
+ * character: the final e row and best-state bits of node node[i] from its
+ * ancestor's final (fin_e / fin_best rows anc[i]: int32 [nchar][k] and
+ * [nchar], a bit per state), its preliminary s row (nodes[node[i]]) and its
+ * children's preliminary s rows (nodes[left[i]], nodes[right[i]]; a leaf
+ * passes itself).  An ancestor's best-state bits must be non-zero (the
+ * root's final holds its cheapest states).  Writes out_e [n][nchar][k] and
+ * out_best [n][nchar]. */
+int poyd_sank_median_3_batch(const int32_t *nodes, const int32_t *fin_e,
+                             const int32_t *fin_best, int32_t nchar, int32_t k,
+                             const int32_t *tcm, int32_t n, const int32_t *anc,
+                             const int32_t *node, const int32_t *left, const int32_t *right,
+                             int32_t *out_e, int32_t *out_best, void *stream);
 /* SankCS.distance (sankCS.ml:371-377) per candidate as the integer sum of
  * per-character (min c - min a.s - min b.s); dist[i] is int64. */
 int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int32_t k,

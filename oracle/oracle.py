@@ -133,6 +133,8 @@ def lib():
             getattr(L, "or_nonadd%d_median_3" % w).argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
         L.or_sank_elt_median.argtypes = [C.c_int, i64p, i64p, i64p, i64p, i64p, i64p]
         L.or_sank_elt_distance.argtypes = [C.c_int, i64p, i64p, i64p]
+        L.or_sank_elt_median_3.argtypes = [C.c_int, i64p, i64p, i64p, C.c_uint32, i64p, i64p,
+                                           i64p, i64p, C.POINTER(C.c_uint32)]
         L.or_sank_elt_distance.restype = C.c_double
         _lib = L
     return _lib
@@ -383,6 +385,21 @@ def sank_elt_median(tcm, a_s, b_s):
     lib().or_sank_elt_median(k, _ptr(tcm, i64p), _ptr(a_s, i64p), _ptr(b_s, i64p),
                              _ptr(c, i64p), _ptr(e, i64p), _ptr(beta, i64p))
     return c, e, beta
+
+
+def sank_elt_median_3(tcm, a_s, a_e, a_best, n_s, l_s, r_s):
+    """elt_median_3: (final e, best-state bits) of a node from its
+    ancestor's final (a_e, a_best bits; 0 = the cheapest states of a_s), its
+    preliminary s and its children's preliminary s."""
+    tcm = np.ascontiguousarray(tcm, np.int64)
+    a_s, a_e, n_s, l_s, r_s = (np.ascontiguousarray(x, np.int64) for x in (a_s, a_e, n_s, l_s, r_s))
+    k = len(n_s)
+    e = np.zeros(k, np.int64)
+    best = C.c_uint32()
+    lib().or_sank_elt_median_3(k, _ptr(tcm, i64p), _ptr(a_s, i64p), _ptr(a_e, i64p),
+                               int(a_best), _ptr(n_s, i64p), _ptr(l_s, i64p), _ptr(r_s, i64p),
+                               _ptr(e, i64p), C.byref(best))
+    return e, int(best.value)
 
 
 def sank_elt_distance(tcm, a_s, b_s):

@@ -957,6 +957,75 @@ void or_sank_elt_median(int k, const int64_t *tcm, const int64_t *a_s,
     }
 }
 
+/* Goloboff's beta of a preliminary cost vector s: e = s - min s with an
+ * infinite state staying infinite (canonize, sankCS.ml:254-271, and
+ * elt_median's e, whose max_int for an infinite state is infinite under
+ * +$), then beta[y] = min_x tcm[y][x] +$ e[x]. */
+static void or_sank_beta(int k, const int64_t *tcm, const int64_t *s, int64_t *beta) {
+    int64_t e[64], mn = OR_SANK_INF;
+    int x, y;
+    for (x = 0; x < k; x++) if (s_less(s[x], mn)) mn = s[x];
+    for (x = 0; x < k; x++) e[x] = s_isinf(s[x]) ? OR_SANK_INF : s_minus(s[x], mn);
+    for (y = 0; y < k; y++) {
+        int64_t best = OR_SANK_INF;
+        for (x = k - 1; x >= 0; x--) {
+            int64_t v = s_isinf(e[x]) ? e[x] : s_plus(e[x], tcm[y * k + x]);
+            if (s_less(v, best)) best = v;
+        }
+        beta[y] = best;
+    }
+}
+
+/* elt_median_3 (sankCS.ml:402-452): the final e and best states of node n
+ * from its ancestor's final (a_e; a_best, a bit per state, 0 when the
+ * ancestor has none, then its cheapest states of a_s are used), the node's
+ * preliminary s (n_s) and the children's preliminary cost vectors (their
+ * beta as in or_sank_beta).  Writes e_out[k] and the best-state bits. */
+void or_sank_elt_median_3(int k, const int64_t *tcm, const int64_t *a_s, const int64_t *a_e,
+                          uint32_t a_best, const int64_t *n_s, const int64_t *l_s,
+                          const int64_t *r_s, int64_t *e_out, uint32_t *best_out) {
+    int64_t lb[64], rb[64], bst[64];
+    int i, s, x, pos;
+    uint32_t abest = a_best, mine = 0;
+    int64_t best_cost = OR_SANK_INF;
+    or_sank_beta(k, tcm, l_s, lb);
+    or_sank_beta(k, tcm, r_s, rb);
+    for (i = 0; i < k; i++) {  /* init_d': the best over x for ancestor state i */
+        int64_t b = OR_SANK_INF;
+        for (x = k - 1; x >= 0; x--) {
+            int64_t v = s_plus(s_plus(tcm[i * k + x], lb[x]), rb[x]);
+            if (s_less(v, b)) b = v;
+        }
+        bst[i] = b;
+    }
+    for (s = 0; s < k; s++) {  /* init_e: min over ancestor states of d'[i][s] */
+        int64_t b = OR_SANK_INF;
+        for (x = k - 1; x >= 0; x--) {
+            int64_t d = s_minus(s_plus(s_plus(s_plus(a_e[x], tcm[x * k + s]), lb[s]), rb[s]), bst[x]);
+            if (s_less(d, b)) b = d;
+        }
+        e_out[s] = b;
+    }
+    if (!abest) {  /* the ancestor's cheapest states (plain comparisons) */
+        int64_t c = OR_SANK_INF;
+        for (pos = 0; pos < k; pos++) {
+            if (c == a_s[pos]) abest |= 1u << pos;
+            else if (c > a_s[pos]) { c = a_s[pos]; abest = 1u << pos; }
+        }
+    }
+    for (pos = 0; pos < k; pos++) {  /* mybest: plain + and min, from infinity */
+        int64_t mc = OR_SANK_INF;
+        for (x = 0; x < k; x++)
+            if ((abest >> x) & 1u) {
+                int64_t v = n_s[pos] + tcm[pos * k + x];
+                if (v < mc) mc = v;
+            }
+        if (mc == best_cost) mine |= 1u << pos;
+        else if (mc < best_cost) { best_cost = mc; mine = 1u << pos; }
+    }
+    *best_out = mine;
+}
+
 double or_sank_elt_distance(int k, const int64_t *tcm, const int64_t *a_s, const int64_t *b_s) {
     /* elt_distance (sankCS.ml:347-354) */
     int64_t c[64], e[64], beta[64];

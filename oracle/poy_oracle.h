@@ -189,6 +189,12 @@ void or_nonadd32_median_3(const uint32_t *A, const uint32_t *N, const uint32_t *
 /* elt_median over k states: a_s, b_s -> c (s), e, beta; tcm is k x k. */
 void or_sank_elt_median(int k, const int64_t *tcm, const int64_t *a_s,
                         const int64_t *b_s, int64_t *c, int64_t *e, int64_t *beta);
+/* elt_median_3 (sankCS.ml:402-452): final e and best-state bits of a node
+ * from its ancestor's final (a_e, a_best; a_best 0: the ancestor's cheapest
+ * states of a_s), its preliminary s and its children's preliminary s. */
+void or_sank_elt_median_3(int k, const int64_t *tcm, const int64_t *a_s, const int64_t *a_e,
+                          uint32_t a_best, const int64_t *n_s, const int64_t *l_s,
+                          const int64_t *r_s, int64_t *e_out, uint32_t *best_out);
 /* elt_distance as a float (sankCS.ml:347-354). */
 double or_sank_elt_distance(int k, const int64_t *tcm, const int64_t *a_s,
                             const int64_t *b_s);

@@ -188,6 +188,102 @@ __global__ void k_sank_median(const int32_t *nodes, int nchar, const int32_t *tc
   }
 }
 
+// Goloboff's beta of a preliminary cost vector: e = s - min s (an infinite
+// state stays infinite; canonize, sankCS.ml:254-271, and elt_median's e,
+// whose max_int is infinite under +$), beta[y] = min_x tcm[y][x] +$ e[x].
+template <int K>
+__device__ __forceinline__ void sank_beta(const int *tcm, const int *s, int *beta) {
+  int mn = kSInf, e[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) mn = s[i] < mn ? s[i] : mn;
+#pragma unroll
+  for (int i = 0; i < K; ++i) e[i] = s[i] >= kSInf ? kSInf : s[i] - mn;
+#pragma unroll
+  for (int y = 0; y < K; ++y) {
+    int best = kSInf;
+#pragma unroll
+    for (int x = 0; x < K; ++x) {
+      const int v = sadd(tcm[y * K + x], e[x]);
+      best = v < best ? v : best;
+    }
+    beta[y] = best;
+  }
+}
+
+// elt_median_3 (sankCS.ml:402-452) for one (node, character): the node's
+// final e and best states from its ancestor's final (e, best-state bits),
+// its preliminary s and its children's preliminary s (their beta).
+template <int K>
+__global__ void k_sank_median3(const int32_t *nodes, const int32_t *fin_e,
+                               const int32_t *fin_best, int nchar, const int32_t *tcm_g, int n,
+                               const int32_t *anc, const int32_t *node, const int32_t *left,
+                               const int32_t *right, int32_t *out_e, int32_t *out_best) {
+  __shared__ int tcm[K * K];
+  for (int t = threadIdx.x; t < K * K; t += blockDim.x) tcm[t] = tcm_g[t];
+  __syncthreads();
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (int64_t)n * nchar) return;
+  const int c = (int)(g / nchar), ch = (int)(g % nchar);
+  const int32_t *ae_p = fin_e + ((int64_t)anc[c] * nchar + ch) * K;
+  const int32_t *ns_p = nodes + ((int64_t)node[c] * nchar + ch) * K;
+  const int32_t *ls_p = nodes + ((int64_t)left[c] * nchar + ch) * K;
+  const int32_t *rs_p = nodes + ((int64_t)right[c] * nchar + ch) * K;
+  const uint32_t abest = (uint32_t)fin_best[(int64_t)anc[c] * nchar + ch];
+  int ae[K], ns[K], ls[K], rs[K], lb[K], rb[K], bst[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    ae[i] = ae_p[i];
+    ns[i] = ns_p[i];
+    ls[i] = ls_p[i];
+    rs[i] = rs_p[i];
+  }
+  sank_beta<K>(tcm, ls, lb);
+  sank_beta<K>(tcm, rs, rb);
+#pragma unroll
+  for (int i = 0; i < K; ++i) {  // init_d': best over x for ancestor state i
+    int b = kSInf;
+#pragma unroll
+    for (int x = 0; x < K; ++x) {
+      const int v = sadd(sadd(tcm[i * K + x], lb[x]), rb[x]);
+      b = v < b ? v : b;
+    }
+    bst[i] = b;
+  }
+  const int64_t o = ((int64_t)c * nchar + ch) * K;
+#pragma unroll
+  for (int s = 0; s < K; ++s) {  // init_e: min over ancestor states of d'[i][s]
+    int b = kSInf;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int d = sadd(sadd(sadd(ae[i], tcm[i * K + s]), lb[s]), rb[s]);
+      // -$: an infinite minuend is infinite here, an infinite subtrahend gives 0
+      const int v = d >= kSInf ? kSInf : (bst[i] >= kSInf ? 0 : d - bst[i]);
+      b = v < b ? v : b;
+    }
+    out_e[o + s] = b;
+  }
+  // best states: the node's states cheapest against the ancestor's best
+  // states (plain + and min from infinity; every final has a best state)
+  int best_cost = kSInf;
+  uint32_t mine = 0;
+#pragma unroll
+  for (int pos = 0; pos < K; ++pos) {
+    int mc = kSInf;
+#pragma unroll
+    for (int x = 0; x < K; ++x)
+      if ((abest >> x) & 1u) {
+        const int v = ns[pos] + tcm[pos * K + x];
+        mc = v < mc ? v : mc;
+      }
+    if (mc == best_cost) mine |= 1u << pos;
+    else if (mc < best_cost) {
+      best_cost = mc;
+      mine = 1u << pos;
+    }
+  }
+  out_best[(int64_t)c * nchar + ch] = (int32_t)mine;
+}
+
 template <int K>
 __global__ void k_sank_distance(const int32_t *nodes, int nchar, const int32_t *tcm_g, int n,
                                 const int32_t *ai, const int32_t *bi, int64_t *dist) {
@@ -314,6 +410,34 @@ extern "C" int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   ProfScope ps("sank_distance", st);
 #define L(KV) k_sank_distance<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, dist)
+  switch (k) {
+    SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
+    SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)
+  }
+#undef L
+  FS_CK(cudaGetLastError());
+  return POYD_OK;
+}
+
+extern "C" int poyd_sank_median_3_batch(const int32_t *nodes, const int32_t *fin_e,
+                                        const int32_t *fin_best, int32_t nchar, int32_t k,
+                                        const int32_t *tcm, int32_t n, const int32_t *anc,
+                                        const int32_t *node, const int32_t *left,
+                                        const int32_t *right, int32_t *out_e,
+                                        int32_t *out_best, void *stream) {
+  if (k < 2 || k > 8) return fail(POYD_EUNSUP, "Sankoff characters need 2..8 states");
+  if (n < 0 || nchar < 0) return fail(POYD_EINVAL, "negative size");
+  if (n == 0 || nchar == 0) return POYD_OK;
+  if (!nodes || !fin_e || !fin_best || !tcm || !anc || !node || !left || !right || !out_e ||
+      !out_best)
+    return fail(POYD_EINVAL, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t total = (int64_t)n * nchar;
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  ProfScope ps("sank_median3", st);
+#define L(KV)                                                                              \
+  k_sank_median3<KV><<<blocks, 256, 0, st>>>(nodes, fin_e, fin_best, nchar, tcm, n, anc, node, \
+                                             left, right, out_e, out_best)
   switch (k) {
     SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
     SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)

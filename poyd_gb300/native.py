@@ -57,7 +57,7 @@ EXPORTED = (
     "poyd_nonadd32_median_batch", "poyd_nonadd8_distance_batch", "poyd_nonadd8_median_3_batch",
     "poyd_nonadd8_median_batch", "poyd_pack_alignments", "poyd_profile_enable",
     "poyd_profile_read", "poyd_relu_grad_bf16", "poyd_sank_distance_batch",
-    "poyd_sank_median_batch", "poyd_to_bf16", "poyd_verify_2_batch", "poyd_version",
+    "poyd_sank_median_3_batch", "poyd_sank_median_batch", "poyd_to_bf16", "poyd_verify_2_batch", "poyd_version",
     "poyd_worst_2_batch",
 )
 

@@ -451,6 +451,67 @@ class GpuBackend:
         s = self.sank[v]
         return int(torch.clamp(s.min(dim=1).values, max=native.SANK_INF).to(torch.int64).sum().item())
 
+    # -- final states of the non-DO characters (uppass) ---------------------
+    def final_slots(self, n_slots: int, fitch_base: int):
+        """Room for n_slots final states: Fitch finals in node rows
+        fitch_base + slot (the median_3 kernel reads ancestors from the node
+        rows), Sankoff finals (e rows, best-state bits) in their own arrays."""
+        self.ensure_nodes(fitch_base + n_slots)
+        self.fin_base = fitch_base
+        if self.ns:
+            self.fin_e = torch.zeros((n_slots, self.ns, self.k), dtype=torch.int32, device=self.dev)
+            self.fin_best = torch.zeros((n_slots, self.ns), dtype=torch.int32, device=self.dev)
+
+    def final_root(self, node: int, slot: int):
+        """The root's final: its preliminary state (a median's final is its
+        preliminary, node.ml:270-290); a Sankoff root's best states are its
+        cheapest states (elt_median_3 takes them when none are set,
+        sankCS.ml:423-436)."""
+        if self.nf:
+            self.fitch[self.fin_base + slot] = self.fitch[node]
+        if self.ns:
+            s = self.sank[node, :self.ns]
+            mn = s.min(dim=1, keepdim=True).values
+            self.fin_e[slot] = torch.where(s >= native.SANK_INF, native.SANK_INF, s - mn)
+            bits = (s == mn).to(torch.int32) << torch.arange(self.k, device=self.dev, dtype=torch.int32)
+            self.fin_best[slot] = bits.sum(dim=1).to(torch.int32)
+
+    def final_states(self, anc, node, left, right, out):
+        """Finals of slots out_i from the ancestors' finals (slots anc_i), the
+        nodes' preliminary states and their children's (node ids; a leaf
+        passes itself): NonaddCS median_3 (nonaddCSc.c:472-544) and SankCS
+        median_3 (sankCS.ml:402-452), as node.ml's cs_median_3 (459-486)."""
+        n = len(out)
+        if n == 0:
+            return
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L = native.lib()
+        t = lambda x: torch.from_numpy(np.ascontiguousarray(x, np.int32)).to(self.dev)
+        ia, inode, il, ir = t(anc), t(node), t(left), t(right)
+        io = torch.from_numpy(np.asarray(out, np.int64)).to(self.dev)
+        if self.nf:
+            tmp = torch.empty((n, self.stride), dtype=torch.uint8, device=self.dev)
+            native.check(L.poyd_nonadd8_median_3_batch(
+                _p(self.fitch), C.c_int64(self.stride), self.nf, n, _p(ia + self.fin_base),
+                _p(inode), _p(il), _p(ir), _p(tmp), st))
+            self.fitch[io + self.fin_base] = tmp
+        if self.ns:
+            e = torch.empty((n, self.ns, self.k), dtype=torch.int32, device=self.dev)
+            b = torch.empty((n, self.ns), dtype=torch.int32, device=self.dev)
+            native.check(L.poyd_sank_median_3_batch(
+                _p(self.sank), _p(self.fin_e), _p(self.fin_best), self.ns, self.k, _p(self.tcm),
+                n, _p(ia), _p(inode), _p(il), _p(ir), _p(e), _p(b), st))
+            self.fin_e[io] = e
+            self.fin_best[io] = b
+
+    def node_final(self, slot: int):
+        """(Fitch final row, Sankoff final e rows, best-state bits) of a slot."""
+        f = self.fitch[self.fin_base + slot, :self.nf].cpu().numpy() if self.nf else \
+            np.zeros(0, np.uint8)
+        if self.ns:
+            return f, self.fin_e[slot].cpu().numpy(), self.fin_best[slot].cpu().numpy()
+        return f, np.zeros((0, self.k), np.int32), np.zeros(0, np.int32)
+
     def node_seq(self, v: int) -> np.ndarray:
         o, l = int(self.off[v]), int(self.len[v])
         return self.pool[o:o + l].cpu().numpy()
@@ -1050,9 +1111,12 @@ class FinalCost:
     cost: int           # the tree cost the reference reports
     root_edge: tuple    # (a, b): a on the handle's side
     root_cost: int      # the best rooting's downpass cost (pick_best_root)
+    # with states=True: per backend, {vertex: (Fitch final row, Sankoff
+    # final e rows, Sankoff best-state bits)} of the non-DO characters
+    finals: list = field(default_factory=list)
 
 
-def final_cost(tree: Tree, be, weight: int = 1) -> FinalCost:
+def final_cost(tree: Tree, be, weight: int = 1, states: bool = False) -> FinalCost:
     """The tree cost the reference reports after a diagnosis
     (``Ptree.get_cost `Adjusted``, poy_test.ml:43): ``pick_best_root``
     (see :func:`root_costs`), then ``assign_single``
@@ -1077,7 +1141,11 @@ def final_cost(tree: Tree, be, weight: int = 1) -> FinalCost:
     (weightfactor:w)``; node costs are ``weight * cost``, node.ml:350-357).
     The root is chosen by absolute cost (allDirChar.ml:794), so the
     rooting and the single sequences do not depend on it and it scales
-    every cost."""
+    every cost.
+
+    With `states`, the non-DO characters' final states are assigned too
+    (``assign_final_states``, allDirChar.ml:1377-1428) and returned in
+    ``FinalCost.finals``; they do not change the cost."""
     bes = list(be) if isinstance(be, (list, tuple)) else [be]
     Ds = [_all_directions(tree, b) for b in bes]
     if Ds[0] is None:
@@ -1093,10 +1161,47 @@ def final_cost(tree: Tree, be, weight: int = 1) -> FinalCost:
     else:
         a, b = (int(x) for x in tree.kids[tree.root])
     cost = 0
+    finals = []
     for B, D in zip(bes, Ds):
         cost += _assign_single_cost(B, D, k, a, b)
+        if states:
+            finals.append(_assign_final_states(B, D, k, a, b, tree.n))
         B.release_nodes(2 * tree.n)
-    return FinalCost(weight * cost, (int(a), int(b)), weight * int(tot[k]))
+    return FinalCost(weight * cost, (int(a), int(b)), weight * int(tot[k]), finals)
+
+
+def _assign_final_states(be, D: _AllDir, k: int, a: int, b: int, n: int) -> dict:
+    """assign_final_states (allDirChar.ml:1377-1428) for the non-DO
+    characters, from root edge k = (a, b): the root median's final is its
+    preliminary; a and b, then every vertex away from them, take
+    median_3(parent's final, own preliminary state seen from the parent,
+    the two children's preliminary states seen from it) -- a leaf passes
+    itself as both children -- one batch per distance from the root.
+    Returns {vertex: (Fitch row, Sankoff e rows, Sankoff best bits)}."""
+    if not (getattr(be, "nf", 0) or getattr(be, "ns", 0)):
+        return {}
+    root_slot = 2 * n - 1               # vertex ids stop at 2n - 2
+    be.final_slots(2 * n, D.next_id + 2 + 2 * n)
+    be.final_root(int(D.root_ids[k]), root_slot)
+    front = [(a, b, root_slot), (b, a, root_slot)]
+    done = []
+    while front:
+        anc = np.array([f[2] for f in front], np.int64)
+        node, left, right = [], [], []
+        for c, p, _ in front:
+            x = D.info[(c, p)]
+            node.append(x[2])
+            if x[3] is None:  # a leaf: median_3 par cur cur cur
+                left.append(x[2])
+                right.append(x[2])
+            else:
+                left.append(D.info[x[3][0]][2])
+                right.append(D.info[x[3][1]][2])
+        out = np.array([c for c, _, _ in front], np.int64)
+        be.final_states(anc, np.array(node), np.array(left), np.array(right), out)
+        done.extend(out.tolist())
+        front = [(x, c, c) for c, p, _ in front for x in D.adj[c] if x != p]
+    return {int(v): be.node_final(int(v)) for v in done}
 
 
 def _assign_single_cost(be, D: _AllDir, k: int, a: int, b: int) -> int:

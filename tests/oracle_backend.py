@@ -105,3 +105,40 @@ class OracleBackend:
         for d in (self.seq, self.fitch, self.sank):
             for v in [v for v in d if v >= first]:
                 del d[v]
+
+    # final states of the non-DO characters (the search module's uppass)
+    def final_slots(self, n_slots, fitch_base):
+        self.fin = {}
+
+    def final_root(self, node, slot):
+        f = self.fitch[int(node)].copy() if self.nf else np.zeros(0, np.uint8)
+        rows, bits = [], []
+        for s in self.sank[int(node)]:
+            mn = int(min(s))
+            rows.append([O.SANK_INF if x >= O.SANK_INF else x - mn for x in s])
+            bits.append(sum(1 << i for i, x in enumerate(s) if x == mn))
+        self.fin[int(slot)] = (f, np.array(rows, np.int64).reshape(self.ns, -1),
+                               np.array(bits, np.int64))
+
+    def final_states(self, anc, node, left, right, out):
+        for a, v, l, r, o in zip(anc, node, left, right, out):
+            fa, ea, ba = self.fin[int(a)]
+            f = O.nonadd_median_3(fa, self.fitch[int(v)], self.fitch[int(l)],
+                                  self.fitch[int(r)]) if self.nf else np.zeros(0, np.uint8)
+            rows, bits = [], []
+            for ch in range(self.ns):
+                e, bb = O.sank_elt_median_3(self.tcm, np.zeros(len(ea[ch]), np.int64), ea[ch],
+                                            int(ba[ch]), self.sank[int(v)][ch],
+                                            self.sank[int(l)][ch], self.sank[int(r)][ch])
+                rows.append(e)
+                bits.append(bb)
+            self.fin[int(o)] = (f, np.array(rows, np.int64).reshape(self.ns, -1),
+                                np.array(bits, np.int64))
+
+    def node_final(self, slot):
+        """(Fitch row, Sankoff e rows with infinity as simulate.SANK_INF,
+        best-state bits) of a final slot, in the GPU backend's layout."""
+        f, e, b = self.fin[int(slot)]
+        e = e.copy()
+        e[e >= O.SANK_INF] = SANK_INF
+        return f, e.astype(np.int32), b.astype(np.int32)
