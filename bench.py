@@ -17,6 +17,16 @@ with gaps, medians, costs, lengths) inside the timed region.  N > 1 runs one
 replica per GPU (the pairs are independent; no collective).  ``--impl
 reference`` times the CPU restatement of the reference (oracle/) on all host
 cores over a bounded sample of the same workload.
+
+The default single-GPU run adds, on a bounded budget, the other
+configurations as keys of the same line: ``affine`` (the same pairs under
+gap opening 3: value, e2e, roofline, CPU baseline, parity),
+``spr_joins_per_s`` (one SPR pass's candidate joins scored per second, 200
+taxa x 1,500 bp + Fitch + Sankoff), ``learned_speedup`` (time to the plain
+search's exact tree cost, plain / learned, 500 taxa x 1,000 bp) and
+``serving`` (req_s, p50_ms, p99_ms of the Poisson request loop).
+``--no-extras`` prints the headline alone; ``--workload`` runs one of them
+on its own line.
 """
 from __future__ import annotations
 
@@ -52,6 +62,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-s", type=float, default=12.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="headline only: skip the affine, SPR, learned and serving keys")
     p.add_argument("--workload", default="align",
                    choices=["align", "spr", "tbr", "learned", "serving"],
                    help="align (default, the headline line) or one of the other configs")
@@ -255,7 +267,7 @@ def aggregate(cells: int, seconds: float, dev, world: int):
 def run_ours(args):
     import torch
     import torch.distributed as dist
-    from poyd_gb300 import align, native, synth
+    from poyd_gb300 import align, synth
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -268,6 +280,68 @@ def run_ours(args):
     host = synth.pair_batch_fast(args.seed + rank, args.pairs)
     pinned = [torch.from_numpy(x).pin_memory() for x in host]
     batch = align.PairBatch.from_packed(pinned, device=dev)
+    env = {"world": world, "rank": rank, "local": local, "dev": dev, "host": host,
+           "pinned": pinned, "batch": batch}
+    line = measure_align(args, env)
+    failed = bool(line and line.get("parity", {}).get("mismatches"))
+    if rank == 0 and world == 1 and args.workload == "align" and not args.no_extras:
+        # The other configurations, on a bounded budget, as keys of the same
+        # line: the affine variant of the same pairs, one SPR pass's
+        # candidate scoring, the learned vs plain search and the serving loop.
+        extras = argparse.Namespace(**vars(args))
+        extras.cpu_sample_s = min(args.cpu_sample_s, 6.0)
+        extras.serve_s = min(args.serve_s, 8.0)
+        if args.model == "linear":
+            extras.model = "affine"
+            aff = _guard(lambda: measure_align(extras, env))
+            keep = ("value", "unit", "ms_per_step", "e2e", "roofline", "cpu_baseline", "parity",
+                    "gpu_launches", "clocks", "kernel_ms_per_step")
+            line["affine"] = {k: aff[k] for k in keep if k in aff} if "error" not in aff else aff
+            line["affine"]["config"] = {"tcm": "sub 1 / indel 2 / gap_opening 3",
+                                        "pairs": args.pairs, "same_pairs_as_headline": True}
+            failed |= bool(line["affine"].get("parity", {}).get("mismatches"))
+            extras.model = "linear"
+        spr = _guard(lambda: run_spr(extras))
+        line["spr_joins_per_s"] = spr.get("value")
+        line["spr"] = spr
+        failed |= spr.get("cpu_baseline", {}).get("bit_exact_on_sample") is False
+        lrn = _guard(lambda: run_learned(extras))
+        # a speedup counts only where the learned search reached the plain
+        # search's exact cost
+        line["learned_speedup"] = lrn.get("speedup") if lrn.get("reached_same_cost") else None
+        line["learned"] = lrn
+        srv = _guard(lambda: run_serving(extras))
+        line["serving"] = {"req_s": srv.get("value"), "p50_ms": srv.get("p50_ms"),
+                           "p99_ms": srv.get("p99_ms"), **srv}
+        failed |= srv.get("sample_identical_alone") is False
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    if failed:
+        sys.stderr.write("bench: a result differs from the oracle or the one-at-a-time run\n")
+        sys.exit(1)
+
+
+def _guard(fn):
+    """Runs one extra workload; an exception is reported in its key rather
+    than losing the headline line."""
+    try:
+        return fn()
+    except Exception as ex:  # noqa: BLE001 -- reported, not hidden
+        return {"error": "%s: %s" % (type(ex).__name__, str(ex)[:300])}
+
+
+def measure_align(args, env):
+    """The batched align_2 measurement (``args.model``) on the pairs of
+    `env`: device-resident value, the host-buffer e2e run, the roofline,
+    the oracle's CPU time on a sample and the parity of both runs' results
+    on that sample.  Returns the line (rank 0) or None."""
+    import torch
+    import torch.distributed as dist
+    from poyd_gb300 import align, native
+    world, rank, local, dev = env["world"], env["rank"], env["local"], env["dev"]
+    host, pinned, batch = env["host"], env["pinned"], env["batch"]
     cm = cm_for(args, align)
 
     def barrier():
@@ -337,70 +411,68 @@ def run_ours(args):
                "api": "poyd_align_2_host (download overlapping the DP)",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
-    if rank == 0:
-        peak_gops = native.int32_peak()
-        dp_launch_ms = dp_ms / max(dp_n, 1)
-        achieved = cells / (dp_launch_ms * 1e-3) * OPS_PER_CELL[args.model] / 1e9
-        traffic = None
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            try:
-                traffic = json.load(open(prof)).get(kname)
-            except Exception:
-                traffic = None
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32", "data": "synthetic (seeded generator, poyd_gb300/synth.py)",
-            "config": dict(workload_config(args), band_cells_per_step=cells,
-                           full_matrix_cells_per_step=full_cells),
-            "gpu_launches": int(launches),
-            "kernel_ms_per_step": {"dp": dp_ms / args.steps, "all": all_ms / args.steps},
-            "roofline": {"bound": "int32", "achieved": achieved, "peak": peak_gops,
-                         "unit": "Gop/s", "frac": achieved / peak_gops if peak_gops else None,
-                         "traffic": traffic, "kernel": kname,
-                         "ops_per_cell": OPS_PER_CELL[args.model],
-                         "peak_source": "measured (poyd_int32_peak: fused add-min on the ALU "
-                                        "pipe interleaved with multiply-add adds on the FMA pipe)",
-                         "peak_alu_pipe_only": native.int_pipe_rate(0)},
-            "clocks": clk.summary(),
-            "e2e": e2e,
-        }
-        # CPU baseline: the oracle port on a bounded sample, all host threads
+    if rank != 0:
+        return None
+    peak_gops = native.int32_peak()
+    dp_launch_ms = dp_ms / max(dp_n, 1)
+    achieved = cells / (dp_launch_ms * 1e-3) * OPS_PER_CELL[args.model] / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
         try:
-            import ctypes as C
-            from oracle import oracle as O
-            O.build()
-            cm_o = oracle_cm(args, O)
-            threads = os.cpu_count() or 1
-            idx = cpu_sample_indices(host, args.cpu_sample_s, threads, C.byref(cm_o),
-                                     args.seed)
-            # the last timed step's results (device-resident run and, when
-            # measured, the host-buffer run) are checked against the oracle
-            # on every sampled pair while the oracle is timed
-            names = ["value"] + (["e2e"] if res_e2e is not None else [])
-            sets = [result_set(res)] + ([result_set(res_e2e)] if res_e2e is not None else [])
-            dt, c, bad = cpu_time_sample(host, idx, C.byref(cm_o), threads, sets)
-            line["cpu_baseline"] = {
-                "value": c / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": "%d of %d pairs (random, seeded), %.1f s" % (len(idx), args.pairs, dt)}
-            line["parity"] = {
-                "checked": int(len(idx)), "mismatches": int(sum(bad)),
-                "by_run": dict(zip(names, bad)),
-                "fields": ["cost", "aligned a", "aligned b", "median_2_with_gaps",
-                           "ancestor_2 median"],
-                "against": "oracle (C restatement of algn.c / sequence.ml, pinned against "
-                           "the compiled reference)"}
-        except Exception as ex:  # the baseline must not hide the GPU line
-            line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
-        print(json.dumps(line), flush=True)
-        if line.get("parity", {}).get("mismatches"):
-            sys.stderr.write("bench: %d of %d sampled pairs differ from the oracle\n"
-                             % (line["parity"]["mismatches"], line["parity"]["checked"]))
-            sys.exit(1)
-    if world > 1:
-        dist.destroy_process_group()
+            traffic = json.load(open(prof)).get(kname)
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic (seeded generator, poyd_gb300/synth.py)",
+        "config": dict(workload_config(args), band_cells_per_step=cells,
+                       full_matrix_cells_per_step=full_cells),
+        "gpu_launches": int(launches),
+        "kernel_ms_per_step": {"dp": dp_ms / args.steps, "all": all_ms / args.steps},
+        "roofline": {"bound": "int32", "achieved": achieved, "peak": peak_gops,
+                     "unit": "Gop/s", "frac": achieved / peak_gops if peak_gops else None,
+                     "traffic": traffic, "kernel": kname,
+                     "ops_per_cell": OPS_PER_CELL[args.model],
+                     "peak_source": "measured (poyd_int32_peak: fused add-min on the ALU "
+                                    "pipe interleaved with multiply-add adds on the FMA pipe)",
+                     "peak_alu_pipe_only": native.int_pipe_rate(0)},
+        "clocks": clk.summary(),
+        "e2e": e2e,
+    }
+    # CPU baseline: the oracle port on a bounded sample, all host threads
+    try:
+        import ctypes as C
+        from oracle import oracle as O
+        O.build()
+        cm_o = oracle_cm(args, O)
+        threads = os.cpu_count() or 1
+        idx = cpu_sample_indices(host, args.cpu_sample_s, threads, C.byref(cm_o), args.seed)
+        # the last timed step's results (device-resident run and, when
+        # measured, the host-buffer run) are checked against the oracle on
+        # every sampled pair while the oracle is timed
+        names = ["value"] + (["e2e"] if res_e2e is not None else [])
+        sets = [result_set(res)] + ([result_set(res_e2e)] if res_e2e is not None else [])
+        dt, c, bad = cpu_time_sample(host, idx, C.byref(cm_o), threads, sets)
+        line["cpu_baseline"] = {
+            "value": c / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d of %d pairs (random, seeded), %.1f s" % (len(idx), args.pairs, dt)}
+        fields = (["cost", "aligned a", "aligned b", "median_2_with_gaps", "ancestor_2 median"]
+                  if args.model == "linear" else
+                  ["cost", "aligned a", "aligned b", "median with gaps", "median"])
+        line["parity"] = {
+            "checked": int(len(idx)), "mismatches": int(sum(bad)),
+            "by_run": dict(zip(names, bad)), "fields": fields,
+            "against": "oracle (C restatement of algn.c / sequence.ml, pinned against "
+                       "the compiled reference)"}
+    except Exception as ex:  # the baseline must not hide the GPU line
+        line["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    if line.get("parity", {}).get("mismatches"):
+        sys.stderr.write("bench: %d of %d sampled %s pairs differ from the oracle\n"
+                         % (line["parity"]["mismatches"], line["parity"]["checked"], args.model))
+    return line
 
 
 def _emit(line):
@@ -508,7 +580,7 @@ def run_spr(args):
     line["cpu_baseline"] = {"value": rate, "unit": "joins/s", "cores": threads, "kind": "port",
                             "sample": "%d of %d candidates" % (k_cpu, n),
                             "bit_exact_on_sample": bool(np.array_equal(out, score[idx]))}
-    _emit(line)
+    return line
 
 
 def run_tbr(args):
@@ -531,7 +603,7 @@ def run_tbr(args):
     dt = time.perf_counter() - t0
     medians = be.stats["median_pairs"]
     st = search.tbr_pass(t, be, max_moves=16, diag=diag)
-    _emit({
+    return ({
         "workload": "TBR pass, 200 taxa x 1500 bp + 2000 Fitch + 200 Sankoff",
         "metric": "TBR candidate joins scored per second", "value": len(S) / dt,
         "unit": "joins/s", "candidates": int(len(S)),
@@ -593,7 +665,7 @@ def run_learned(args):
                 break
     torch.cuda.synchronize()
     sec_l = time.perf_counter() - t0
-    _emit({
+    return ({
         "workload": "config 3: learned join proposal vs plain exhaustive SPR, 500 taxa x 1000 bp",
         "metric": "SPR time to equal tree cost, learned vs plain GPU",
         "plain_seconds": sec_p, "plain_seconds_with_confirming_pass": sec_all_p,
@@ -629,7 +701,7 @@ def run_serving(args):
         else:
             r = align.align_2(b, cm, dos_empty=True).to_host()[0]
             ok &= r["cost"] == j.cost and np.array_equal(r["median"], j.median)
-    _emit({"workload": "config 4: serving loop, 16 searches, Poisson 2000 req/s, 120 GB budget",
+    return ({"workload": "config 4: serving loop, 16 searches, Poisson 2000 req/s, 120 GB budget",
            "metric": "served requests/s", "value": len(done) / wall, "unit": "req/s",
            "offered_rate": 2000.0, "seconds": wall, "batches": srv.batches,
            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
@@ -641,13 +713,13 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "spr":
-        run_spr(args)
+        _emit(run_spr(args))
     elif args.workload == "tbr":
-        run_tbr(args)
+        _emit(run_tbr(args))
     elif args.workload == "learned":
-        run_learned(args)
+        _emit(run_learned(args))
     elif args.workload == "serving":
-        run_serving(args)
+        _emit(run_serving(args))
     else:
         run_ours(args)
 

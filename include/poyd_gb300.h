@@ -374,6 +374,67 @@ int poyd_sank_distance_batch(const int32_t *nodes, int32_t nchar, int32_t k,
                              int64_t *dist, void *stream);
 
 /* ---------------------------------------------------------------------
+ * Downpass levels with the node data resident on the device.
+ *
+ * The downpass (AllDirChar.internal_downpass, allDirChar.ml:722-790) makes
+ * every interior vertex's preliminary data the median of its two
+ * children's (Node.median, node.ml:638: DOS.median, seqCS.ml:747-776, for
+ * the sequence; NonaddCS8.median, node.ml:272; SankCS.median, node.ml:333)
+ * in a post-order visit.  Vertices of one height are independent, so a
+ * downpass -- or the re-diagnosis of the vertices a tree move changes --
+ * is a list of levels, each one batch of median pairs whose inputs are
+ * existing nodes or outputs of earlier levels.
+ *
+ * Node store (device memory, owned by the caller):
+ *   pool: the sequences' bytes; node v's sequence is pool[node_off[v] ..
+ *         + node_len[v]) (the leading gap included);
+ *   fitch: rows [node][fitch_stride] of fitch_len NonaddCS8 characters
+ *         (16-byte aligned; fitch_len 0: none);
+ *   sank: rows [node][sank_nchar][sank_k] int32 (POYD_SANK_INF as above),
+ *         sank_tcm [k][k] (sank_nchar 0: none).
+ * ------------------------------------------------------------------- */
+typedef struct poyd_node_store {
+  uint8_t *pool;
+  int64_t pool_size;
+  uint8_t *fitch;
+  int64_t fitch_stride;
+  int32_t fitch_len;
+  int32_t sank_nchar;
+  int32_t *sank;
+  const int32_t *sank_tcm;
+  int32_t sank_k;
+  int32_t pad;
+} poyd_node_store;
+
+#define POYD_ESPACE -6  /* the caller's pool is too small (poyd_median_levels) */
+
+/* Levels l = 0 .. n_levels-1 of median pairs, pairs
+ * [level_start[l], level_start[l+1]): node out[i] becomes the median of
+ * nodes a[i] and b[i] (DOS.median with Sequence.is_empty's all-gap rule,
+ * as poyd_align_2_batch with POYD_FLAG_DOS_EMPTY, plus the Fitch and
+ * Sankoff medians of its rows).  Every out[i] is distinct and none is an
+ * input of its own or an earlier level.  The medians are written into the
+ * pool from *pool_top upwards (the four-sequence result slots of
+ * poyd_align_2_batch; node out[i] points at the fourth, the median).
+ *
+ * node_off / node_len are HOST arrays over all n_nodes node ids, in and
+ * out: the call reads the inputs' places and writes the outputs'.
+ * level_start, a, b, out are host arrays too; everything else stays on the
+ * device, and the call waits for the stream once per level (the align_2
+ * plan) and once at the end.  costs (host, may be NULL) receives per pair
+ * the DO cost and the Fitch median cost (int64 pairs).  Before any launch
+ * the call bounds the bytes it can need (a median is at most as long as
+ * its two inputs together); when *pool_top + that bound exceeds pool_size
+ * it writes the bound to *need (may be NULL) and returns POYD_ESPACE,
+ * leaving everything unchanged, so that the caller can compact or grow its
+ * pool and call again.  *pool_top returns the first unused byte. */
+int poyd_median_levels(const poyd_cm *cm, const poyd_node_store *store, int32_t n_nodes,
+                       int64_t *node_off, int32_t *node_len, int32_t n_levels,
+                       const int32_t *level_start, const int32_t *a, const int32_t *b,
+                       const int32_t *out, int64_t *pool_top, int64_t *need, int64_t *costs,
+                       void *stream);
+
+/* ---------------------------------------------------------------------
  * Learned join proposal (no counterpart in the reference): building blocks
  * of the 32-256-256-128-1 ReLU MLP with BF16 weights/activations and FP32
  * accumulation on tensor cores.  Matrices are row-major bf16 (uint16

@@ -55,15 +55,18 @@ __global__ void k_fitch_distance(const uint8_t *nodes, int64_t stride, int len, 
   if (lane == 0) dist[c] = cnt;
 }
 
+// Output row c of `out`, or row oi[c] when an output index is given (the
+// level engine writes the output nodes' own rows of the node array; a
+// level's outputs are never its inputs).
 __global__ void k_fitch_median(const uint8_t *nodes, int64_t stride, int len, int n,
                                const int32_t *ai, const int32_t *bi, uint8_t *out,
-                               int64_t *added) {
+                               int64_t *added, const int32_t *oi) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= n) return;
   const uint4 *a = (const uint4 *)(nodes + (int64_t)ai[c] * stride);
   const uint4 *b = (const uint4 *)(nodes + (int64_t)bi[c] * stride);
-  uint4 *r = (uint4 *)(out + (int64_t)c * stride);
+  uint4 *r = (uint4 *)(out + (int64_t)(oi ? oi[c] : c) * stride);
   const int nv = (len + 15) >> 4;
   unsigned cnt = 0;
   for (int v = lane; v < nv; v += 32) {
@@ -166,7 +169,7 @@ __device__ __forceinline__ void sank_char(const int *tcm, const int *as, const i
 template <int K>
 __global__ void k_sank_median(const int32_t *nodes, int nchar, const int32_t *tcm_g, int n,
                               const int32_t *ai, const int32_t *bi, int32_t *out_s,
-                              int32_t *out_e, int32_t *out_b) {
+                              int32_t *out_e, int32_t *out_b, const int32_t *oi) {
   __shared__ int tcm[K * K];
   for (int t = threadIdx.x; t < K * K; t += blockDim.x) tcm[t] = tcm_g[t];
   __syncthreads();
@@ -179,7 +182,7 @@ __global__ void k_sank_median(const int32_t *nodes, int nchar, const int32_t *tc
 #pragma unroll
   for (int i = 0; i < K; ++i) { as[i] = a[i]; bs[i] = b[i]; }
   sank_char<K>(tcm, as, bs, cc, e, beta, minc, mina, minb);
-  const int64_t o = ((int64_t)c * nchar + ch) * K;
+  const int64_t o = ((int64_t)(oi ? oi[c] : c) * nchar + ch) * K;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
     out_s[o + i] = cc[i];
@@ -352,7 +355,7 @@ extern "C" int poyd_nonadd8_median_batch(const uint8_t *nodes, int64_t stride, i
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("fitch_median", st);
   k_fitch_median<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
-      nodes, stride, len, n, a_idx, b_idx, out, added_cost);
+      nodes, stride, len, n, a_idx, b_idx, out, added_cost, nullptr);
   FS_CK(cudaGetLastError());
   return POYD_OK;
 }
@@ -389,7 +392,7 @@ extern "C" int poyd_sank_median_batch(const int32_t *nodes, int32_t nchar, int32
   const int64_t total = (int64_t)n * nchar;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   ProfScope ps("sank_median", st);
-#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, out_s, out_e, out_beta)
+#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, out_s, out_e, out_beta, nullptr)
   switch (k) {
     SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
     SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)
@@ -438,6 +441,38 @@ extern "C" int poyd_sank_median_3_batch(const int32_t *nodes, const int32_t *fin
 #define L(KV)                                                                              \
   k_sank_median3<KV><<<blocks, 256, 0, st>>>(nodes, fin_e, fin_best, nchar, tcm, n, anc, node, \
                                              left, right, out_e, out_best)
+  switch (k) {
+    SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
+    SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)
+  }
+#undef L
+  FS_CK(cudaGetLastError());
+  return POYD_OK;
+}
+
+// Medians written into the node arrays' own rows out_idx[c] (the level
+// engine, csrc/levels.cu); same kernels and arguments as the entry points
+// above, checked by the caller.
+int poyd::launch_fitch_median_rows(uint8_t *nodes, int64_t stride, int32_t len, int32_t n,
+                                   const int32_t *a_idx, const int32_t *b_idx,
+                                   const int32_t *out_idx, int64_t *added, cudaStream_t st) {
+  if (n == 0) return POYD_OK;
+  ProfScope ps("fitch_median", st);
+  k_fitch_median<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
+      nodes, stride, len, n, a_idx, b_idx, nodes, added, out_idx);
+  FS_CK(cudaGetLastError());
+  return POYD_OK;
+}
+
+int poyd::launch_sank_median_rows(int32_t *nodes, int32_t nchar, int32_t k, const int32_t *tcm,
+                                  int32_t n, const int32_t *a_idx, const int32_t *b_idx,
+                                  const int32_t *out_idx, cudaStream_t st) {
+  if (n == 0 || nchar == 0) return POYD_OK;
+  if (k < 2 || k > 8) return fail(POYD_EUNSUP, "Sankoff characters need 2..8 states");
+  const int64_t total = (int64_t)n * nchar;
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  ProfScope ps("sank_median", st);
+#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, nodes, nullptr, nullptr, out_idx)
   switch (k) {
     SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
     SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)

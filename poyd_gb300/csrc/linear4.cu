@@ -494,7 +494,8 @@ __device__ __noinline__ void tb_pair4(const LinTbArgs &A, const uint8_t *med, in
   const int64_t cap = slot_cap(la, lb);
   uint8_t *oa = A.out + A.out_off[id];
   uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
-  const uint8_t *s1 = A.seq + P.s1_off, *s2 = A.seq + P.s2_off;
+  const uint8_t *__restrict__ s1 = A.seq + P.s1_off;
+  const uint8_t *__restrict__ s2 = A.seq + P.s2_off;
   if (P.empty) {
     // DOS.median: the non-empty (or second) sequence is the median
     const bool a_empty = P.empty == 1;
@@ -525,6 +526,19 @@ __device__ __noinline__ void tb_pair4(const LinTbArgs &A, const uint8_t *med, in
       break;
     }
     const int key = (blk * 32 + k) * 2 + (vv >> 4);
+    // The walk mostly follows the diagonal: the line it reaches 16 rows on
+    // (same band index) is prefetched into L1, so that the L2 latency of
+    // the direction words overlaps the steps in between.  Rows map to
+    // increasing step positions, so that line lies inside this pair's
+    // (128-byte aligned) direction matrix.
+    if (r >= 16) {
+      const int rp = r - 16, kp = (rp & 127) >> 2;
+      const int Gp = (rp >> 7) * g.W + k4Lag * kp + lam4(rp & 3) + bi;
+      asm volatile("prefetch.L1 [%0];" ::"l"(dm4 + ((Gp >> 5) * 32 + kp) * 2 + ((Gp & 31) >> 4)));
+    }
+    // both characters are read whatever the move (r, j >= 0 here), off the
+    // read-only path, so that the loads issue ahead of the move's decode
+    const int c1 = __ldg(s1 + r), c2 = __ldg(s2 + j);
     if (key != cur_key) {
       cur = dm4[key];
       cur_key = key;
@@ -534,7 +548,7 @@ __device__ __noinline__ void tb_pair4(const LinTbArgs &A, const uint8_t *med, in
     // rank 1 is insert when swaped, else delete
     const int move = code == 0 ? 0 : (((code == 1u) == swaped) ? 1 : 2);
     const bool dr = move != 1, dj = move != 2;  // consumes a row / a column
-    const int cr = dr ? (int)s1[r] : gap, cc = dj ? (int)s2[j] : gap;
+    const int cr = dr ? c1 : gap, cc = dj ? c2 : gap;
     r -= dr;
     j -= dj;
     const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
@@ -553,6 +567,117 @@ __device__ __noinline__ void tb_pair4(const LinTbArgs &A, const uint8_t *med, in
   wm.flush();
   A.out_len[2 * id] = bad ? -1 : (int32_t)n;
   A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
+}
+
+// The same traceback by the pair's whole warp, for small batches where
+// every pair has its own warp.  tb_pair4's walk is one dependent chain of
+// index arithmetic (a few hundred cycles per step for a lone warp); here the
+// lanes read a stretch of the path at once.  Most moves are diagonal, so
+// lane i reads the move of cell (r - i, j - i) on the current diagonal (the
+// same band index); a ballot finds the first cell whose move is not
+// diagonal, and the warp takes the diagonal run up to it plus that cell's
+// move in one iteration, each lane writing its own column of the outputs
+// (the gap-free median by a ballot prefix count).  The path and the bytes
+// written are those of tb_pair4.  The direction words come from an 8-block
+// window of the pair's direction matrix that all lanes load together into
+// the warp's profile buffer (free once its fill is done); step positions
+// never increase along the walk (a diagonal move or a delete lowers the
+// row part of G by at least as much as the band index rises; an insert
+// lowers the band index), so the window slides down.
+__device__ __noinline__ void tb_pair4_solo(const LinTbArgs &A, const uint8_t *med, int id,
+                                           uint4 *win, int lane) {
+  const LinPlan P = A.plans[id];
+  const int gap = A.gap;
+  const int la = P.swap ? P.l2 : P.l1, lb = P.swap ? P.l1 : P.l2;
+  const int64_t cap = slot_cap(la, lb);
+  uint8_t *oa = A.out + A.out_off[id];
+  uint8_t *ob = oa + cap, *ow = ob + cap, *om = ow + cap;
+  const uint8_t *__restrict__ s1 = A.seq + P.s1_off;
+  const uint8_t *__restrict__ s2 = A.seq + P.s2_off;
+  if (P.empty) {
+    // DOS.median: the non-empty (or second) sequence is the median
+    const bool a_empty = P.empty == 1;
+    const uint8_t *src = (a_empty != (bool)P.swap) ? s2 : s1;
+    const int len = a_empty ? lb : la;
+    for (int i = lane; i < len; i += 32) om[cap - len + i] = src[i];
+    if (lane == 0) {
+      A.out_len[2 * id] = 0;
+      A.out_len[2 * id + 1] = len;
+    }
+    return;
+  }
+  const Geo4 g = geo4(P);
+  const uint4 *dm4 = (const uint4 *)(A.dm + A.dm_off[id]);
+  const int nq = g.nblk * 64;  // 16-byte words of the pair's direction matrix
+  const bool swaped = A.swaped < 0 ? !P.swap : (A.swaped != 0);
+  int r = P.l1 - 1, j = P.l2 - 1;  // the walk's cell (the same on every lane)
+  int n = 0, nm = 0;
+  int wlo = g.nblk;  // the window holds blocks [wlo, wlo + 8)
+  bool bad = false;
+  while (r > 0 || (r == 0 && j >= 0)) {
+    const int bi = (j - r) - g.dlo;  // band index, constant along the diagonal
+    const int G0 = (r >> 7) * g.W + k4Lag * ((r & 127) >> 2) + lam4(r & 3) + bi;
+    const int blk0 = G0 >> 5;
+    if (j < 0 || bi < 0 || bi >= g.wd || blk0 >= g.nblk || n + 2 >= cap) {  // left the band: a bug
+      bad = true;
+      break;
+    }
+    if (blk0 < wlo || blk0 >= wlo + 8) {
+      wlo = max(blk0 - 7, 0);
+      __syncwarp();
+      for (int i = lane; i < 8 * 64; i += 32) {
+        const int q = wlo * 64 + i;
+        if (q < nq) win[i] = dm4[q];
+      }
+      __syncwarp();
+    }
+    // lane i: the move of cell (r - i, j - i); 4 = not read (the run stops
+    // before this cell: outside the matrix, the output slot or the window)
+    const int ri = r - lane, ji = j - lane;
+    uint32_t code = 4;
+    if (ri >= 0 && ji >= 0 && n + lane + 2 < cap) {
+      const int k = (ri & 127) >> 2, m = ri & 3;
+      const int G = (ri >> 7) * g.W + k4Lag * k + lam4(m) + bi;
+      const int blk = G >> 5, vv = G & 31;
+      if (blk >= wlo) {
+        const uint4 cur = win[(blk - wlo) * 64 + k * 2 + (vv >> 4)];
+        const uint32_t w = (m & 1) ? ((vv & 8) ? cur.w : cur.z) : ((vv & 8) ? cur.y : cur.x);
+        code = (w >> (2 * (7 - (vv & 7)) + 16 * (m >> 1))) & 3u;
+      }
+    }
+    const uint32_t stop = __ballot_sync(kFull4, code != 0);
+    const int f = stop ? __ffs(stop) - 1 : 32;  // lanes below f move diagonally
+    const uint32_t cf = __shfl_sync(kFull4, code, f & 31);
+    const bool step_f = f < 32 && cf != 4;  // lane f's cell was read: its move too
+    // rank 1 is insert when swaped, else delete
+    const int move_f = step_f ? (((cf == 1u) == swaped) ? 1 : 2) : 0;
+    const bool writes = lane < f || (lane == f && step_f);
+    int md = gap;
+    if (writes) {
+      const bool dr = lane < f || move_f != 1, dj = lane < f || move_f != 2;
+      const int cr = dr ? (int)__ldg(s1 + ri) : gap, cc = dj ? (int)__ldg(s2 + ji) : gap;
+      const int ca = P.swap ? cc : cr, cb = P.swap ? cr : cc;
+      md = med[(ca << 5) | cb];
+      const int64_t pos = cap - 1 - (n + lane);
+      oa[pos] = (uint8_t)ca;
+      ob[pos] = (uint8_t)cb;
+      ow[pos] = (uint8_t)md;
+    }
+    const bool keep = writes && md != gap;
+    const uint32_t kb = __ballot_sync(kFull4, keep);
+    if (keep) om[cap - 1 - (nm + __popc(kb & ((1u << lane) - 1u)))] = (uint8_t)md;
+    n += f + (step_f ? 1 : 0);
+    nm += __popc(kb);
+    r -= f + ((step_f && move_f != 1) ? 1 : 0);
+    j -= f + ((step_f && move_f != 2) ? 1 : 0);
+  }
+  if (lane == 0) {
+    // ancestor_2 ends with the leading gap (algn.c:4140-4141)
+    if (!bad) om[cap - 1 - nm] = (uint8_t)gap;
+    A.out_len[2 * id] = bad ? -1 : (int32_t)n;
+    A.out_len[2 * id + 1] = bad ? -1 : (int32_t)(nm + 1);
+  }
+  __syncwarp();
 }
 
 template <int MODE>
@@ -596,10 +721,13 @@ __global__ void __launch_bounds__(k4Warps * 32, 2) k_lin_dp4(LinDpArgs A) {
   const int warp = threadIdx.x >> 5;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   uint32_t *bnd = (uint32_t *)A.scratch + gw * A.slab;
-  for (;;) {
-    int p = 0;
-    if (lane == 0) p = atomicAdd(A.counter, 1);
-    p = __shfl_sync(kFull4, p, 0);
+  // Every warp's first pair is fixed by position, warp-major over the
+  // blocks (consecutive pairs on different blocks, so on different SMs):
+  // a small batch then runs one pair per SM instead of sharing schedulers.
+  // Later pairs come from the counter, past the first wave.
+  const int nwarps = (int)gridDim.x * k4Warps;
+  int p = warp * (int)gridDim.x + (int)blockIdx.x;
+  for (;; p = __shfl_sync(kFull4, lane == 0 ? atomicAdd(A.counter, 1) + nwarps : 0, 0)) {
     if (p >= A.n) break;
     const int id = A.order ? A.order[p] : p;
     const LinPlan P = A.plans[id];
@@ -608,7 +736,11 @@ __global__ void __launch_bounds__(k4Warps * 32, 2) k_lin_dp4(LinDpArgs A) {
     } else {
       lin4_pair<MODE>(A, sb, warp, lane, P, MODE == kDpChoice ? A.dm_off[id] : 0, id, bnd);
     }
-    if (MODE == kDpChoice && A.fuse_tb) {
+    if (MODE == kDpChoice && A.fuse_tb && A.tb_solo) {
+      __syncwarp();  // the fill's direction words and profile reads are done
+      tb_pair4_solo(A.tb, med, id,
+                    (uint4 *)(lin4_dsm + (sb - raw) + kSmProf + warp * 8192), lane);
+    } else if (MODE == kDpChoice && A.fuse_tb) {
       // Publish this pair's direction matrix; the warp completing the batch
       // (no waiting: the count tells) walks all of its pairs, one per lane.
       __syncwarp();

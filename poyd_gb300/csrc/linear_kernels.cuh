@@ -70,6 +70,10 @@ struct LinDpArgs {
   // with fuse_tb: done[b] = 1 once batch b's results are written (host-mapped
   // memory a caller polls to download finished slots early; may be null)
   int *done;
+  // with fuse_tb, packed kernel: every pair has its own warp (n <= warps of
+  // the grid) and no done flags are kept, so the warp that filled a pair
+  // walks it at once, all lanes together (latency of small batches)
+  int tb_solo;
   LinTbArgs tb;
   DpK k;  // multiplier constants (1, -1, 4, -65536)
 };

@@ -175,7 +175,8 @@ extern "C" int poyd_cost_2_batch_noalloc(const poyd_cm *cm, int32_t n, const uin
   DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = nullptr; DA.order = nullptr;
   DA.tables = tabs; DA.gap = cm->gap; DA.counter = counter; DA.scratch = slabs;
   DA.slab = kNaSlabInts; DA.dm = nullptr; DA.cost = cost; DA.swaped = -1;
-  DA.fuse_tb = 0; DA.batch_done = nullptr; DA.done = nullptr; DA.tb = LinTbArgs{}; DA.k = dp_constants();
+  DA.fuse_tb = 0; DA.batch_done = nullptr; DA.done = nullptr; DA.tb_solo = 0; DA.tb = LinTbArgs{};
+  DA.k = dp_constants();
   launch_lin_dp(DA, kDpCost, kNaWarps / kDpWarps, st);
   NA_CK(cudaGetLastError());
   return POYD_OK;

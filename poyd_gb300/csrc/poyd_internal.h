@@ -87,7 +87,7 @@ void *ws_buffer(Workspace *w, int slot, size_t bytes);
 enum WsSlot {
   WS_TABLES = 0, WS_PLANS, WS_DMWORDS, WS_WD, WS_ORDER, WS_DM, WS_SCRATCH,
   WS_COUNTER, WS_CELLS, WS_AFF, WS_ERR, WS_SEQ, WS_META, WS_OUT, WS_BATCH, WS_ORDSCR,
-  WS_NSLOTS
+  WS_LVL_NODES, WS_LVL_PAIRS, WS_NSLOTS
 };
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);
@@ -104,5 +104,14 @@ struct ProfScope {
   ProfScope(const char *name, cudaStream_t s) : st(s) { prof_begin(name, s, &tok); }
   ~ProfScope() { prof_end(tok, st); }
 };
+
+// Fitch / Sankoff medians of node pairs written into the node arrays' own
+// rows out_idx[c] (fitch_sankoff.cu), for the level engine.
+int launch_fitch_median_rows(uint8_t *nodes, int64_t stride, int32_t len, int32_t n,
+                             const int32_t *a_idx, const int32_t *b_idx, const int32_t *out_idx,
+                             int64_t *added, cudaStream_t st);
+int launch_sank_median_rows(int32_t *nodes, int32_t nchar, int32_t k, const int32_t *tcm,
+                            int32_t n, const int32_t *a_idx, const int32_t *b_idx,
+                            const int32_t *out_idx, cudaStream_t st);
 
 }  // namespace poyd

@@ -311,6 +311,7 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
     DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
     DA.done = (ls && fuse && wave_at.size() == 2) ? ls->done : nullptr;
+    DA.tb_solo = (fuse && packed && !DA.done && (int64_t)m <= (int64_t)blocks * warps) ? 1 : 0;
     {
       ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st);
       if (packed) launch_lin_dp4(DA, mode, blocks, st);

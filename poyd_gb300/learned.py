@@ -48,13 +48,19 @@ def node_info(t: search.Tree, be):
     return size, depth, par, sib
 
 
+def _as_idx(be, x):
+    """Node ids as a device int32 tensor (host arrays are uploaded once)."""
+    if isinstance(x, torch.Tensor):
+        return x.to(device=be.dev, dtype=torch.int32)
+    return torch.from_numpy(np.ascontiguousarray(x, np.int32)).to(be.dev)
+
+
 def _fitch_dist(be, a, b):
-    n = len(a)
-    out = torch.empty(n, dtype=torch.int64, device=be.dev)
+    ia, ib = _as_idx(be, a), _as_idx(be, b)
+    n = int(ia.numel())
     if not be.nf or n == 0:
         return torch.zeros(n, dtype=torch.float32, device=be.dev)
-    ia = torch.from_numpy(np.asarray(a, np.int32)).to(be.dev)
-    ib = torch.from_numpy(np.asarray(b, np.int32)).to(be.dev)
+    out = torch.empty(n, dtype=torch.int64, device=be.dev)
     native.check(native.lib().poyd_nonadd8_distance_batch(
         C.c_void_p(be.fitch.data_ptr()), C.c_int64(be.stride), be.nf, n, C.c_void_p(ia.data_ptr()),
         C.c_void_p(ib.data_ptr()), C.c_void_p(out.data_ptr()),
@@ -63,12 +69,11 @@ def _fitch_dist(be, a, b):
 
 
 def _sank_dist(be, a, b):
-    n = len(a)
+    ia, ib = _as_idx(be, a), _as_idx(be, b)
+    n = int(ia.numel())
     if not be.ns or n == 0:
         return torch.zeros(n, dtype=torch.float32, device=be.dev)
     out = torch.empty(n, dtype=torch.int64, device=be.dev)
-    ia = torch.from_numpy(np.asarray(a, np.int32)).to(be.dev)
-    ib = torch.from_numpy(np.asarray(b, np.int32)).to(be.dev)
     native.check(native.lib().poyd_sank_distance_batch(
         C.c_void_p(be.sank.data_ptr()), be.ns, be.k, C.c_void_p(be.tcm.data_ptr()), n,
         C.c_void_p(ia.data_ptr()), C.c_void_p(ib.data_ptr()), C.c_void_p(out.data_ptr()),
@@ -81,21 +86,23 @@ def features(t: search.Tree, be, S: np.ndarray, E: np.ndarray, cur: dict) -> tor
     dev = be.dev
     size, depth, par, sib = node_info(t, be)
     T = lambda x: torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(dev)
+    I = lambda x: torch.from_numpy(np.ascontiguousarray(x, np.int64)).to(dev)
     L = T(be.len)
     nf, ns = max(be.nf, 1), max(be.ns, 1)
     amb = (_POPC.to(dev)[be.fitch[:, :be.nf].long()].mean(dim=1) if be.nf
            else torch.zeros(len(be.len), device=dev))
-    s = torch.from_numpy(S).to(dev)
-    e = torch.from_numpy(E).to(dev)
-    pe = torch.from_numpy(par[E]).to(dev)
-    ps = torch.from_numpy(par[S]).to(dev)
-    sb = sib[S]
-    fse = _fitch_dist(be, S, E) / nf * 10
-    fspe = _fitch_dist(be, S, par[E]) / nf * 10
-    fsib = _fitch_dist(be, S, sb) / nf * 10
-    sse = _sank_dist(be, S, E) / ns
-    ssib = _sank_dist(be, S, sb) / ns
-    curs = T(cur[S].astype(np.float32))
+    # the candidates are uploaded once; parents, siblings and attachment
+    # costs are gathered on the device from per-node tables
+    s32, e32 = _as_idx(be, S), _as_idx(be, E)
+    s, e = s32.long(), e32.long()
+    par_t, sib_t = I(par), I(sib)
+    pe, ps, sb = par_t[e], par_t[s], sib_t[s]
+    fse = _fitch_dist(be, s32, e32) / nf * 10
+    fspe = _fitch_dist(be, s32, pe) / nf * 10
+    fsib = _fitch_dist(be, s32, sb) / nf * 10
+    sse = _sank_dist(be, s32, e32) / ns
+    ssib = _sank_dist(be, s32, sb) / ns
+    curs = T(cur.astype(np.float32))[s]
     size_t, depth_t = T(size), T(depth)
     f = [
         torch.log1p(size_t[s]), torch.log1p(size_t[e]),

@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libpoyd_gb300.so")
 
 POYD_OK = 0
-ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ERANGE", -4: "ENOMEM", -5: "EUNSUP"}
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ERANGE", -4: "ENOMEM", -5: "EUNSUP", -6: "ESPACE"}
+ESPACE = -6
 DELTAW_DEFAULT, DELTAW_EXPLICIT, DELTAW_DOS_DISTANCE = 0, 1, 2
 FLAG_DOS_EMPTY = 1
 SANK_INF = 1 << 30
@@ -39,6 +40,18 @@ class PoydCM(C.Structure):
     ]
 
 
+class PoydNodeStore(C.Structure):
+    """``poyd_node_store`` (include/poyd_gb300.h): device node data of the
+    level engine."""
+
+    _fields_ = [
+        ("pool", C.c_void_p), ("pool_size", C.c_int64),
+        ("fitch", C.c_void_p), ("fitch_stride", C.c_int64), ("fitch_len", C.c_int32),
+        ("sank_nchar", C.c_int32), ("sank", C.c_void_p), ("sank_tcm", C.c_void_p),
+        ("sank_k", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
 # Every entry point the public header declares (include/poyd_gb300.h);
 # tests check the header's declarations against this list and that the
 # library exports each of them.
@@ -51,6 +64,7 @@ EXPORTED = (
     "poyd_cost_2_batch", "poyd_cost_2_batch_noalloc", "poyd_gemm_bf16", "poyd_int32_peak",
     "poyd_int_pipe_rate", "poyd_last_error", "poyd_launch_count", "poyd_matrix_create",
     "poyd_matrix_free", "poyd_median_2_no_gaps_batch", "poyd_median_2_with_gaps_batch",
+    "poyd_median_levels",
     "poyd_mlp_head_backward", "poyd_mlp_head_forward", "poyd_nonadd16_distance_batch",
     "poyd_nonadd16_median_3_batch", "poyd_nonadd16_median_batch",
     "poyd_nonadd32_distance_batch", "poyd_nonadd32_median_3_batch",
@@ -74,6 +88,9 @@ SIGNATURES = [
     ("poyd_cost_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp]),
     ("poyd_align_2_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _i32, _vp]),
+    ("poyd_median_levels", C.c_int, [_cmp, C.POINTER(PoydNodeStore), _i32, _vp, _vp, _i32, _vp,
+                                     _vp, _vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                     _vp, _vp]),
     ("poyd_profile_enable", C.c_int, [C.c_int]),
     ("poyd_profile_read", C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int]),
     ("poyd_launch_count", C.c_longlong, []),

@@ -240,7 +240,10 @@ class GpuBackend:
         self.sank = torch.from_numpy(sk).to(self.dev)
         self.tcm = torch.from_numpy(np.ascontiguousarray(data.sank_tcm, np.int32)).to(self.dev)
         total = sum(len(s) for s in data.seqs)
-        self.pool = torch.zeros(max(1 << 20, 16 * total), dtype=torch.uint8, device=self.dev)
+        # the level engine leaves each median inside its four-sequence
+        # result slot (about 8x a sequence's bytes); compaction reclaims
+        # the rest
+        self.pool = torch.zeros(max(64 << 20, 64 * total), dtype=torch.uint8, device=self.dev)
         self.off = np.zeros(n_nodes, np.int64)
         self.len = np.zeros(n_nodes, np.int32)
         self.top = 0
@@ -257,15 +260,18 @@ class GpuBackend:
         return o
 
     def _compact(self, extra: int = 0):
-        live = [v for v in range(len(self.len)) if self.len[v] > 0]
-        need = sum(int(self.len[v]) for v in live) + extra
-        newpool = torch.zeros(max(2 * need, self.pool.numel()), dtype=torch.uint8, device=self.dev)
-        top = 0
-        for v in live:
-            o, l = int(self.off[v]), int(self.len[v])
-            newpool[top:top + l] = self.pool[o:o + l]
-            self.off[v] = top
-            top += l
+        """Moves every live sequence to the front of a fresh pool with room
+        for `extra` more bytes (one gather on the device)."""
+        live = np.flatnonzero(self.len > 0)
+        ln = self.len[live].astype(np.int64)
+        top = int(ln.sum())
+        newpool = torch.zeros(max(2 * (top + extra), self.pool.numel()), dtype=torch.uint8,
+                              device=self.dev)
+        if top:
+            dst = np.cumsum(ln) - ln
+            src = np.repeat(self.off[live] - dst, ln) + np.arange(top, dtype=np.int64)
+            newpool[:top] = self.pool[torch.from_numpy(src).to(self.dev)]
+            self.off[live] = dst
         self.pool, self.top = newpool, top
 
     def _put(self, v: int, seq: torch.Tensor):
@@ -278,50 +284,51 @@ class GpuBackend:
         return align.PairBatch(self.pool, t(self.off[a], np.int64), t(self.len[a], np.int32),
                                t(self.off[b], np.int64), t(self.len[b], np.int32))
 
-    def _batch_indexed(self, a, b, out):
-        """The pair batch of nodes (a_i, b_i), the node ids a, b and out on
-        the device and the output layout, from two uploads of host arrays
-        (no device read-back)."""
-        a = np.asarray(a, np.int64)
-        b = np.asarray(b, np.int64)
-        n = len(a)
-        la, lb = self.len[a].astype(np.int64), self.len[b].astype(np.int64)
-        cap = (la + lb + 2 + 3) // 4 * 4
-        off = np.cumsum(4 * cap) - 4 * cap
-        h64 = np.concatenate([self.off[a], self.off[b], off, cap, np.asarray(out, np.int64)])
-        h32 = np.concatenate([la, lb, a, b]).astype(np.int32)
-        d64 = torch.from_numpy(h64).to(self.dev)
-        d32 = torch.from_numpy(h32).to(self.dev)
-        batch = align.PairBatch(self.pool, d64[:n], d32[:n], d64[n:2 * n], d32[n:2 * n])
-        total = int(4 * cap.sum()) if n else 0
-        return batch, d32[2 * n:3 * n], d32[3 * n:], d64[4 * n:], \
-            (d64[2 * n:3 * n], total, d64[3 * n:4 * n])
-
     # -- batched operations -------------------------------------------------
     def medians(self, a: np.ndarray, b: np.ndarray, out: np.ndarray):
         """Downpass medians of (a_i, b_i) into nodes out_i; returns the DO
         and Fitch costs of each median (numpy int64)."""
-        n = len(a)
+        return self.median_levels([(a, b, out)])[0]
+
+    def median_levels(self, levels):
+        """Several dependent levels of downpass medians in one call of the
+        level engine (``poyd_median_levels``): `levels` lists (a, b, out)
+        node-id arrays; a level's inputs are existing nodes or outputs of
+        earlier levels.  Returns [(DO costs, Fitch costs)] per level."""
+        sizes = [len(lv[0]) for lv in levels]
+        n = int(sum(sizes))
+        if n == 0:
+            return [(np.zeros(0, np.int64), np.zeros(0, np.int64)) for _ in levels]
+        start = np.zeros(len(levels) + 1, np.int32)
+        start[1:] = np.cumsum(sizes)
+        cat = lambda k: np.ascontiguousarray(np.concatenate(
+            [np.asarray(lv[k], np.int64) for lv in levels]).astype(np.int32))
+        A, B, O = cat(0), cat(1), cat(2)
+        costs = np.zeros(2 * n, np.int64)
         st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         L = native.lib()
-        batch, ia, ib, oi, layout = self._batch_indexed(a, b, out)
-        res = align.align_2(batch, self.cm, dos_empty=True, layout=layout)
-        tmp_f = torch.empty((n, self.stride), dtype=torch.uint8, device=self.dev)
-        added = torch.zeros(n, dtype=torch.int64, device=self.dev)
-        if self.nf:
-            native.check(L.poyd_nonadd8_median_batch(_p(self.fitch), C.c_int64(self.stride), self.nf,
-                                                     n, _p(ia), _p(ib), _p(tmp_f), _p(added), st))
-        if self.ns:
-            tmp_s = torch.empty((n, self.ns, self.k), dtype=torch.int32, device=self.dev)
-            native.check(L.poyd_sank_median_batch(_p(self.sank), self.ns, self.k, _p(self.tcm), n,
-                                                  _p(ia), _p(ib), _p(tmp_s), None, None, st))
-        do_cost, f_cost = self._store(res, out, added)
-        if self.nf:
-            self.fitch[oi] = tmp_f
-        if self.ns:
-            self.sank[oi] = tmp_s
+        for attempt in range(2):
+            store = native.PoydNodeStore(
+                pool=self.pool.data_ptr(), pool_size=self.pool.numel(),
+                fitch=self.fitch.data_ptr(), fitch_stride=self.stride, fitch_len=self.nf,
+                sank_nchar=self.ns, sank=self.sank.data_ptr(), sank_tcm=self.tcm.data_ptr(),
+                sank_k=self.k, pad=0)
+            top, need = C.c_int64(self.top), C.c_int64(0)
+            rc = L.poyd_median_levels(self.cm.ref, C.byref(store), len(self.len),
+                                      self.off.ctypes.data, self.len.ctypes.data, len(levels),
+                                      start.ctypes.data, A.ctypes.data, B.ctypes.data,
+                                      O.ctypes.data, C.byref(top), C.byref(need),
+                                      costs.ctypes.data, st)
+            if rc == native.ESPACE and attempt == 0:
+                self._compact(extra=int(need.value))
+                continue
+            native.check(rc)
+            break
+        self.top = int(top.value)
         self.stats["median_pairs"] += n
-        return do_cost, f_cost
+        c = costs.reshape(n, 2)
+        return [(c[start[l]:start[l + 1], 0].copy(), c[start[l]:start[l + 1], 1].copy())
+                for l in range(len(levels))]
 
     def _store(self, res: align.AlignResult, out, extra=None):
         """Moves each pair's fourth output sequence (the median, or the
@@ -547,11 +554,13 @@ def downpass(tree: Tree, be, nodes=None) -> Diagnosis:
     """Preliminary medians of every internal node, one batch per height."""
     d = Diagnosis()
     mc = tree.min_codes()
+    levels = []
     for level in tree.levels():
         lv = np.array(level, np.int64)
         a, b = _by_code(tree.kids[lv, 0], tree.kids[lv, 1], mc)
-        do, fi = be.medians(a, b, lv)
-        for i, v in enumerate(level):
+        levels.append((a, b, lv))
+    for (_, _, lv), (do, fi) in zip(levels, be.median_levels(levels)):
+        for i, v in enumerate(lv.tolist()):
             d.do_cost[v] = int(do[i])
             d.fitch_cost[v] = int(fi[i])
     d.total = sum(d.do_cost.values()) + sum(d.fitch_cost.values()) + be.sank_cost(tree.root)
@@ -747,33 +756,52 @@ def tbr_candidates(t: Tree, be, diag: Diagnosis | None = None):
         size[v] = 1 if v < n else 1 + size[t.kids[v][0]] + size[t.kids[v][1]]
     # two medians (up, root) for every clade node below the clade's children
     be.ensure_nodes(nxt + sum(2 * (int(size[s]) - 3) for s in fronts))
-    roots = []       # (a, b, out, s, u, cost below the root median)
+    # The medians' node ids do not depend on their costs: every depth's up
+    # medians and then all root medians are laid out first (ids in the
+    # order depth by depth, each depth's up medians before its roots) and
+    # computed in one call of dependent levels.  A front entry is (node,
+    # id of up(node), min code of up(node), job computing up(node) or -1,
+    # constant part of its cost); a job's cost below its median is its
+    # entry's cost plus the sibling subtree's downpass cost.
+    fronts = {s: [(u, up, upmc, -1, upc) for u, up, upmc, upc in f] for s, f in fronts.items()}
+    levels = []      # per depth: (a, b, out) of the up medians
+    jobs = []        # per up median: (parent job or -1, constant cost below it)
+    roots = []       # (a, b, out, s, u, job of up(u))
     while fronts:
-        jobs, meta = [], []
+        lvl, entries = [], []
         for s, front in fronts.items():
-            for u, upid, upmc, upc in front:
+            for u, upid, upmc, pj, pc in front:
                 if u < n:
                     continue
                 for w in (int(t.kids[u][0]), int(t.kids[u][1])):
                     x = int(t.kids[u][0] if t.kids[u][1] == w else t.kids[u][1])
-                    jobs.append((upid, x, nxt) if upmc < mc[x] else (x, upid, nxt))
-                    meta.append((s, w, nxt, min(upmc, int(mc[x])), upc + int(tot[x])))
+                    lvl.append((upid, x, nxt) if upmc < mc[x] else (x, upid, nxt))
+                    jobs.append((pj, pc + int(tot[x])))
+                    entries.append((s, w, nxt, min(upmc, int(mc[x])), len(jobs) - 1))
                     nxt += 1
-        if not jobs:
+        if not lvl:
             break
-        j = np.array(jobs, np.int64)
-        do, fi = be.medians(j[:, 0], j[:, 1], j[:, 2])
+        levels.append(np.array(lvl, np.int64))
         fronts = {}
-        for i, (s, w, wid, wmc, below) in enumerate(meta):
-            upc = below + int(do[i]) + int(fi[i])
-            fronts.setdefault(s, []).append((w, wid, wmc, upc))
+        for s, w, wid, wmc, ji in entries:
+            fronts.setdefault(s, []).append((w, wid, wmc, ji, 0))
             a, b = (w, wid) if mc[w] < wmc else (wid, w)
-            roots.append((a, b, nxt, s, w, int(tot[w]) + upc))
+            roots.append((a, b, nxt, s, w, ji))
             nxt += 1
     if roots:
         r = np.array([x[:3] for x in roots], np.int64)
-        do, fi = be.medians(r[:, 0], r[:, 1], r[:, 2])
-        for i, (_, _, rid, s, w, below) in enumerate(roots):
+        res = be.median_levels([(j[:, 0], j[:, 1], j[:, 2]) for j in levels] +
+                               [(r[:, 0], r[:, 1], r[:, 2])])
+        upc = np.zeros(len(jobs), np.int64)
+        k = 0
+        for do, fi in res[:-1]:
+            for i in range(len(do)):
+                pj, pc = jobs[k]
+                upc[k] = pc + (upc[pj] if pj >= 0 else 0) + int(do[i]) + int(fi[i])
+                k += 1
+        do, fi = res[-1]
+        for i, (_, _, rid, s, w, ji) in enumerate(roots):
+            below = int(tot[w]) + int(upc[ji])
             cand.append((s, w, rid, below + int(do[i]) + int(fi[i]) - int(tot[s])))
     # join edges: outside the clade, not its parent, not (own rooting) its
     # sibling; one (candidate x node) mask, rows in candidate order
@@ -942,9 +970,8 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
         roots.append(tid[T.root])
     be.ensure_nodes(tid_next)
     new = np.zeros(len(moves), np.int64)
-    for lvl in sorted(recs):
-        r = np.array(recs[lvl], np.int64)
-        do, fi = be.medians(r[:, 1], r[:, 2], r[:, 3])
+    rs = [np.array(recs[lvl], np.int64) for lvl in sorted(recs)]
+    for r, (do, fi) in zip(rs, be.median_levels([(r[:, 1], r[:, 2], r[:, 3]) for r in rs])):
         np.add.at(new, r[:, 0], do + fi)
         if detail is not None:
             for i in range(len(r)):
@@ -1053,27 +1080,33 @@ def _all_directions(tree: Tree, be) -> _AllDir | None:
     for e, x in info.items():
         if x[3] is not None:
             levels.setdefault(x[0], []).append(e)
-    for h in sorted(levels):
+    # every directed median, height by height, then the root median of
+    # every edge: one call of dependent levels
+    hs = sorted(levels)
+    jobs = []
+    for h in hs:
         es = levels[h]
-        a = np.array([info[info[e][3][0]][2] for e in es], np.int64)
-        b = np.array([info[info[e][3][1]][2] for e in es], np.int64)
-        out = np.array([info[e][2] for e in es], np.int64)
-        do, fi = be.medians(a, b, out)
-        for i, e in enumerate(es):
-            k1, k2 = info[e][3]
-            cdo[e] = cdo[k1] + cdo[k2] + int(do[i])
-            cfi[e] = cfi[k1] + cfi[k2] + int(fi[i])
-    a, b, bdo, bfi = [], [], [], []
+        jobs.append((np.array([info[info[e][3][0]][2] for e in es], np.int64),
+                     np.array([info[info[e][3][1]][2] for e in es], np.int64),
+                     np.array([info[e][2] for e in es], np.int64)))
+    ends = []
     for u, v in edges:
         d1, d2 = (u, v), (v, u)
         if info[d1][1] > info[d2][1]:
             d1, d2 = d2, d1
-        a.append(info[d1][2])
-        b.append(info[d2][2])
-        bdo.append(cdo[d1] + cdo[d2])
-        bfi.append(cfi[d1] + cfi[d2])
+        ends.append((d1, d2))
     out = np.arange(nxt, nxt + len(edges), dtype=np.int64)
-    do, fi = be.medians(np.array(a, np.int64), np.array(b, np.int64), out)
+    jobs.append((np.array([info[d1][2] for d1, _ in ends], np.int64),
+                 np.array([info[d2][2] for _, d2 in ends], np.int64), out))
+    res = be.median_levels(jobs)
+    for h, (do, fi) in zip(hs, res):
+        for i, e in enumerate(levels[h]):
+            k1, k2 = info[e][3]
+            cdo[e] = cdo[k1] + cdo[k2] + int(do[i])
+            cfi[e] = cfi[k1] + cfi[k2] + int(fi[i])
+    bdo = [cdo[d1] + cdo[d2] for d1, d2 in ends]
+    bfi = [cfi[d1] + cfi[d2] for d1, d2 in ends]
+    do, fi = res[-1]
     other = np.array(bfi, np.int64) + fi
     if getattr(be, "ns", 0):
         other = other + be.sank_costs(out)

@@ -23,6 +23,9 @@ class OracleBackend:
         self.nf = data.fitch.shape[1]
         self.ns = data.sank.shape[1]
 
+    def median_levels(self, levels):
+        return [self.medians(a, b, out) for a, b, out in levels]
+
     def medians(self, a, b, out):
         do, fi = [], []
         for x, y, v in zip(a, b, out):

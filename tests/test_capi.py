@@ -168,3 +168,44 @@ def test_header_matches_exported_list():
     loader sets up names one of them."""
     assert declared_symbols() == sorted(native.EXPORTED)
     assert {n for n, _, _ in native.SIGNATURES} <= set(native.EXPORTED)
+
+
+def test_median_levels_argument_checks_without_a_gpu(lib):
+    """poyd_median_levels refuses bad level lists, and a pool too small for
+    its bound with POYD_ESPACE and the bound, all before any CUDA call."""
+    L = C.CDLL(native.LIB_PATH)
+    L.poyd_last_error.restype = C.c_char_p
+    L.poyd_median_levels.argtypes = [C.POINTER(native.PoydCM), C.POINTER(native.PoydNodeStore),
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p,
+                                     C.c_void_p]
+    cm = _dna(lib)
+    store = native.PoydNodeStore(pool=64, pool_size=1 << 20)  # never dereferenced here
+    off = np.zeros(8, np.int64)
+    ln = np.array([100, 120, 90, 0, 0, 0, 0, 0], np.int32)
+
+    def call(start, a, b, out, size=1 << 20, top=0):
+        store.pool_size = size
+        st, aa, bb, oo = (np.asarray(x, np.int32) for x in (start, a, b, out))
+        t, need = C.c_int64(top), C.c_int64(-1)
+        rc = L.poyd_median_levels(C.byref(cm), C.byref(store), 8, off.ctypes.data, ln.ctypes.data,
+                                  len(st) - 1, st.ctypes.data, aa.ctypes.data, bb.ctypes.data,
+                                  oo.ctypes.data, C.byref(t), C.byref(need), None, None)
+        return rc, need.value, L.poyd_last_error()
+
+    EINVAL, ESPACE = -1, -6
+    assert call([0, 1], [0], [9], [4])[0] == EINVAL            # id out of range
+    assert call([0, 2], [0, 1], [1, 2], [4, 4])[0] == EINVAL   # node 4 written twice
+    assert call([0, 2], [0, 4], [1, 2], [4, 5])[0] == EINVAL   # output read in its own level
+    assert b"same level" in call([0, 2], [0, 4], [1, 2], [4, 5])[2]
+    assert call([0, 1], [0], [3], [4])[0] == EINVAL            # input without a sequence
+    assert call([1, 1], [0], [1], [4])[0] == EINVAL            # level_start[0] != 0
+    # two levels: 4 = m(0, 1), 5 = m(4, 2); bound slots 4*cap(100,120) and
+    # 4*cap(220, 90), each level rounded to 128 bytes, plus 128
+    slot = lambda x, y: 4 * ((x + y + 2 + 3) // 4 * 4)
+    bound = sum((slot(*p) + 127) // 128 * 128 for p in [(100, 120), (220, 90)]) + 128
+    rc, need, msg = call([0, 1, 2], [0, 4], [1, 2], [4, 5], size=1000)
+    assert rc == ESPACE and need == bound and b"pool too small" in msg
+    assert np.array_equal(ln, [100, 120, 90, 0, 0, 0, 0, 0])   # nothing changed
+    assert call([0, 0], [], [], [])[0] == 0                     # no pairs: a no-op
