@@ -140,12 +140,14 @@ class Tree:
             self.parent[nxt] = path[j]
 
     def nodes(self):
-        out, stack = [], [self.root]
+        """Preorder (a node before its children, the second child first)."""
+        kids, n = self.kids.tolist(), self.n
+        out, stack = [], [int(self.root)]
         while stack:
             v = stack.pop()
             out.append(v)
-            if v >= self.n:
-                stack.extend(self.kids[v])
+            if v >= n:
+                stack.extend(kids[v])
         return out
 
     def subtree(self, s: int):
@@ -160,18 +162,25 @@ class Tree:
     def min_codes(self) -> np.ndarray:
         """Smallest leaf id under every node (POY's ``min_child_code``,
         node.ml:674; a leaf's is its own taxon code)."""
-        mc = np.arange(len(self.parent), dtype=np.int64)
+        kids, n = self.kids.tolist(), self.n
+        mc = list(range(len(self.parent)))
         for v in self.nodes()[::-1]:
-            if v >= self.n:
-                mc[v] = min(mc[self.kids[v][0]], mc[self.kids[v][1]])
-        return mc
+            if v >= n:
+                a, b = kids[v]
+                mc[v] = min(mc[a], mc[b])
+        return np.array(mc, np.int64)
 
     def levels(self):
         """Internal nodes grouped by height (all children before parents)."""
+        kids, n = self.kids.tolist(), self.n
         h = {}
         order = self.nodes()[::-1]
         for v in order:
-            h[v] = 0 if v < self.n else 1 + max(h[self.kids[v][0]], h[self.kids[v][1]])
+            if v < n:
+                h[v] = 0
+            else:
+                a, b = kids[v]
+                h[v] = 1 + max(h[a], h[b])
         groups = {}
         for v in order:
             if v >= self.n:
@@ -902,9 +911,14 @@ def _valid_move(t: Tree, s: int, e: int) -> bool:
 
 
 def _heights(t: Tree) -> dict:
+    kids, n = t.kids.tolist(), t.n
     h = {}
     for v in t.nodes()[::-1]:
-        h[v] = 0 if v < t.n else 1 + max(h[t.kids[v][0]], h[t.kids[v][1]])
+        if v < n:
+            h[v] = 0
+        else:
+            a, b = kids[v]
+            h[v] = 1 + max(h[a], h[b])
     return h
 
 
