@@ -693,22 +693,51 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     # The accepted move's recomputed medians become the tree's own (no
     # re-diagnosis per move); one full downpass at the end of the pass
     # checks the incremental totals.
+    #
+    # A round's levels are latency-bound batches, so each round also
+    # evaluates the next round speculatively: every remaining move after
+    # the best-scored one (the guess).  When the guess is the round's exact
+    # best, those totals are exactly the next round's and that round is
+    # skipped; the moves accepted are the same as without the speculation.
     best = diag.total
     while moves:
         st.moves_tried += len(moves)
+        guess = moves[0]
+        tg = t.copy()
+        tg.insert(guess[0], guess[1], tg.prune(guess[0]))
+        follow = [m for m in moves[1:] if _valid_move(tg, m[0], m[1])]
+        trials = [[m] for m in moves] + [[guess, m] for m in follow]
         detail = {}
-        totals = evaluate_moves(t, be, diag, moves, detail)
-        k = int(np.argmin(totals))
-        if totals[k] >= best:
+        totals = evaluate_trials(t, be, diag, trials, detail)
+        single = totals[:len(moves)]
+        k = int(np.argmin(single))
+        if single[k] >= best:
             be.release_nodes(2 * t.n)
             break
         s, e = moves.pop(k)
-        w = t.prune(s)
-        t.insert(s, e, w)
-        commit_move(be, diag, detail[k], totals[k])
-        be.release_nodes(2 * t.n)
-        best = int(totals[k])
+        t.insert(s, e, t.prune(s))
         st.moves_accepted += 1
+        if k == 0 and follow:
+            # the guess was the best: the next round is already evaluated
+            st.moves_tried += len(follow)
+            pair = totals[len(single):]
+            k2 = int(np.argmin(pair))
+            if pair[k2] >= single[0]:
+                commit_move(be, diag, detail[0], single[0])
+                be.release_nodes(2 * t.n)
+                best = int(single[0])
+                break
+            s2, e2 = follow[k2]
+            t.insert(s2, e2, t.prune(s2))
+            commit_move(be, diag, detail[len(single) + k2], pair[k2])
+            be.release_nodes(2 * t.n)
+            best = int(pair[k2])
+            st.moves_accepted += 1
+            moves = [(a, b) for a, b in follow if (a, b) != (s2, e2) and _valid_move(t, a, b)]
+            continue
+        commit_move(be, diag, detail[k], single[k])
+        be.release_nodes(2 * t.n)
+        best = int(single[k])
         moves = [(a, b) for a, b in moves if _valid_move(t, a, b)]
     if st.moves_accepted:
         check = downpass(t, be)
@@ -935,28 +964,38 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
     With `detail` (a dict), the scratch slots are kept and detail[m] lists
     (node, scratch slot, DO cost, Fitch cost) of trial m's recomputed nodes,
     for commit_move; the caller then releases the slots."""
+    return evaluate_trials(t, be, diag, [[mv] for mv in moves], detail)
+
+
+def evaluate_trials(t: Tree, be, diag: Diagnosis, trials, detail=None) -> np.ndarray:
+    """``evaluate_moves`` for trials of several moves applied in order (each
+    in the tree the previous ones left): the dirty nodes are the ancestors,
+    in the trial's final tree, of every move's prune and regraft points and
+    re-rooted path nodes."""
     h_base = _heights(t)
     mc_base = t.min_codes()
     base_sank = be.sank_cost(t.root)
     tid_next = 2 * t.n
     recs = {}      # level -> list of (trial, a_ref, b_ref, out_tid)
-    old = np.zeros(len(moves), np.int64)
+    old = np.zeros(len(trials), np.int64)
     roots = []
-    for m, mv in enumerate(moves):
-        s, e = int(mv[0]), int(mv[1])
-        u = int(mv[2]) if len(mv) > 2 else -1
+    for m, trial in enumerate(trials):
         T = t.copy()
-        changed = []
-        if u >= 0:
-            T.reroot(s, u)
-            changed = [v for v in T.subtree(s)
-                       if v >= T.n and set(T.kids[v].tolist()) != set(t.kids[v].tolist())]
-        p = T.parent[s]
-        g = T.parent[p]
-        w = T.prune(s)
-        T.insert(s, e, w)
+        starts = []
+        for mv in trial:
+            s, e = int(mv[0]), int(mv[1])
+            u = int(mv[2]) if len(mv) > 2 else -1
+            if u >= 0:
+                T.reroot(s, u)
+                starts += [v for v in T.subtree(s)
+                           if v >= T.n and set(T.kids[v].tolist()) != set(t.kids[v].tolist())]
+            p = T.parent[s]
+            starts.append(int(T.parent[p]))
+            w = T.prune(s)
+            T.insert(s, e, w)
+            starts.append(int(w))
         dirty = set()
-        for v in [g, w] + changed:
+        for v in starts:
             while v >= 0 and v not in dirty:
                 dirty.add(v)
                 v = T.parent[v]
@@ -983,7 +1022,7 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
             old[m] += diag.do_cost[v] + diag.fitch_cost[v]
         roots.append(tid[T.root])
     be.ensure_nodes(tid_next)
-    new = np.zeros(len(moves), np.int64)
+    new = np.zeros(len(trials), np.int64)
     rs = [np.array(recs[lvl], np.int64) for lvl in sorted(recs)]
     for r, (do, fi) in zip(rs, be.median_levels([(r[:, 1], r[:, 2], r[:, 3]) for r in rs])):
         np.add.at(new, r[:, 0], do + fi)
