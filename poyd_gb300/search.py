@@ -693,51 +693,21 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     # The accepted move's recomputed medians become the tree's own (no
     # re-diagnosis per move); one full downpass at the end of the pass
     # checks the incremental totals.
-    #
-    # A round's levels are latency-bound batches, so each round also
-    # evaluates the next round speculatively: every remaining move after
-    # the best-scored one (the guess).  When the guess is the round's exact
-    # best, those totals are exactly the next round's and that round is
-    # skipped; the moves accepted are the same as without the speculation.
     best = diag.total
     while moves:
         st.moves_tried += len(moves)
-        guess = moves[0]
-        tg = t.copy()
-        tg.insert(guess[0], guess[1], tg.prune(guess[0]))
-        follow = [m for m in moves[1:] if _valid_move(tg, m[0], m[1])]
-        trials = [[m] for m in moves] + [[guess, m] for m in follow]
         detail = {}
-        totals = evaluate_trials(t, be, diag, trials, detail)
-        single = totals[:len(moves)]
-        k = int(np.argmin(single))
-        if single[k] >= best:
+        totals = evaluate_moves(t, be, diag, moves, detail)
+        k = int(np.argmin(totals))
+        if totals[k] >= best:
             be.release_nodes(2 * t.n)
             break
         s, e = moves.pop(k)
         t.insert(s, e, t.prune(s))
-        st.moves_accepted += 1
-        if k == 0 and follow:
-            # the guess was the best: the next round is already evaluated
-            st.moves_tried += len(follow)
-            pair = totals[len(single):]
-            k2 = int(np.argmin(pair))
-            if pair[k2] >= single[0]:
-                commit_move(be, diag, detail[0], single[0])
-                be.release_nodes(2 * t.n)
-                best = int(single[0])
-                break
-            s2, e2 = follow[k2]
-            t.insert(s2, e2, t.prune(s2))
-            commit_move(be, diag, detail[len(single) + k2], pair[k2])
-            be.release_nodes(2 * t.n)
-            best = int(pair[k2])
-            st.moves_accepted += 1
-            moves = [(a, b) for a, b in follow if (a, b) != (s2, e2) and _valid_move(t, a, b)]
-            continue
-        commit_move(be, diag, detail[k], single[k])
+        commit_move(be, diag, detail[k], totals[k])
         be.release_nodes(2 * t.n)
-        best = int(single[k])
+        best = int(totals[k])
+        st.moves_accepted += 1
         moves = [(a, b) for a, b in moves if _valid_move(t, a, b)]
     if st.moves_accepted:
         check = downpass(t, be)
