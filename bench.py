@@ -65,7 +65,7 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="headline only: skip the affine, SPR, learned and serving keys")
     p.add_argument("--workload", default="align",
-                   choices=["align", "spr", "tbr", "learned", "serving"],
+                   choices=["align", "spr", "tbr", "learned", "serving", "kernels"],
                    help="align (default, the headline line) or one of the other configs")
     p.add_argument("--train-trees", type=int, default=2)
     p.add_argument("--max-passes", type=int, default=8)
@@ -708,6 +708,129 @@ def run_serving(args):
            "jobs": st["n"], "sample_identical_alone": bool(ok)})
 
 
+def run_kernels(args):
+    """The other kernels on their own: Fitch and Sankoff distance / median
+    over node arrays larger than L2 (HBM-bound: achieved GB/s of the bytes
+    each launch must move, against the measured copy bandwidth), closest
+    on config-1 pairs, and the MLP's BF16 GEMMs (against the measured
+    cuBLAS bf16 rate).  Inputs are seeded random state sets and costs; CUDA
+    events, 3 warm-up launches, the mean of `--steps` launches."""
+    import ctypes as C
+    import torch
+    from poyd_gb300 import align, learned, native, synth
+    dev = torch.device("cuda")
+    L = native.lib()
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    P = lambda t: C.c_void_p(t.data_ptr())
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    g = torch.Generator(device="cpu").manual_seed(args.seed)
+    steps = max(args.steps, 1)
+
+    def timed(fn):
+        for _ in range(3):
+            native.check(fn())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            native.check(fn())
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def hbm_line(ms, nbytes, **kw):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return dict(kw, ms=ms, bytes_per_launch=int(nbytes), gb_s=gbs, peak_gb_s=hbm,
+                    frac=gbs / hbm)
+
+    out = {}
+    # Fitch: 262,144 nodes x 2,048 characters (512 MiB of rows)
+    NN, NF, n = 1 << 18, 2048, 1 << 20
+    fitch = torch.randint(1, 256, (NN, NF), dtype=torch.uint8, generator=g).to(dev)
+    ia = torch.randint(0, NN, (n,), dtype=torch.int32, generator=g).to(dev)
+    ib = torch.randint(0, NN, (n,), dtype=torch.int32, generator=g).to(dev)
+    dist = torch.empty(n, dtype=torch.int64, device=dev)
+    ms = timed(lambda: L.poyd_nonadd8_distance_batch(P(fitch), C.c_int64(NF), NF, n, P(ia),
+                                                     P(ib), P(dist), st))
+    out["fitch_distance"] = hbm_line(ms, n * (2 * NF + 8), kernel="k_fitch_distance", pairs=n,
+                                     row_bytes=NF, node_array_mib=NN * NF >> 20)
+    nm = 1 << 18
+    res = torch.empty((nm, NF), dtype=torch.uint8, device=dev)
+    added = torch.empty(nm, dtype=torch.int64, device=dev)
+    ms = timed(lambda: L.poyd_nonadd8_median_batch(P(fitch), C.c_int64(NF), NF, nm, P(ia),
+                                                   P(ib), P(res), P(added), st))
+    out["fitch_median"] = hbm_line(ms, nm * (3 * NF + 8), kernel="k_fitch_median", pairs=nm,
+                                   row_bytes=NF)
+    del res
+    # Sankoff: 131,072 nodes x 256 characters x 4 states, int32 (512 MiB)
+    NS, NC, K = 1 << 17, 256, 4
+    sank = torch.randint(0, 20, (NS, NC, K), dtype=torch.int32, generator=g).to(dev)
+    tcm = torch.tensor([[0 if i == j else 1 + (i + j) % 5 for j in range(K)] for i in range(K)],
+                       dtype=torch.int32, device=dev)
+    sa, sb = ia % NS, ib % NS
+    row = NC * K * 4
+    ms = timed(lambda: L.poyd_sank_distance_batch(P(sank), NC, K, P(tcm), n, P(sa), P(sb),
+                                                  P(dist), st))
+    out["sank_distance"] = hbm_line(ms, n * (2 * row + 8), kernel="k_sank_distance", pairs=n,
+                                    row_bytes=row, node_array_mib=NS * row >> 20)
+    ns_ = 1 << 17
+    out_s = torch.empty((ns_, NC, K), dtype=torch.int32, device=dev)
+    ms = timed(lambda: L.poyd_sank_median_batch(P(sank), NC, K, P(tcm), ns_, P(sa), P(sb),
+                                                P(out_s), None, None, st))
+    out["sank_median"] = hbm_line(ms, ns_ * 3 * row, kernel="k_sank_median", pairs=ns_,
+                                  row_bytes=row)
+    del out_s, sank, fitch
+    torch.cuda.synchronize()
+    # closest: (parent single, node median) = config-1 pairs
+    host = synth.pair_batch_fast(args.seed, 8192)
+    batch = align.PairBatch.from_packed([torch.from_numpy(x) for x in host], device=dev)
+    cm = align.CostMatrix.default()
+    for _ in range(3):
+        align.closest(batch, cm)
+    torch.cuda.synchronize()
+    native.lib().poyd_profile_enable(1)
+    native.profile_read(clear=True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        align.closest(batch, cm)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / steps
+    cms, _ = native.profile_read("closest", clear=False)
+    dps, _ = native.profile_read("lin_dp_dm", clear=False)
+    native.profile_read(clear=True)
+    native.lib().poyd_profile_enable(0)
+    out["closest"] = {"kernel": "k_closest (after the batched align_2 of each pair)", "pairs": 8192,
+                      "pairs_per_s": 8192 / wall, "column_pass_ms": cms / steps,
+                      "align_dp_ms": dps / steps}
+    # the MLP (32-256-256-128-1): forward + backward + Adam at batch 65,536
+    prop = learned.Proposal(seed=0)
+    X = torch.randn((1 << 16, learned.NFEAT), generator=g).to(dev)
+    y = torch.randn(1 << 16, generator=g).to(dev)
+    prop.fit(X, y, epochs=1, batch=4096)
+    torch.cuda.synchronize()
+    native.lib().poyd_profile_enable(1)
+    native.profile_read(clear=True)
+    t0 = time.perf_counter()
+    prop.fit(X, y, epochs=steps, batch=4096)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    gms, gn = native.profile_read("mlp_gemm", clear=False)
+    native.profile_read(clear=True)
+    native.lib().poyd_profile_enable(0)
+    dims = (learned.NFEAT, 256, 256, 128)
+    fwd = sum(2 * dims[i] * dims[i + 1] for i in range(3))  # per sample, GEMM layers
+    flops = steps * (1 << 16) * (3 * fwd - 2 * dims[0] * dims[1])  # fwd, dW, dH (no dX)
+    tf = flops / (gms * 1e-3) / 1e12 if gms else None
+    out["mlp_gemm"] = {"kernel": "k_gemm_bf16 (mma.sync m16n8k16)", "samples_per_s":
+                       steps * (1 << 16) / wall, "gemm_ms": gms, "gemm_launches": gn,
+                       "tflop_s": tf, "peak_tflop_s": bf16, "frac": tf / bf16 if tf else None}
+    return {"workload": "kernels: Fitch / Sankoff rows larger than L2, closest, MLP GEMMs",
+            "steps": steps, "results": out}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -720,6 +843,8 @@ def main():
         _emit(run_learned(args))
     elif args.workload == "serving":
         _emit(run_serving(args))
+    elif args.workload == "kernels":
+        _emit(run_kernels(args))
     else:
         run_ours(args)
 
