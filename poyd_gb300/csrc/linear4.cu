@@ -526,16 +526,6 @@ __device__ __noinline__ void tb_pair4(const LinTbArgs &A, const uint8_t *med, in
       break;
     }
     const int key = (blk * 32 + k) * 2 + (vv >> 4);
-    // The walk mostly follows the diagonal: the line it reaches 16 rows on
-    // (same band index) is prefetched into L1, so that the L2 latency of
-    // the direction words overlaps the steps in between.  Rows map to
-    // increasing step positions, so that line lies inside this pair's
-    // (128-byte aligned) direction matrix.
-    if (r >= 16) {
-      const int rp = r - 16, kp = (rp & 127) >> 2;
-      const int Gp = (rp >> 7) * g.W + k4Lag * kp + lam4(rp & 3) + bi;
-      asm volatile("prefetch.L1 [%0];" ::"l"(dm4 + ((Gp >> 5) * 32 + kp) * 2 + ((Gp & 31) >> 4)));
-    }
     // both characters are read whatever the move (r, j >= 0 here), off the
     // read-only path, so that the loads issue ahead of the move's decode
     const int c1 = __ldg(s1 + r), c2 = __ldg(s2 + j);
