@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-s", type=float, default=12.0)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="launch the default variant instead of the autotuner's choice")
     p.add_argument("--no-extras", action="store_true",
                    help="headline only: skip the affine, SPR, learned and serving keys")
     p.add_argument("--workload", default="align",
@@ -295,7 +297,7 @@ def run_ours(args):
             extras.model = "affine"
             aff = _guard(lambda: measure_align(extras, env))
             keep = ("value", "unit", "ms_per_step", "e2e", "roofline", "cpu_baseline", "parity",
-                    "gpu_launches", "clocks", "kernel_ms_per_step")
+                    "gpu_launches", "clocks", "kernel_ms_per_step", "autotune")
             line["affine"] = {k: aff[k] for k in keep if k in aff} if "error" not in aff else aff
             line["affine"]["config"] = {"tcm": "sub 1 / indel 2 / gap_opening 3",
                                         "pairs": args.pairs, "same_pairs_as_headline": True}
@@ -349,6 +351,11 @@ def measure_align(args, env):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # autotuner (untimed): the launch variant for this batch's shape class,
+    # every variant checked to give the same results
+    tuned = None
+    if args.model == "linear" and not args.no_autotune:
+        tuned = align.autotune(batch, cm, align=True, reps=1)
     # warm-up (also sizes the workspace)
     res = None
     for _ in range(args.warmup):
@@ -442,6 +449,8 @@ def measure_align(args, env):
         "clocks": clk.summary(),
         "e2e": e2e,
     }
+    if tuned is not None:
+        line["autotune"] = tuned
     # CPU baseline: the oracle port on a bounded sample, all host threads
     try:
         import ctypes as C

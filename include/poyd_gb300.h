@@ -408,6 +408,44 @@ typedef struct poyd_node_store {
 
 #define POYD_ESPACE -6  /* the caller's pool is too small (poyd_median_levels) */
 
+/* ---------------------------------------------------------------------
+ * Autotuner (no counterpart in the reference).  The batched linear DP
+ * (poyd_cost_2_batch, poyd_align_2_batch, poyd_align_2_host and every
+ * caller of them) has launch variants with identical results: the packed
+ * kernel when its 16-bit bound holds or the 32-bit kernel, a persistent
+ * grid of 1 to the maximum resident blocks per SM, and for batches with a
+ * warp per pair the whole-warp or the batched traceback walk.  A variant
+ * is kept per shape class: (device, align 0/1, floor(log2 pairs),
+ * floor(log2 widest band)).  Without an entry the defaults apply (packed
+ * when it can, the maximum grid, the whole-warp walk when every pair has
+ * its own warp).  The band is always the reference's.
+ * ------------------------------------------------------------------- */
+typedef struct poyd_tune_result {
+  int32_t packed, blocks_per_sm, solo; /* the variant kept (-1: default) */
+  int32_t lg_pairs, lg_width;          /* its class */
+  int32_t n_variants;
+  float ms[8];                         /* mean time of each variant tried */
+  int32_t variant[8][3];               /* {packed, blocks_per_sm, solo} */
+} poyd_tune_result;
+/* Times every variant on this batch (one warm-up, then `reps` runs each;
+ * the arguments of poyd_align_2_batch when align != 0, else of
+ * poyd_cost_2_batch with `deltaw_policy`), checks that each gives the
+ * default's costs (and lengths), and keeps the fastest for the batch's
+ * class.  The outputs hold the batch's results on return.  Returns
+ * POYD_ERANGE if a variant's results differ (a bug, reported). */
+int poyd_autotune_batch(const poyd_cm *cm, int32_t align, int32_t n, const uint8_t *seq,
+                        const int64_t *a_off, const int32_t *a_len, const int64_t *b_off,
+                        const int32_t *b_len, int32_t deltaw_policy, int32_t *cost,
+                        uint8_t *out, const int64_t *out_off, int32_t *out_len, int32_t flags,
+                        int32_t reps, poyd_tune_result *res, void *stream);
+/* Sets / reads (returns 1 when present, else 0) / clears the kept variants
+ * (host tables only: no CUDA call). */
+int poyd_autotune_set(int32_t device, int32_t align, int32_t lg_pairs, int32_t lg_width,
+                      int32_t packed, int32_t blocks_per_sm, int32_t solo);
+int poyd_autotune_get(int32_t device, int32_t align, int32_t lg_pairs, int32_t lg_width,
+                      int32_t *packed, int32_t *blocks_per_sm, int32_t *solo);
+int poyd_autotune_clear(void);
+
 /* Levels l = 0 .. n_levels-1 of median pairs, pairs
  * [level_start[l], level_start[l+1]): node out[i] becomes the median of
  * nodes a[i] and b[i] (DOS.median with Sequence.is_empty's all-gap rule,

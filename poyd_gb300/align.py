@@ -279,6 +279,35 @@ def align_2(batch: PairBatch, cm: CostMatrix, dos_empty: bool = False,
     return AlignResult(cost, out, out_off, out_len, cap, cells)
 
 
+def autotune(batch: PairBatch, cm: CostMatrix, align: bool = True, deltaw=None,
+             dos_empty: bool = False, reps: int = 2, stream=None) -> dict:
+    """Times the launch variants of the batched linear DP on this batch
+    (``poyd_autotune_batch``) and keeps the fastest for every later batch
+    of its shape class; all variants give identical results (checked).
+    `align` tunes ``align_2``, else ``cost_2`` with `deltaw` ("dos" or
+    None).  Returns the variant kept and the time of each tried."""
+    dev = batch.seq.device
+    cost = torch.empty(batch.n, dtype=torch.int32, device=dev)
+    out = out_off = out_len = None
+    if align:
+        out_off, total, _ = batch.out_layout()
+        out = torch.empty(max(total, 16), dtype=torch.uint8, device=dev)
+        out_len = torch.empty(2 * batch.n, dtype=torch.int32, device=dev)
+    pol = native.DELTAW_DOS_DISTANCE if deltaw == "dos" else native.DELTAW_DEFAULT
+    res = native.PoydTuneResult()
+    ptr = lambda t: t.data_ptr() if t is not None else None
+    check(lib().poyd_autotune_batch(
+        cm.ref, int(bool(align)), batch.n, batch.seq.data_ptr(), batch.a_off.data_ptr(),
+        batch.a_len.data_ptr(), batch.b_off.data_ptr(), batch.b_len.data_ptr(), pol,
+        cost.data_ptr(), ptr(out), ptr(out_off), ptr(out_len),
+        native.FLAG_DOS_EMPTY if dos_empty else 0, int(reps), C.byref(res),
+        _stream_handle(stream)))
+    tried = [{"packed": res.variant[i][0], "blocks_per_sm": res.variant[i][1],
+              "solo": res.variant[i][2], "ms": float(res.ms[i])} for i in range(res.n_variants)]
+    return {"packed": res.packed, "blocks_per_sm": res.blocks_per_sm, "solo": res.solo,
+            "lg_pairs": res.lg_pairs, "lg_width": res.lg_width, "tried": tried}
+
+
 def host_outputs(parts, pin: bool = True) -> dict:
     """Host result buffers for :func:`align_2_host` on a batch whose host
     arrays are `parts` (``PairBatch.pack_host``); reusable across calls."""

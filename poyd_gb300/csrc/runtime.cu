@@ -10,6 +10,7 @@
 #include <map>
 #include <mutex>
 #include <numeric>
+#include <tuple>
 #include <vector>
 #include "poyd_internal.h"
 #include "linear_kernels.cuh"
@@ -157,6 +158,43 @@ int upload_tables_ws(Workspace *w, const poyd_cm *cm, DevTables **dev, void *str
 
 // Shared driver of poyd_cost_2_batch (want_align = false) and
 // poyd_align_2_batch (want_align = true) for the linear model.
+constexpr int kTuneMax = 8;  // variants timed per batch (poyd_tune_result)
+
+// ---------------------------------------------------------------------------
+// Autotuner (no counterpart in the reference, whose C code has one kernel per
+// operation).  The batched linear DP has several implementations that give
+// identical results: the packed kernel (k_lin_dp4, when the plan finds every
+// value fits 16 bits) or the 32-bit one (k_lin_dp), a persistent grid of 1 to
+// the kernel's maximum resident blocks per SM, and, for batches with a warp
+// per pair, the whole-warp small-batch walk or the batched one.  Which is
+// fastest depends on the batch's shape; poyd_autotune_batch times each on a
+// caller's batch and records the winner for the batch's shape class (device,
+// mode, log2 of the pair count, log2 of the widest band), and every later
+// batch of that class launches it.  Without an entry the defaults apply
+// (packed when eligible, the maximum resident grid, the solo walk when
+// every pair has its own warp).  The band itself is always the reference's.
+// ---------------------------------------------------------------------------
+struct LinVariant {
+  int packed;         // 1 packed when eligible, 0 the 32-bit kernel, -1 default
+  int blocks_per_sm;  // 0: the maximum resident
+  int solo;           // 1 / 0 small-batch walk on / off, -1 default
+};
+using TuneKey = std::tuple<int, int, int, int>;  // device, align, lg pairs, lg width
+static std::mutex g_tune_mu;
+static std::map<TuneKey, LinVariant> g_tune;
+static thread_local const LinVariant *g_force = nullptr;  // set while tuning
+static thread_local TuneKey g_last_key{-1, -1, -1, -1};  // class of the last batch
+static thread_local bool g_last_eligible = false;         // ... packed-eligible
+
+static int ilog2_64(int64_t x) {
+  int r = 0;
+  while (x > 1) {
+    x >>= 1;
+    ++r;
+  }
+  return r;
+}
+
 static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
                         const int64_t *a_off, const int32_t *a_len, const int64_t *b_off,
                         const int32_t *b_len, int32_t policy, const int32_t *deltaw,
@@ -275,7 +313,29 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   // POYD_PACKED=0 keeps the 32-bit kernel.
   bool packed = !(tl.err & 16) && mode != kDpSets;
   if (const char *e = std::getenv("POYD_PACKED")) packed = packed && std::atoi(e) != 0;
-  const int blocks = packed ? lin_dp4_blocks(mode) : lin_dp_blocks(mode);
+  // the launch variant of this batch's shape class (autotuner)
+  LinVariant var{-1, 0, -1};
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    g_last_key = TuneKey(dev, mode == kDpChoice ? 1 : 0, ilog2_64(n), ilog2_64(maxwd));
+    g_last_eligible = packed;
+    if (g_force) {
+      var = *g_force;
+    } else if (mode != kDpSets) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(g_last_key);
+      if (it != g_tune.end()) var = it->second;
+    }
+  }
+  if (var.packed == 0) packed = false;
+  int blocks = packed ? lin_dp4_blocks(mode) : lin_dp_blocks(mode);
+  if (var.blocks_per_sm > 0) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    blocks = std::min(blocks, var.blocks_per_sm * std::max(sms, 1));
+  }
   const int warps = packed ? lin_dp4_warps() : kDpWarps;
   const int64_t slab = maxwd + 64;
   int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * warps);
@@ -311,7 +371,8 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
     DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
     DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
     DA.done = (ls && fuse && wave_at.size() == 2) ? ls->done : nullptr;
-    DA.tb_solo = (fuse && packed && !DA.done && (int64_t)m <= (int64_t)blocks * warps) ? 1 : 0;
+    DA.tb_solo = (fuse && packed && !DA.done && (int64_t)m <= (int64_t)blocks * warps &&
+                  var.solo != 0) ? 1 : 0;
     {
       ProfScope ps(want_align ? "lin_dp_dm" : "lin_dp_cost", st);
       if (packed) launch_lin_dp4(DA, mode, blocks, st);
@@ -599,4 +660,157 @@ extern "C" int poyd_algn_align_affine_3(const uint8_t *si, int32_t li, const uin
                                         uint8_t *resj, uint8_t *median, uint8_t *medianwg,
                                         int32_t cap, int32_t *lens, int32_t *cost) {
   return affine_one(si, li, sj, lj, cm, true, resi, resj, median, medianwg, cap, lens, cost);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner entry points (see LinVariant above).
+// ---------------------------------------------------------------------------
+extern "C" int poyd_autotune_set(int32_t device, int32_t align, int32_t lg_pairs,
+                                 int32_t lg_width, int32_t packed, int32_t blocks_per_sm,
+                                 int32_t solo) {
+  if (packed < -1 || packed > 1 || solo < -1 || solo > 1 || blocks_per_sm < 0)
+    return fail(POYD_EINVAL, "autotune: packed and solo are -1, 0 or 1; blocks_per_sm >= 0");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[TuneKey(device, align ? 1 : 0, lg_pairs, lg_width)] = LinVariant{packed, blocks_per_sm, solo};
+  return POYD_OK;
+}
+
+extern "C" int poyd_autotune_get(int32_t device, int32_t align, int32_t lg_pairs,
+                                 int32_t lg_width, int32_t *packed, int32_t *blocks_per_sm,
+                                 int32_t *solo) {
+  if (!packed || !blocks_per_sm || !solo) return fail(POYD_EINVAL, "autotune: null argument");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(TuneKey(device, align ? 1 : 0, lg_pairs, lg_width));
+  if (it == g_tune.end()) return 0;
+  *packed = it->second.packed;
+  *blocks_per_sm = it->second.blocks_per_sm;
+  *solo = it->second.solo;
+  return 1;
+}
+
+extern "C" int poyd_autotune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return POYD_OK;
+}
+
+namespace {
+struct ForceGuard {  // the forced variant lasts for one scope only
+  explicit ForceGuard(const LinVariant *v) { g_force = v; }
+  ~ForceGuard() { g_force = nullptr; }
+};
+}  // namespace
+
+extern "C" int poyd_autotune_batch(const poyd_cm *cm, int32_t align, int32_t n,
+                                   const uint8_t *seq, const int64_t *a_off, const int32_t *a_len,
+                                   const int64_t *b_off, const int32_t *b_len,
+                                   int32_t deltaw_policy, int32_t *cost, uint8_t *out,
+                                   const int64_t *out_off, int32_t *out_len, int32_t flags,
+                                   int32_t reps, poyd_tune_result *res, void *stream) {
+  int maxc = 0;
+  int rc = check_cm(cm, &maxc);
+  if (rc) return rc;
+  if (cm->cost_model != 0) return fail(POYD_EUNSUP, "autotune: linear model only");
+  if (n <= 0 || !seq || !a_off || !a_len || !b_off || !b_len || !cost || !res ||
+      (align && (!out || !out_off || !out_len)))
+    return fail(POYD_EINVAL, "poyd_autotune_batch: null argument or empty batch");
+  if (deltaw_policy == POYD_DELTAW_EXPLICIT || deltaw_policy == POYD_DELTAW_RAW)
+    return fail(POYD_EINVAL, "autotune: deltaw policies with a per-pair array are not tuned");
+  cudaStream_t st = (cudaStream_t)stream;
+  auto run = [&]() -> int {
+    return align ? poyd_align_2_batch(cm, n, seq, a_off, a_len, b_off, b_len, cost, out, out_off,
+                                      out_len, nullptr, flags, stream)
+                 : poyd_cost_2_batch(cm, n, seq, a_off, a_len, b_off, b_len, deltaw_policy,
+                                     nullptr, cost, nullptr, stream);
+  };
+  // the defaults first: the batch's class, and the results every variant
+  // must reproduce
+  const LinVariant dflt{-1, 0, -1};
+  {
+    ForceGuard g(&dflt);
+    rc = run();
+  }
+  if (rc) return rc;
+  const TuneKey key = g_last_key;
+  const bool eligible = g_last_eligible;
+  std::vector<int32_t> ref_cost((size_t)n), ref_len(align ? 2 * (size_t)n : 0), chk;
+  CK(cudaMemcpyAsync(ref_cost.data(), cost, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  if (align)
+    CK(cudaMemcpyAsync(ref_len.data(), out_len, sizeof(int32_t) * 2 * (size_t)n,
+                       cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  sms = std::max(sms, 1);
+  const int mode = align ? kDpChoice : kDpCost;
+  std::vector<LinVariant> cands;
+  for (int pk = eligible ? 1 : 0; pk >= 0; --pk) {
+    const int maxb = (pk ? lin_dp4_blocks(mode) : lin_dp_blocks(mode)) / sms;
+    for (int b = std::max(maxb, 1); b >= 1 && (int)cands.size() < kTuneMax; --b) {
+      const bool small = align && pk && (int64_t)n <= (int64_t)b * sms * lin_dp4_warps();
+      cands.push_back(LinVariant{pk, b, small ? 1 : -1});
+      if (small && (int)cands.size() < kTuneMax) cands.push_back(LinVariant{pk, b, 0});
+    }
+  }
+  reps = std::max(reps, 1);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int best = -1;
+  float best_ms = 0.f;
+  res->n_variants = (int32_t)cands.size();
+  for (size_t c = 0; c < cands.size(); ++c) {
+    ForceGuard g(&cands[c]);
+    rc = run();  // warm-up, and the result check below
+    if (!rc) {
+      CK(cudaEventRecord(e0, st));
+      for (int r = 0; r < reps && !rc; ++r) rc = run();
+      CK(cudaEventRecord(e1, st));
+    }
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= (float)reps;
+    chk.resize((size_t)n);
+    CK(cudaMemcpy(chk.data(), cost, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost));
+    bool same = chk == ref_cost;
+    if (same && align) {
+      chk.resize(2 * (size_t)n);
+      CK(cudaMemcpy(chk.data(), out_len, sizeof(int32_t) * 2 * (size_t)n, cudaMemcpyDeviceToHost));
+      same = chk == ref_len;
+    }
+    if (!same) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(POYD_ERANGE, "autotune: variant %d (packed %d, %d blocks per SM, solo %d) "
+                  "changed the results", (int)c, cands[c].packed, cands[c].blocks_per_sm,
+                  cands[c].solo);
+    }
+    res->ms[c] = ms;
+    res->variant[c][0] = cands[c].packed;
+    res->variant[c][1] = cands[c].blocks_per_sm;
+    res->variant[c][2] = cands[c].solo;
+    if (best < 0 || ms < best_ms) {
+      best = (int)c;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = cands[(size_t)best];
+  }
+  res->packed = cands[(size_t)best].packed;
+  res->blocks_per_sm = cands[(size_t)best].blocks_per_sm;
+  res->solo = cands[(size_t)best].solo;
+  res->lg_pairs = std::get<2>(key);
+  res->lg_width = std::get<3>(key);
+  return POYD_OK;
 }

@@ -52,11 +52,22 @@ class PoydNodeStore(C.Structure):
     ]
 
 
+class PoydTuneResult(C.Structure):
+    """``poyd_tune_result`` (include/poyd_gb300.h)."""
+
+    _fields_ = [
+        ("packed", C.c_int32), ("blocks_per_sm", C.c_int32), ("solo", C.c_int32),
+        ("lg_pairs", C.c_int32), ("lg_width", C.c_int32), ("n_variants", C.c_int32),
+        ("ms", C.c_float * 8), ("variant", (C.c_int32 * 3) * 8),
+    ]
+
+
 # Every entry point the public header declares (include/poyd_gb300.h);
 # tests check the header's declarations against this list and that the
 # library exports each of them.
 EXPORTED = (
-    "poyd_adam_step", "poyd_algn_align_2d", "poyd_algn_align_affine_3", "poyd_algn_ancestor_2",
+    "poyd_adam_step", "poyd_autotune_batch", "poyd_autotune_clear", "poyd_autotune_get",
+    "poyd_autotune_set", "poyd_algn_align_2d", "poyd_algn_align_affine_3", "poyd_algn_ancestor_2",
     "poyd_algn_backtrack_2d", "poyd_algn_cost_affine_3", "poyd_algn_median_2_no_gaps",
     "poyd_algn_median_2_with_gaps", "poyd_algn_simple_2", "poyd_algn_verify_2",
     "poyd_algn_worst_2", "poyd_align_2_batch", "poyd_align_2_host", "poyd_ancestor_2_batch",
@@ -91,6 +102,12 @@ SIGNATURES = [
     ("poyd_median_levels", C.c_int, [_cmp, C.POINTER(PoydNodeStore), _i32, _vp, _vp, _i32, _vp,
                                      _vp, _vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                      _vp, _vp]),
+    ("poyd_autotune_batch", C.c_int, [_cmp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _vp,
+                                      _vp, _vp, _i32, _i32, C.POINTER(PoydTuneResult), _vp]),
+    ("poyd_autotune_set", C.c_int, [_i32] * 7),
+    ("poyd_autotune_get", C.c_int, [_i32, _i32, _i32, _i32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("poyd_autotune_clear", C.c_int, []),
     ("poyd_profile_enable", C.c_int, [C.c_int]),
     ("poyd_profile_read", C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int]),
     ("poyd_launch_count", C.c_longlong, []),

@@ -209,3 +209,29 @@ def test_median_levels_argument_checks_without_a_gpu(lib):
     assert rc == ESPACE and need == bound and b"pool too small" in msg
     assert np.array_equal(ln, [100, 120, 90, 0, 0, 0, 0, 0])   # nothing changed
     assert call([0, 0], [], [], [])[0] == 0                     # no pairs: a no-op
+
+
+def test_autotune_table_without_a_gpu(lib):
+    """The autotuner's kept variants: set, read back, cleared; bad values
+    and arguments refused (host tables only)."""
+    L = native.lib()
+    assert L.poyd_autotune_clear() == 0
+    p, b, s = C.c_int32(), C.c_int32(), C.c_int32()
+    assert L.poyd_autotune_get(0, 1, 16, 7, C.byref(p), C.byref(b), C.byref(s)) == 0
+    assert L.poyd_autotune_set(0, 1, 16, 7, 0, 2, -1) == 0
+    assert L.poyd_autotune_get(0, 1, 16, 7, C.byref(p), C.byref(b), C.byref(s)) == 1
+    assert (p.value, b.value, s.value) == (0, 2, -1)
+    assert L.poyd_autotune_get(0, 0, 16, 7, C.byref(p), C.byref(b), C.byref(s)) == 0  # cost mode
+    assert L.poyd_autotune_set(0, 1, 16, 7, 2, 1, 0) == -1     # packed is -1, 0 or 1
+    assert L.poyd_autotune_set(0, 1, 16, 7, 1, -1, 0) == -1    # blocks per SM >= 0
+    assert L.poyd_autotune_get(0, 1, 16, 7, None, C.byref(b), C.byref(s)) == -1
+    assert L.poyd_autotune_clear() == 0
+    assert L.poyd_autotune_get(0, 1, 16, 7, C.byref(p), C.byref(b), C.byref(s)) == 0
+    # an affine matrix or an empty batch is refused before any CUDA call
+    res = native.PoydTuneResult()
+    aff = _dna(lib, 3)
+    assert L.poyd_autotune_batch(C.byref(aff), 1, 4, None, None, None, None, None, 0, None,
+                                 None, None, None, 0, 1, C.byref(res), None) == -5
+    lin = _dna(lib)
+    assert L.poyd_autotune_batch(C.byref(lin), 1, 0, None, None, None, None, None, 0, None,
+                                 None, None, None, 0, 1, C.byref(res), None) == -1
