@@ -139,16 +139,31 @@ class Tree:
             self.parent[other[j - 1]] = path[j]
             self.parent[nxt] = path[j]
 
+    def _memo(self, name, fn):
+        """fn() cached until the tree's root or children change (compared
+        exactly; trees are also built by writing the arrays directly)."""
+        key = (int(self.root), self.kids.tobytes())
+        memo = self.__dict__.setdefault("_cache", {})
+        hit = memo.get(name)
+        if hit is not None and hit[0] == key:
+            return hit[1]
+        val = fn()
+        memo[name] = (key, val)
+        return val
+
     def nodes(self):
-        """Preorder (a node before its children, the second child first)."""
-        kids, n = self.kids.tolist(), self.n
-        out, stack = [], [int(self.root)]
-        while stack:
-            v = stack.pop()
-            out.append(v)
-            if v >= n:
-                stack.extend(kids[v])
-        return out
+        """Preorder (a node before its children, the second child first).
+        The list is shared by later calls on the same tree: do not modify it."""
+        def walk():
+            kids, n = self.kids.tolist(), self.n
+            out, stack = [], [int(self.root)]
+            while stack:
+                v = stack.pop()
+                out.append(v)
+                if v >= n:
+                    stack.extend(kids[v])
+            return out
+        return self._memo("nodes", walk)
 
     def subtree(self, s: int):
         out, stack = [], [s]
@@ -162,13 +177,15 @@ class Tree:
     def min_codes(self) -> np.ndarray:
         """Smallest leaf id under every node (POY's ``min_child_code``,
         node.ml:674; a leaf's is its own taxon code)."""
-        kids, n = self.kids.tolist(), self.n
-        mc = list(range(len(self.parent)))
-        for v in self.nodes()[::-1]:
-            if v >= n:
-                a, b = kids[v]
-                mc[v] = min(mc[a], mc[b])
-        return np.array(mc, np.int64)
+        def compute():
+            kids, n = self.kids.tolist(), self.n
+            mc = list(range(len(self.parent)))
+            for v in self.nodes()[::-1]:
+                if v >= n:
+                    a, b = kids[v]
+                    mc[v] = min(mc[a], mc[b])
+            return np.array(mc, np.int64)
+        return self._memo("min_codes", compute).copy()
 
     def levels(self):
         """Internal nodes grouped by height (all children before parents)."""
@@ -910,15 +927,18 @@ def _valid_move(t: Tree, s: int, e: int) -> bool:
 
 
 def _heights(t: Tree) -> dict:
-    kids, n = t.kids.tolist(), t.n
-    h = {}
-    for v in t.nodes()[::-1]:
-        if v < n:
-            h[v] = 0
-        else:
-            a, b = kids[v]
-            h[v] = 1 + max(h[a], h[b])
-    return h
+    """Height of every node of the tree (leaves 0); shared, do not modify."""
+    def compute():
+        kids, n = t.kids.tolist(), t.n
+        h = {}
+        for v in t.nodes()[::-1]:
+            if v < n:
+                h[v] = 0
+            else:
+                a, b = kids[v]
+                h[v] = 1 + max(h[a], h[b])
+        return h
+    return t._memo("heights", compute)
 
 
 def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarray:
@@ -937,60 +957,113 @@ def evaluate_moves(t: Tree, be, diag: Diagnosis, moves, detail=None) -> np.ndarr
     return evaluate_trials(t, be, diag, [[mv] for mv in moves], detail)
 
 
+def _spr_overlay(par, kids, root, trial):
+    """The parents and children a trial of SPR moves (s, e) changes, applied
+    in order over the base tree's lists exactly as ``Tree.prune`` and
+    ``Tree.insert`` would (the pruned parent node is the inserted one);
+    returns (parent changes, children changes, root, prune and regraft
+    points)."""
+    P, K = {}, {}
+    gp = lambda v: P[v] if v in P else par[v]
+    gk = lambda v: K[v] if v in K else kids[v]
+    starts = []
+    for mv in trial:
+        s, e = int(mv[0]), int(mv[1])
+        p = gp(s)
+        kp = gk(p)
+        o = kp[0] if kp[1] == s else kp[1]
+        g = gp(p)
+        P[o] = g
+        if g < 0:
+            root = o
+        else:
+            kg = list(gk(g))
+            kg[0 if kg[0] == p else 1] = o
+            K[g] = kg
+        P[p] = P[s] = -1
+        K[p] = [-1, -1]
+        q = gp(e)
+        K[p] = [e, s]
+        P[p], P[e], P[s] = q, p, p
+        if q < 0:
+            root = p
+        else:
+            kq = list(gk(q))
+            kq[0 if kq[0] == e else 1] = p
+            K[q] = kq
+        starts += [g, p]
+    return P, K, root, starts
+
+
 def evaluate_trials(t: Tree, be, diag: Diagnosis, trials, detail=None) -> np.ndarray:
     """``evaluate_moves`` for trials of several moves applied in order (each
     in the tree the previous ones left): the dirty nodes are the ancestors,
     in the trial's final tree, of every move's prune and regraft points and
-    re-rooted path nodes."""
+    re-rooted path nodes.  Trials of SPR moves only are applied as overlays
+    of the changed parents and children over the base tree; TBR moves on a
+    copy of the tree."""
     h_base = _heights(t)
-    mc_base = t.min_codes()
+    mcb = t.min_codes().tolist()
     base_sank = be.sank_cost(t.root)
     tid_next = 2 * t.n
     recs = {}      # level -> list of (trial, a_ref, b_ref, out_tid)
     old = np.zeros(len(trials), np.int64)
     roots = []
+    spr_only = all(len(mv) == 2 for trial in trials for mv in trial)
+    if spr_only:
+        par_l = t._memo("parent_list", lambda: t.parent.tolist())
+        kids_l = t._memo("kids_list", lambda: t.kids.tolist())
     for m, trial in enumerate(trials):
-        T = t.copy()
-        starts = []
-        for mv in trial:
-            s, e = int(mv[0]), int(mv[1])
-            u = int(mv[2]) if len(mv) > 2 else -1
-            if u >= 0:
-                T.reroot(s, u)
-                starts += [v for v in T.subtree(s)
-                           if v >= T.n and set(T.kids[v].tolist()) != set(t.kids[v].tolist())]
-            p = T.parent[s]
-            starts.append(int(T.parent[p]))
-            w = T.prune(s)
-            T.insert(s, e, w)
-            starts.append(int(w))
+        if spr_only:
+            P, K, root_m, starts = _spr_overlay(par_l, kids_l, int(t.root), trial)
+            gp = lambda v, P=P: P[v] if v in P else par_l[v]
+            gk = lambda v, K=K: K[v] if v in K else kids_l[v]
+        else:
+            T = t.copy()
+            starts = []
+            for mv in trial:
+                s, e = int(mv[0]), int(mv[1])
+                u = int(mv[2]) if len(mv) > 2 else -1
+                if u >= 0:
+                    T.reroot(s, u)
+                    starts += [v for v in T.subtree(s)
+                               if v >= T.n and set(T.kids[v].tolist()) != set(t.kids[v].tolist())]
+                p = T.parent[s]
+                starts.append(int(T.parent[p]))
+                w = T.prune(s)
+                T.insert(s, e, w)
+                starts.append(int(w))
+            gp = lambda v, T=T: int(T.parent[v])
+            gk = lambda v, T=T: T.kids[v].tolist()
+            root_m = int(T.root)
         dirty = set()
         for v in starts:
             while v >= 0 and v not in dirty:
                 dirty.add(v)
-                v = T.parent[v]
+                v = gp(v)
         h, tid = {}, {}
 
         def height(v):
             if v not in dirty:
                 return h_base[v]
             if v not in h:
-                h[v] = 1 + max(height(T.kids[v][0]), height(T.kids[v][1]))
+                a, b = gk(v)
+                h[v] = 1 + max(height(a), height(b))
             return h[v]
 
         mc = {}   # min codes of the trial tree's dirty nodes
-        code = lambda c: mc[c] if c in dirty else mc_base[c]
+        code = lambda c: mc[c] if c in dirty else mcb[c]
         for v in sorted(dirty, key=height):
             tid[v] = tid_next
             tid_next += 1
-            a, b = T.kids[v]
+            a, b = gk(v)
             if code(a) > code(b):
                 a, b = b, a
             mc[v] = code(a)
             ref = lambda c: tid[c] if c in dirty else c
             recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v], v))
             old[m] += diag.do_cost[v] + diag.fitch_cost[v]
-        roots.append(tid[T.root])
+        roots.append(tid[root_m])
     be.ensure_nodes(tid_next)
     new = np.zeros(len(trials), np.int64)
     rs = [np.array(recs[lvl], np.int64) for lvl in sorted(recs)]

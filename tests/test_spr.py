@@ -43,3 +43,30 @@ def test_distinct_nodes_matches_unique():
         ids = rng.integers(0, 700, n)
         assert np.array_equal(search.distinct_nodes(ids, 700), np.unique(ids))
     assert search.distinct_nodes(np.zeros(0, np.int64), 10).dtype == np.int64
+
+
+def test_overlay_evaluation_equals_tree_copies():
+    """SPR trials applied as overlays over the base tree (evaluate_trials'
+    fast path) give the totals and recomputed nodes of the same trials
+    applied to tree copies (the path TBR moves take; (s, e, -1) is an SPR
+    move written as TBR without re-rooting), single moves and pairs."""
+    data = simulate.simulate(4, 18, 60, 8, 2)
+    be = OracleBackend(data, O.cm_dna(1, 2, -1))
+    t = learned.random_tree(data.n_taxa, 5)
+    diag = search.downpass(t, be)
+    S, E = search.spr_candidates(t)
+    rng = np.random.default_rng(0)
+    pick = rng.choice(len(S), size=12, replace=False)
+    moves = [(int(S[i]), int(E[i])) for i in pick]
+    trials = [[m] for m in moves]
+    for a in moves[:4]:
+        tg = t.copy()
+        tg.insert(a[0], a[1], tg.prune(a[0]))
+        trials += [[a, b] for b in moves[4:] if search._valid_move(tg, *b)]
+    d1, d2 = {}, {}
+    r1 = search.evaluate_trials(t, be, diag, trials, d1)
+    be.release_nodes(2 * t.n)
+    r2 = search.evaluate_trials(t, be, diag, [[(s, e, -1) for s, e in tr] for tr in trials], d2)
+    be.release_nodes(2 * t.n)
+    assert np.array_equal(r1, r2) and len(trials) > 12
+    assert d1 == d2
