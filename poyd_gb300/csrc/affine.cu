@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <numeric>
 #include <vector>
 #include "affine_kernels.cuh"
@@ -92,6 +93,7 @@ struct AffDpArgs {
   int64_t slab;
   uint32_t *dm;
   int32_t *cost;
+  int32_t *err;  // k_aff_dp2: bit 8 when a final cost is past its exact range
 };
 
 struct AffTbArgs {
@@ -377,6 +379,368 @@ __device__ __forceinline__ void aff_pair(const AffDpArgs &A, AffSmem &sm, int wa
   if (k == 0 && has) A.cost[id] = r;
 }
 
+// ---------------------------------------------------------------------------
+// Packed affine DP (k_aff_dp2): two pairs per lane group, pair A in the low
+// 16-bit half of every register and pair B in the high half, so one
+// instruction advances two cells.  Values are kept times four with the two
+// low bits free: every minimum takes its candidates tagged with the rank
+// the reference's tie rule gives them, so the winner's rank is the choice
+// and clearing the bits gives the value:
+//   todo   = min(EH|0, CB|1, EV|2, EB|3)         (DO_HORIZONTAL > DO_ALIGN >
+//                                                 DO_VERTICAL > DO_DIAGONAL)
+//   achoice = min(fh|0, fd|1, fv|2, fa|3)        (ALIGN_TO_HORIZONTAL >
+//                                                 _DIAGONAL > _VERTICAL)
+//   END_x  = the opening candidate (rank 0) wins ties against the
+//            extension (rank 1): `ext < open ? 0 : END` of the cell rules.
+// HIGH_NUM becomes the 16-bit infinity 0xC000: every add of a cost
+// saturates there (__viaddmin_u16x2 with the infinity as the bound; a cost
+// is far below the 0x4000 headroom), and where the reference adds HIGH_NUM
+// itself the infinity is selected instead.  Exactness: the
+// values on a pair's optimal path are at most its final cost, and every
+// choice the traceback reads at a path cell compares a path value with
+// candidates that are either exact or saturated above it.  So the results
+// are the reference's whenever the final cost is below kAffPackLim (every
+// path value x4 plus one step's largest add stays below the infinity); a
+// pair above it sets error bit 8 and the host runs the batch again on the
+// 32-bit kernel.  The direction bytes have k_aff_dp's layout, per pair, so
+// k_aff_traceback reads them unchanged.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kInfA2 = 0xC000C000u;   // the infinity in both halves
+constexpr uint32_t kLo1 = 0x00010001u;
+constexpr uint32_t kRk = 0x00030003u;      // the rank bits of both halves
+constexpr int kAffPackLim = 12000;         // final costs below this are exact
+
+struct AffSmem2 {
+  uint32_t tab[1024];            // packed {cost[a][b], cost[gap][b]}
+  uint16_t cost4[1024];          // 4 * cost[a][b]
+  uint4 col[kAffWarps][kAffGroups][64];   // both pairs' columns (x4 costs, characters)
+  uint4 ring_in[kAffWarps][kAffGroups][32];
+  uint4 ring_out[kAffWarps][kAffGroups][32];
+};
+
+__device__ __forceinline__ uint32_t am2(uint32_t a, uint32_t b) {
+  return __viaddmin_u16x2(a, b, kInfA2);  // saturating add, both halves
+}
+// min / max per half as the fused add-min / add-max with a zero addend (one
+// instruction each; the plain SIMD min and max are not)
+__device__ __forceinline__ uint32_t mn2(uint32_t a, uint32_t b) { return __viaddmin_u16x2(a, 0u, b); }
+__device__ __forceinline__ uint32_t mx2(uint32_t a, uint32_t b) { return __viaddmax_u16x2(a, 0u, b); }
+// selects b where m is all ones, else a (m: 0 / 0xFFFF per half)
+__device__ __forceinline__ uint32_t sel2(uint32_t a, uint32_t b, uint32_t m) {
+  return (a & ~m) | (b & m);
+}
+
+// Column quantities of both pairs (aff_column, times four), one half each.
+__device__ __forceinline__ uint4 aff_column2(const uint32_t *tab, int jca, int jpa, int jcb,
+                                            int jpb, int j, int go) {
+  const int4 a = aff_column(tab, jca, jpa, j, go), b = aff_column(tab, jcb, jpb, j, go);
+  return make_uint4((uint32_t)(4 * a.x) | ((uint32_t)(4 * b.x) << 16),
+                    (uint32_t)(4 * a.y) | ((uint32_t)(4 * b.y) << 16),
+                    (uint32_t)(4 * a.z) | ((uint32_t)(4 * b.z) << 16),
+                    (uint32_t)a.w | ((uint32_t)b.w << 16));
+}
+
+struct AffRow2 {
+  uint32_t vext, vopen, sopen;  // 4 * si_vext, 4 * (si_open + si_ext), 4 * si_open
+  uint32_t icg;                 // 0xFFFF in a half whose row character has the gap bit
+  const uint16_t *srowA, *srowB;  // 4 * cost[ic & 15][.] of each pair
+  int i;
+  uint32_t specL, specRA, specRB;  // bit u: step u of the half block is a boundary cell
+  uint32_t spec;                   // any of the three
+  int uFA, uFB;                    // step of each pair's final cell in the half block
+};
+struct AffState2 {
+  uint32_t eh_l, cb_l;
+  uint32_t eh_d, ev_d, eb_d, cb_d;
+  uint32_t m_eh, m_ev, m_eb, m_cb;
+  uint32_t wA, wB;
+  int resA, resB;
+};
+
+// ENDS: the strip holds row 0 or a pair's last row.  Boundary cells (left
+// and right of the band) are handled under a per-step test of the lane's
+// bits: choosing between copies of the half block per half block (by a
+// warp vote) measured 40 % slower, and computing the masks on every step
+// 4 % slower.
+template <bool BT, bool ENDS>
+__device__ __forceinline__ void aff2_half(AffState2 &S, const AffRow2 &R, const uint4 *clane,
+                                          const uint4 *rin, uint4 *rout, int s0, uint32_t go4,
+                                          uint32_t go8, uint32_t *dmA, uint32_t *dmB, int lane) {
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    uint32_t u_eh = __shfl_up_sync(kFullA, S.m_eh, 1, kAffRows);
+    uint32_t u_ev = __shfl_up_sync(kFullA, S.m_ev, 1, kAffRows);
+    uint32_t u_eb = __shfl_up_sync(kFullA, S.m_eb, 1, kAffRows);
+    uint32_t u_cb = __shfl_up_sync(kFullA, S.m_cb, 1, kAffRows);
+    if (lane == 0) {
+      const uint4 v = rin[u];
+      u_eh = v.x; u_ev = v.y; u_eb = v.z; u_cb = v.w;
+    }
+    const uint4 D = clane[u];  // {hext, sj_open + sj_ext, sj_open} x4, characters
+    const uint32_t jg = ((D.w >> 4) & kLo1) * 0xFFFFu;  // column character has the gap bit
+    // FILL_EXTEND_HORIZONTAL: extension (rank 1) against opening (rank 0)
+    const uint32_t ehr = mn2(am2(S.eh_l, D.x) | kLo1, am2(S.cb_l, D.y));
+    // FILL_EXTEND_VERTICAL
+    const uint32_t v1 = am2(u_ev, R.vext);
+    const uint32_t evr = mn2(v1 | kLo1, am2(u_cb, R.vopen));
+    // FILL_EXTEND_BLOCK_DIAGONAL[_NOBT]: the HIGH_NUM terms are selected,
+    // not added (an infinite operand plus the infinity would wrap)
+    const uint32_t both = R.icg & jg;
+    const uint32_t b2 = sel2(kInfA2, BT ? S.cb_d : am2(S.cb_d, go8), both);
+    const uint32_t ebr = mn2(sel2(kInfA2, S.eb_d, both) | kLo1, b2);
+    // FILL_CLOSE_BLOCK_DIAGONAL, achoice ranks fh 0, fd 1, fv 2, fa 3
+    const uint32_t cd = (uint32_t)R.srowA[D.w & 15u] | ((uint32_t)R.srowB[(D.w >> 16) & 15u] << 16);
+    const uint32_t fh = am2(S.eh_d, cd + (R.sopen & jg));
+    const uint32_t fd = am2(S.eb_d, cd + mx2(D.z, R.sopen)) | kLo1;
+    const uint32_t fv = am2(S.ev_d, cd + (D.z & R.icg)) | (2u * kLo1);
+    const uint32_t fa = am2(S.cb_d, cd) | kRk;
+    const uint32_t cbr = mn2(mn2(fh, fd), mn2(fv, fa));
+    uint32_t eh = ehr & ~kRk, ev = evr & ~kRk, eb = ebr & ~kRk, cb = cbr & ~kRk;
+    // ASSIGN_MINIMUM, todo ranks EH 0, CB 1, EV 2, EB 3
+    uint32_t f = mn2(mn2(eh, cb | kLo1), mn2(ev | (2u * kLo1), eb | kRk));
+    uint32_t code = 0;
+    if (BT)
+      code = (f & kRk) | ((~evr & kLo1) << 2) | ((~ehr & kLo1) << 3) | ((~ebr & kLo1) << 4) |
+             ((cbr & kRk) << 5);
+    f &= ~kRk;
+    bool row0 = false;
+    if (ENDS && R.i == 0) {  // initialize_matrices_affine row 0 (both pairs: j = d)
+      row0 = true;
+      if (kDlo + s0 + u - 2 * lane == 0) {
+        eh = go4; ev = go4; eb = 0; cb = 0; f = 0;
+      } else {
+        eh = am2(S.eh_l, D.y - D.z);
+        cb = eh; eb = kInfA2; ev = kInfA2; f = eh;
+      }
+    }
+    if (!row0 && ((R.spec >> u) & 1u)) {
+      // the vertical boundary cell left of the band (the same step in both
+      // pairs: one row) and each pair's HIGH_NUM cell right of it
+      const uint32_t mL = (R.specL >> u) & 1u ? 0xFFFFFFFFu : 0u;
+      const uint32_t mR = ((R.specRA >> u) & 1u ? 0xFFFFu : 0u) |
+                          ((R.specRB >> u) & 1u ? 0xFFFF0000u : 0u);
+      const uint32_t mLR = mL | mR;
+      eh = sel2(eh, kInfA2, mLR);
+      cb = sel2(cb, kInfA2, mLR);
+      eb = sel2(eb, kInfA2, mLR);
+      ev = sel2(sel2(ev, v1, mL), kInfA2, mR);
+      f = sel2(f, ev, mL);
+      if (BT)
+        code = sel2(code, (kCodeLeft * kLo1 & mL) | (kCodeRight * kLo1 & mR), mLR & 0x00FF00FFu);
+    }
+    if (ENDS) {
+      if (u == R.uFA) S.resA = (int)(f & 0xFFFFu);
+      if (u == R.uFB) S.resB = (int)(f >> 16);
+    }
+    if (BT) {
+      S.wA = __byte_perm(S.wA, code, 0x2104);  // (wA << 8) | code byte 0
+      S.wB = __byte_perm(S.wB, code, 0x2106);  // (wB << 8) | code byte 2
+      if ((u & 3) == 3) {
+        if (dmA) dmA[(u >> 2) * kAffRows] = S.wA;
+        if (dmB) dmB[(u >> 2) * kAffRows] = S.wB;
+      }
+    }
+    S.m_eh = eh; S.m_ev = ev; S.m_eb = eb; S.m_cb = cb;
+    if (lane == kAffRows - 1) rout[u] = make_uint4(eh, ev, eb, cb);
+    S.eh_d = u_eh; S.ev_d = u_ev; S.eb_d = u_eb; S.cb_d = u_cb;
+    S.eh_l = eh; S.cb_l = cb;
+  }
+}
+
+// Bit u of the mask: step s0 + u is in [st, st + 16) at st.
+__device__ __forceinline__ uint32_t step_bit(int st, int hs) {
+  const int u = st - hs;
+  return (u >= 0 && u < 16) ? (1u << u) : 0u;
+}
+
+// Two pairs per lane group (A low half, B high half), kAffGroups groups per
+// warp; the warp runs its strips, blocks and half blocks to the largest
+// pair's bounds, like aff_pair.
+template <bool BT>
+__device__ __forceinline__ void aff2_pairs(const AffDpArgs &A, AffSmem2 &sm, int warp,
+                                           const AffPlan &PA, const AffPlan &PB, bool hasA,
+                                           bool hasB, int64_t offA, int64_t offB, int idA,
+                                           int idB, uint4 *bnd, int lane) {
+  const int h = lane / kAffRows, k = lane & (kAffRows - 1);
+  const uint8_t *siA = A.seq + PA.si_off, *sjA = A.seq + PA.sj_off;
+  const uint8_t *siB = A.seq + PB.si_off, *sjB = A.seq + PB.sj_off;
+  const int go = A.go;
+  const uint32_t go4 = 4u * (uint32_t)go * kLo1, go8 = 8u * (uint32_t)go * kLo1;
+  const int ThA = hasA ? PA.nstrips : 0, ThB = hasB ? PB.nstrips : 0;
+  const int ShA = hasA ? PA.sblocks * 4 : 0, ShB = hasB ? PB.sblocks * 4 : 0;
+  const int T = __reduce_max_sync(kFullA, max(ThA, ThB));
+  uint4 *win = sm.col[warp][h];
+  uint4 *rin = sm.ring_in[warp][h], *rout = sm.ring_out[warp][h];
+  const uint4 *wl = win + kAffRows - k;
+  const uint4 kInf4 = make_uint4(kInfA2, kInfA2, kInfA2, kInfA2);
+  AffState2 S;
+  S.resA = S.resB = 0;
+  uint32_t *dmbaseA = (BT && hasA) ? A.dm + offA : nullptr;
+  uint32_t *dmbaseB = (BT && hasB) ? A.dm + offB : nullptr;
+
+  for (int strip = 0; strip < T; ++strip) {
+    const bool actA = strip < ThA, actB = strip < ThB;
+    const int Spad = __reduce_max_sync(kFullA, max(actA ? ShA : 0, actB ? ShB : 0));
+    const bool ends = __any_sync(kFullA, strip == 0 || (actA && strip == ThA - 1) ||
+                                             (actB && strip == ThB - 1));
+    const int r0 = strip * kAffRows;
+    AffRow2 R;
+    R.i = r0 + k;
+    const bool okA = actA && R.i <= PA.leni, okB = actB && R.i <= PB.leni;
+    const int icA = okA ? siA[R.i] : 0, ipA = (okA && R.i > 0) ? siA[R.i - 1] : 0;
+    const int icB = okB ? siB[R.i] : 0, ipB = (okB && R.i > 0) ? siB[R.i - 1] : 0;
+    auto rowq = [&](int ic, int ip, uint32_t &vext, uint32_t &vopen, uint32_t &sopen) {
+      const int si_ext = (int)(sm.tab[(ic << 5) | 16] & 0xffffu);
+      const int si_open = (!(ip & 16) && (ic & 16)) ? 0 : go;
+      const int si_vext = (R.i > 1 && (ip & 16) && !(ic & 16)) ? si_open + si_ext : si_ext;
+      vext = 4u * (uint32_t)si_vext;
+      vopen = 4u * (uint32_t)(si_open + si_ext);
+      sopen = 4u * (uint32_t)si_open;
+    };
+    uint32_t xa, ya, za, xb, yb, zb;
+    rowq(icA, ipA, xa, ya, za);
+    rowq(icB, ipB, xb, yb, zb);
+    R.vext = xa | (xb << 16);
+    R.vopen = ya | (yb << 16);
+    R.sopen = za | (zb << 16);
+    R.icg = ((icA & 16) ? 0xFFFFu : 0u) | ((icB & 16) ? 0xFFFF0000u : 0u);
+    R.srowA = sm.cost4 + ((icA & 15) << 5);
+    R.srowB = sm.cost4 + ((icB & 15) << 5);
+    // the boundary cells' steps in the strip (aff_pair's sL, sR, sF)
+    const int d_lb = (-R.i > kDlo) ? -R.i : kDlo;
+    const int sL = d_lb - kDlo + 2 * k;
+    const int sRA = (PA.e0 <= PA.lenj - R.i) ? PA.e0 - kDlo + 2 * k : -1000000;
+    const int sRB = (PB.e0 <= PB.lenj - R.i) ? PB.e0 - kDlo + 2 * k : -1000000;
+    const int sFA = (actA && R.i == PA.leni) ? (PA.lenj - PA.leni) - kDlo + 2 * k : -1000000;
+    const int sFB = (actB && R.i == PB.leni) ? (PB.lenj - PB.leni) - kDlo + 2 * k : -1000000;
+
+    S.eh_l = kInfA2; S.cb_l = kInfA2;
+    S.eh_d = kInfA2; S.ev_d = kInfA2; S.eb_d = kInfA2; S.cb_d = kInfA2;
+    S.m_eh = kInfA2; S.m_ev = kInfA2; S.m_eb = kInfA2; S.m_cb = kInfA2;
+    S.wA = S.wB = 0;
+    if (k == 0 && strip > 0) {
+      // a pair past its last strip reads an infinite record
+      const uint4 v = bnd[0];
+      const uint32_t keep = (actA ? 0xFFFFu : 0u) | (actB ? 0xFFFF0000u : 0u);
+      S.eh_d = sel2(kInfA2, v.x, keep); S.ev_d = sel2(kInfA2, v.y, keep);
+      S.eb_d = sel2(kInfA2, v.z, keep); S.cb_d = sel2(kInfA2, v.w, keep);
+    }
+    for (int s0 = 0; s0 < Spad; s0 += 32) {
+      __syncwarp();
+      {
+        auto chrA = [&](int j) { return (actA && j >= 0 && j <= PA.lenj) ? (int)sjA[j] : 0; };
+        auto chrB = [&](int j) { return (actB && j >= 0 && j <= PB.lenj) ? (int)sjB[j] : 0; };
+        const int jb = r0 + kDlo + s0 - kAffRows;
+#pragma unroll
+        for (int e = k; e < 32; e += kAffRows) {
+          const int x = s0 + e + 1;
+          uint4 v = kInf4;
+          const bool inA = actA && strip > 0 && x < PA.wd, inB = actB && strip > 0 && x < PB.wd;
+          if (inA || inB) {
+            const uint4 b = bnd[x];
+            const uint32_t keep = (inA ? 0xFFFFu : 0u) | (inB ? 0xFFFF0000u : 0u);
+            v = make_uint4(sel2(kInfA2, b.x, keep), sel2(kInfA2, b.y, keep),
+                           sel2(kInfA2, b.z, keep), sel2(kInfA2, b.w, keep));
+          }
+          rin[e] = v;
+        }
+#pragma unroll
+        for (int x = k; x < 64; x += kAffRows)
+          win[x] = aff_column2(sm.tab, chrA(jb + x), chrA(jb + x - 1), chrB(jb + x),
+                               chrB(jb + x - 1), jb + x, go);
+      }
+      __syncwarp();
+      uint32_t *dmbA = (BT && actA) ? dmbaseA + ((int64_t)strip * PA.sblocks + (s0 >> 2)) * kAffRows + k
+                                    : nullptr;
+      uint32_t *dmbB = (BT && actB) ? dmbaseB + ((int64_t)strip * PB.sblocks + (s0 >> 2)) * kAffRows + k
+                                    : nullptr;
+#pragma unroll 1
+      for (int hh = 0; hh < 2; ++hh) {
+        const int hs = s0 + 16 * hh;
+        if (hs >= Spad) break;
+        R.specL = step_bit(sL, hs);
+        R.specRA = step_bit(sRA, hs);
+        R.specRB = step_bit(sRB, hs);
+        R.uFA = sFA - hs;
+        R.uFB = sFB - hs;
+        uint32_t *dmhA = (dmbA && hs < ShA) ? dmbA + 4 * kAffRows * hh : nullptr;
+        uint32_t *dmhB = (dmbB && hs < ShB) ? dmbB + 4 * kAffRows * hh : nullptr;
+        R.spec = R.specL | R.specRA | R.specRB;
+        const uint4 *cl = wl + 16 * hh, *ri = rin + 16 * hh;
+        uint4 *ro = rout + 16 * hh;
+        if (ends)
+          aff2_half<BT, true>(S, R, cl, ri, ro, hs, go4, go8, dmhA, dmhB, k);
+        else
+          aff2_half<BT, false>(S, R, cl, ri, ro, hs, go4, go8, dmhA, dmhB, k);
+      }
+      __syncwarp();
+      const int wdm = max(actA ? PA.wd : 0, actB ? PB.wd : 0);
+#pragma unroll
+      for (int e = k; e < 32; e += kAffRows) {
+        const int x = s0 + e - 2 * (kAffRows - 1);
+        if (x >= 0 && x < wdm) bnd[x] = rout[e];
+      }
+    }
+    __syncwarp();
+  }
+  const int rA = __shfl_sync(kFullA, S.resA, h * kAffRows + (PA.leni & (kAffRows - 1)));
+  const int rB = __shfl_sync(kFullA, S.resB, h * kAffRows + (PB.leni & (kAffRows - 1)));
+  if (k == 0) {
+    if (hasA) {
+      A.cost[idA] = rA >> 2;
+      if ((rA >> 2) >= kAffPackLim) atomicOr(A.err, 8);
+    }
+    if (hasB) {
+      A.cost[idB] = rB >> 2;
+      if ((rB >> 2) >= kAffPackLim) atomicOr(A.err, 8);
+    }
+  }
+}
+
+template <bool BT>
+__global__ void __launch_bounds__(kAffWarps * 32, 5) k_aff_dp2(AffDpArgs A) {
+  __shared__ AffSmem2 sm;
+  for (int t = threadIdx.x; t < 1024; t += blockDim.x) {
+    sm.tab[t] = A.tables->packed[t];
+    sm.cost4[t] = (uint16_t)(4u * (A.tables->packed[t] & 0xffffu));
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int h = lane / kAffRows;
+  uint4 *bnd = (uint4 *)A.scratch + (gw * kAffGroups + h) * A.slab;  // one slab per lane group
+  for (;;) {
+    int p = 0;
+    if (lane == 0) p = atomicAdd(A.counter, 2 * kAffGroups);  // consecutive pairs: similar sizes
+    p = __shfl_sync(kFullA, p, 0);
+    if (p >= A.n) break;
+    AffPlan P2[2];
+    bool has2[2];
+    int id2[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int ph = p + 2 * h + q;
+      has2[q] = ph < A.n;
+      id2[q] = has2[q] ? (A.order ? A.order[ph] : ph) : 0;
+      P2[q] = AffPlan{};
+      P2[q].leni = P2[q].lenj = -1;
+      if (has2[q]) {
+        const AffPlan Q = A.plans[id2[q]];
+        if (Q.empty) {
+          if ((lane & (kAffRows - 1)) == 0) A.cost[id2[q]] = 0;
+          has2[q] = false;
+        } else {
+          P2[q] = Q;
+        }
+      }
+    }
+    aff2_pairs<BT>(A, sm, warp, P2[0], P2[1], has2[0], has2[1],
+                   (BT && has2[0]) ? A.dm_off[id2[0]] : 0, (BT && has2[1]) ? A.dm_off[id2[1]] : 0,
+                   id2[0], id2[1], bnd, lane);
+  }
+}
+
 template <bool BT>
 __global__ void __launch_bounds__(kAffWarps * 32, 24 / kAffWarps) k_aff_dp(AffDpArgs A) {
   __shared__ AffSmem sm;
@@ -521,14 +885,16 @@ __global__ void __launch_bounds__(128) k_aff_traceback(AffTbArgs A) {
   A.out_len[2 * id + 1] = bad ? -1 : (int32_t)nm;
 }
 
-int aff_blocks(bool bt) {
-  static int cache[2][64] = {};
+int aff_blocks(bool bt, bool packed) {
+  static int cache[4][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  int &c = cache[bt ? 1 : 0][dev & 63];
+  int &c = cache[(bt ? 1 : 0) + (packed ? 2 : 0)][dev & 63];
   if (!c) {
     int per_sm = 0, sms = 0;
-    if (bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<true>, kAffWarps * 32, 0);
+    if (packed && bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp2<true>, kAffWarps * 32, 0);
+    else if (packed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp2<false>, kAffWarps * 32, 0);
+    else if (bt) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<true>, kAffWarps * 32, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aff_dp<false>, kAffWarps * 32, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
@@ -600,31 +966,48 @@ int affine_batch(const poyd_cm *cm, int maxc, int32_t n, const uint8_t *seq,
     dm = (uint32_t *)ws_buffer(w, WS_DM, sizeof(uint32_t) * (size_t)std::max<int64_t>(total, 1));
     if (!dm) return fail(POYD_ENOMEM, "affine direction matrix allocation failed");
   }
-  const int blocks = aff_blocks(want_align);
-  const int64_t slab = maxwd + 8;
-  int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH,
-                                    sizeof(int4) * (size_t)slab * (size_t)blocks * kAffWarps *
-                                        kAffGroups);
-  if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
-  AffDpArgs DA;
-  DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
-  DA.go = cm->gap_open; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
-  DA.cost = cost;
-  {
-    ProfScope ps(want_align ? "aff_dp_dm" : "aff_dp_cost", st);
-    if (want_align) k_aff_dp<true><<<blocks, kAffWarps * 32, 0, st>>>(DA);
-    else k_aff_dp<false><<<blocks, kAffWarps * 32, 0, st>>>(DA);
-  }
-  CKA(cudaGetLastError());
-  if (want_align) {
-    AffTbArgs TA;
-    TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
-    TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+  // The packed kernel runs when one step's largest add stays far below its
+  // 16-bit infinity (small cost tables; POYD_AFF_PACKED=0 keeps the 32-bit
+  // kernel); a pair whose final cost is past its exact range sends the
+  // whole batch to the 32-bit kernel afterwards.
+  bool packed = 4LL * (PA.maxc + 2LL * cm->gap_open + 1) < 0x3000;
+  if (const char *e = std::getenv("POYD_AFF_PACKED")) packed = packed && std::atoi(e) != 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const int blocks = aff_blocks(want_align, packed);
+    const int64_t slab = maxwd + 8;
+    int4 *scratch = (int4 *)ws_buffer(w, WS_SCRATCH,
+                                      sizeof(int4) * (size_t)slab * (size_t)blocks * kAffWarps *
+                                          kAffGroups);
+    if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
+    AffDpArgs DA;
+    DA.n = n; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord; DA.tables = tabs;
+    DA.go = cm->gap_open; DA.counter = counter; DA.scratch = scratch; DA.slab = slab; DA.dm = dm;
+    DA.cost = cost; DA.err = err;
+    if (attempt) CKA(cudaMemsetAsync(counter, 0, 4, st));
     {
-      ProfScope ps("aff_traceback", st);
-      k_aff_traceback<<<(n + 127) / 128, 128, 0, st>>>(TA);
+      ProfScope ps(want_align ? "aff_dp_dm" : "aff_dp_cost", st);
+      if (packed && want_align) k_aff_dp2<true><<<blocks, kAffWarps * 32, 0, st>>>(DA);
+      else if (packed) k_aff_dp2<false><<<blocks, kAffWarps * 32, 0, st>>>(DA);
+      else if (want_align) k_aff_dp<true><<<blocks, kAffWarps * 32, 0, st>>>(DA);
+      else k_aff_dp<false><<<blocks, kAffWarps * 32, 0, st>>>(DA);
     }
     CKA(cudaGetLastError());
+    if (want_align) {
+      AffTbArgs TA;
+      TA.n = n; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
+      TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
+      {
+        ProfScope ps("aff_traceback", st);
+        k_aff_traceback<<<(n + 127) / 128, 128, 0, st>>>(TA);
+      }
+      CKA(cudaGetLastError());
+    }
+    if (!packed) break;
+    int32_t e = 0;
+    CKA(cudaMemcpyAsync(&e, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CKA(cudaStreamSynchronize(st));
+    if (!(e & 8)) break;
+    packed = false;  // a cost past the packed range: the 32-bit kernel, again
   }
   return POYD_OK;
 }
