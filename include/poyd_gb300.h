@@ -500,6 +500,14 @@ int poyd_mlp_head_backward(const void *H, const void *w, const float *y, const f
 int poyd_adam_step(float *w, void *w16, const float *g, float *m, float *v, int64_t n, float lr,
                    float b1, float b2, float eps, int32_t step, void *stream);
 int poyd_to_bf16(const float *x, void *y, int64_t n, void *stream);
+/* The whole 32-256-256-128-1 forward for inference in one launch: y[m] for
+ * the M rows of X ([M][32] bf16, 16-byte aligned) with the weights
+ * transposed (W1t [256][32], W2t [256][256], W3t [128][256] bf16), biases
+ * fp32, the output layer w4 [128] bf16 and b4 [1]; the same values as the
+ * layer-by-layer poyd_gemm_bf16 + poyd_mlp_head_forward path, bit for bit. */
+int poyd_mlp_forward(const void *X, int32_t M, const void *W1t, const float *b1,
+                     const void *W2t, const float *b2, const void *W3t, const float *b3,
+                     const void *w4, const float *b4, float *y, void *stream);
 
 /* ---------------------------------------------------------------------
  * Measurement helpers (no counterpart in the reference, which has no

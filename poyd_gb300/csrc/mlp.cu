@@ -86,6 +86,117 @@ __global__ void __launch_bounds__(128) k_gemm(const __nv_bfloat16 *A, int lda, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused inference of the 32-256-256-128-1 MLP: a block takes 64 rows and
+// runs the three hidden layers and the head with the activations in shared
+// memory.  Each layer is the same arithmetic as k_gemm (mma.sync m16n8k16
+// over k chunks in ascending order, + bias, ReLU, bf16 rounding) and the
+// head that of k_head_forward (lane-strided sums, then the xor butterfly),
+// so the predictions equal the layer-by-layer path's bit for bit.  The
+// weights come in transposed (Wt[n][k]), so every B fragment is one 32-bit
+// load from L2; activation rows are padded by 8 elements so that the A
+// fragment loads hit 32 distinct banks.
+// ---------------------------------------------------------------------------
+constexpr int kFRows = 64;
+constexpr int kFPadX = 32 + 8, kFPadH = 256 + 8;
+constexpr int kFSmem = (kFRows * kFPadX + 2 * kFRows * kFPadH) * 2;
+
+template <int K, int N, int LDI, int LDO>
+__device__ __forceinline__ void fwd_layer(const __nv_bfloat16 *in,
+                                          const __nv_bfloat16 *__restrict__ Wt,
+                                          const float *__restrict__ bias, __nv_bfloat16 *out,
+                                          int warp, int lane) {
+  constexpr int NT = N / 64;  // n8 tiles of each of the 8 warps
+  const int g = lane >> 2, t = lane & 3;
+  const int nb = warp * (N / 8);
+  float acc[4][NT][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+#pragma unroll 2
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    uint32_t a[4][4];
+#pragma unroll
+    for (int mt = 0; mt < 4; ++mt) {
+      const __nv_bfloat16 *r0 = in + (mt * 16 + g) * LDI + k0 + 2 * t;
+      const __nv_bfloat16 *r1 = r0 + 8 * LDI;
+      a[mt][0] = *reinterpret_cast<const uint32_t *>(r0);
+      a[mt][1] = *reinterpret_cast<const uint32_t *>(r1);
+      a[mt][2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+      a[mt][3] = *reinterpret_cast<const uint32_t *>(r1 + 8);
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+      const __nv_bfloat16 *w = Wt + (int64_t)(nb + nt * 8 + g) * K + k0 + 2 * t;
+      const uint32_t b0 = *reinterpret_cast<const uint32_t *>(w);
+      const uint32_t b1 = *reinterpret_cast<const uint32_t *>(w + 8);
+#pragma unroll
+      for (int mt = 0; mt < 4; ++mt)
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+            "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+f"(acc[mt][nt][0]), "+f"(acc[mt][nt][1]), "+f"(acc[mt][nt][2]),
+              "+f"(acc[mt][nt][3])
+            : "r"(a[mt][0]), "r"(a[mt][1]), "r"(a[mt][2]), "r"(a[mt][3]), "r"(b0), "r"(b1));
+    }
+  }
+#pragma unroll
+  for (int mt = 0; mt < 4; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int m = mt * 16 + g + (q >= 2 ? 8 : 0);
+        const int n = nb + nt * 8 + 2 * t + (q & 1);
+        float v = acc[mt][nt][q] + bias[n];
+        v = v > 0.f ? v : 0.f;
+        out[m * LDO + n] = __float2bfloat16_rn(v);
+      }
+}
+
+__global__ void __launch_bounds__(256) k_mlp_forward(const __nv_bfloat16 *__restrict__ X, int M,
+                                                     const __nv_bfloat16 *__restrict__ W1t,
+                                                     const float *__restrict__ b1,
+                                                     const __nv_bfloat16 *__restrict__ W2t,
+                                                     const float *__restrict__ b2,
+                                                     const __nv_bfloat16 *__restrict__ W3t,
+                                                     const float *__restrict__ b3,
+                                                     const __nv_bfloat16 *__restrict__ w4,
+                                                     const float *__restrict__ b4, float *y) {
+  extern __shared__ __align__(16) unsigned char mlp_dsm[];
+  __nv_bfloat16 *xs = reinterpret_cast<__nv_bfloat16 *>(mlp_dsm);
+  __nv_bfloat16 *h1 = xs + kFRows * kFPadX;
+  __nv_bfloat16 *h2 = h1 + kFRows * kFPadH;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t m0 = (int64_t)blockIdx.x * kFRows;
+  // the block's 64 input rows (32 bf16 each), zero past M
+  for (int e = threadIdx.x; e < kFRows * 4; e += blockDim.x) {
+    const int r = e >> 2, c = (e & 3) * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (m0 + r < M) v = *reinterpret_cast<const uint4 *>(X + (m0 + r) * 32 + c);
+    *reinterpret_cast<uint4 *>(xs + r * kFPadX + c) = v;
+  }
+  __syncthreads();
+  fwd_layer<32, 256, kFPadX, kFPadH>(xs, W1t, b1, h1, warp, lane);
+  __syncthreads();
+  fwd_layer<256, 256, kFPadH, kFPadH>(h1, W2t, b2, h2, warp, lane);
+  __syncthreads();
+  fwd_layer<256, 128, kFPadH, kFPadH>(h2, W3t, b3, h1, warp, lane);
+  __syncthreads();
+  // the head, k_head_forward's order: 8 rows per warp
+  for (int rr = 0; rr < kFRows / 8; ++rr) {
+    const int r = warp * (kFRows / 8) + rr;
+    float sacc = 0.f;
+    for (int k = lane; k < 128; k += 32)
+      sacc += __bfloat162float(h1[r * kFPadH + k]) * __bfloat162float(w4[k]);
+    for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+    if (lane == 0 && m0 + r < M) y[m0 + r] = sacc + b4[0];
+  }
+}
+
 // dZ = dH * (H > 0), bf16 in / out
 __global__ void k_relu_grad(const __nv_bfloat16 *dH, const __nv_bfloat16 *H, __nv_bfloat16 *dZ,
                             int64_t n) {
@@ -258,6 +369,34 @@ extern "C" int poyd_to_bf16(const float *x, void *y, int64_t n, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("mlp_to_bf16", st);
   k_to_bf16<<<nblk(n, 256), 256, 0, st>>>(x, (__nv_bfloat16 *)y, n);
+  MLP_LAUNCH_CHECK();
+  return POYD_OK;
+}
+
+extern "C" int poyd_mlp_forward(const void *X, int32_t M, const void *W1t, const float *b1,
+                                const void *W2t, const float *b2, const void *W3t,
+                                const float *b3, const void *w4, const float *b4, float *y,
+                                void *stream) {
+  if (M < 0) return fail(POYD_EINVAL, "negative size");
+  if (M == 0) return POYD_OK;
+  if (!X || !W1t || !b1 || !W2t || !b2 || !W3t || !b3 || !w4 || !b4 || !y)
+    return fail(POYD_EINVAL, "poyd_mlp_forward: null argument");
+  if (((uintptr_t)X & 15) || ((uintptr_t)W1t & 3) || ((uintptr_t)W2t & 3) || ((uintptr_t)W3t & 3))
+    return fail(POYD_EINVAL, "poyd_mlp_forward: X must be 16-byte aligned, weights 4-byte aligned");
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr[dev & 63]) {
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kFSmem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_mlp_forward)");
+    attr[dev & 63] = true;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  ProfScope ps("mlp_forward", st);
+  k_mlp_forward<<<nblk(M, kFRows), 256, kFSmem, st>>>(
+      (const __nv_bfloat16 *)X, M, (const __nv_bfloat16 *)W1t, b1, (const __nv_bfloat16 *)W2t, b2,
+      (const __nv_bfloat16 *)W3t, b3, (const __nv_bfloat16 *)w4, b4, y);
   MLP_LAUNCH_CHECK();
   return POYD_OK;
 }

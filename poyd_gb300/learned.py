@@ -30,22 +30,29 @@ _POPC = torch.tensor([bin(i).count("1") for i in range(256)], dtype=torch.float3
 
 
 def node_info(t: search.Tree, be):
+    """Subtree sizes, depths, parents (a root is its own) and siblings of
+    every node (cached per tree state; do not modify the arrays)."""
+    return t._memo("node_info", lambda: _node_info(t))
+
+
+def _node_info(t: search.Tree):
     n_nodes = len(t.parent)
-    size = np.zeros(n_nodes, np.float32)
-    depth = np.zeros(n_nodes, np.float32)
+    parent, kids, n = t.parent.tolist(), t.kids.tolist(), t.n
+    size = [0.0] * n_nodes
+    depth = [0.0] * n_nodes
+    sib = list(range(n_nodes))
     order = t.nodes()
     for v in order:  # preorder: parents first
-        p = t.parent[v]
-        depth[v] = 0 if p < 0 else depth[p] + 1
-    for v in order[::-1]:
-        size[v] = 1 if v < t.n else size[t.kids[v][0]] + size[t.kids[v][1]]
-    par = np.where(t.parent >= 0, t.parent, np.arange(n_nodes))
-    sib = np.arange(n_nodes)
-    for v in order:
-        p = t.parent[v]
+        p = parent[v]
         if p >= 0:
-            sib[v] = t.kids[p][0] if t.kids[p][1] == v else t.kids[p][1]
-    return size, depth, par, sib
+            depth[v] = depth[p] + 1
+            a, b = kids[p]
+            sib[v] = a if b == v else b
+    for v in order[::-1]:
+        size[v] = 1.0 if v < n else size[kids[v][0]] + size[kids[v][1]]
+    par = np.where(t.parent >= 0, t.parent, np.arange(n_nodes))
+    return (np.array(size, np.float32), np.array(depth, np.float32), par,
+            np.array(sib, np.int64))
 
 
 def _as_idx(be, x):
@@ -168,8 +175,9 @@ def learned_scorer(prop: Proposal, be, frac: float = 0.03, min_k: int = 64, stat
     """scorer for search.spr_pass: exact scores for the best-predicted
     fraction of candidates, a large sentinel for the rest."""
 
-    def scorer(t, S, E):
-        cur = current_attachment(t, be, S)
+    def scorer(t, S, E, cur=None):
+        if cur is None:
+            cur = current_attachment(t, be, S)
         X = features(t, be, S, E, cur)
         pred = prop.predict(X)
         k = min(len(S), max(min_k, int(frac * len(S))))

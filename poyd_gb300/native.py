@@ -76,7 +76,7 @@ EXPORTED = (
     "poyd_int_pipe_rate", "poyd_last_error", "poyd_launch_count", "poyd_matrix_create",
     "poyd_matrix_free", "poyd_median_2_no_gaps_batch", "poyd_median_2_with_gaps_batch",
     "poyd_median_levels",
-    "poyd_mlp_head_backward", "poyd_mlp_head_forward", "poyd_nonadd16_distance_batch",
+    "poyd_mlp_forward", "poyd_mlp_head_backward", "poyd_mlp_head_forward", "poyd_nonadd16_distance_batch",
     "poyd_nonadd16_median_3_batch", "poyd_nonadd16_median_batch",
     "poyd_nonadd32_distance_batch", "poyd_nonadd32_median_3_batch",
     "poyd_nonadd32_median_batch", "poyd_nonadd8_distance_batch", "poyd_nonadd8_median_3_batch",

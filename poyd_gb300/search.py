@@ -677,10 +677,6 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
     S, E = spr_candidates(t)
     st.candidates = len(S)
     t1 = time.perf_counter()
-    if scorer is None:
-        score = be.distances(S, E)
-    else:
-        score = scorer(t, S, E)
     # the cost of each subtree where it is now: distance to its sibling
     subs = distinct_nodes(S, len(t.parent))
     cur = np.zeros(len(t.parent), np.int64)
@@ -688,6 +684,8 @@ def spr_pass(t: Tree, be, max_moves: int = 16, scorer=None, log=None, diag=None)
         p = t.parent[subs]
         sib = np.where(t.kids[p, 0] == subs, t.kids[p, 1], t.kids[p, 0])
         cur[subs] = be.distances(subs, sib)
+    # a scorer receives those attachment costs (indexed by node id) too
+    score = be.distances(S, E) if scorer is None else scorer(t, S, E, cur)
     st.seconds_scoring = time.perf_counter() - t1
     if log is not None:
         log.append((t.copy(), S, E, score))

@@ -49,3 +49,19 @@ def test_training_reduces_loss():
     p1 = net.predict(Xd)
     l1 = float(((p1 - yd) ** 2).mean().item())
     assert l1 < 0.25 * l0, (l0, l1)
+
+
+@pytest.mark.parametrize("rows", [1, 63, 64, 1000, 70001])
+def test_fused_inference_equals_layer_by_layer(rows):
+    """poyd_mlp_forward (one launch, activations in shared memory) gives
+    forward()'s predictions bit for bit, also for partial 64-row tiles, and
+    after training steps have moved the weights."""
+    net = mlp.MLP(seed=5)
+    g = torch.Generator(device="cpu").manual_seed(rows)
+    X = torch.randn((rows, 32), generator=g).cuda()
+    if rows >= 1000:
+        net.fit(X[:4096], torch.randn(min(rows, 4096), generator=g).cuda(), epochs=1, batch=512)
+    want = torch.cat([net.forward(X[s:s + 65536].to(torch.bfloat16).contiguous()).clone()
+                      for s in range(0, rows, 65536)])
+    got = net.predict(X)
+    assert torch.equal(want, got)
