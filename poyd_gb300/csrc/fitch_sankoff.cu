@@ -55,18 +55,15 @@ __global__ void k_fitch_distance(const uint8_t *nodes, int64_t stride, int len, 
   if (lane == 0) dist[c] = cnt;
 }
 
-// Output row c of `out`, or row oi[c] when an output index is given (the
-// level engine writes the output nodes' own rows of the node array; a
-// level's outputs are never its inputs).
 __global__ void k_fitch_median(const uint8_t *nodes, int64_t stride, int len, int n,
                                const int32_t *ai, const int32_t *bi, uint8_t *out,
-                               int64_t *added, const int32_t *oi) {
+                               int64_t *added) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= n) return;
   const uint4 *a = (const uint4 *)(nodes + (int64_t)ai[c] * stride);
   const uint4 *b = (const uint4 *)(nodes + (int64_t)bi[c] * stride);
-  uint4 *r = (uint4 *)(out + (int64_t)(oi ? oi[c] : c) * stride);
+  uint4 *r = (uint4 *)(out + (int64_t)c * stride);
   const int nv = (len + 15) >> 4;
   unsigned cnt = 0;
   for (int v = lane; v < nv; v += 32) {
@@ -169,7 +166,7 @@ __device__ __forceinline__ void sank_char(const int *tcm, const int *as, const i
 template <int K>
 __global__ void k_sank_median(const int32_t *nodes, int nchar, const int32_t *tcm_g, int n,
                               const int32_t *ai, const int32_t *bi, int32_t *out_s,
-                              int32_t *out_e, int32_t *out_b, const int32_t *oi) {
+                              int32_t *out_e, int32_t *out_b) {
   __shared__ int tcm[K * K];
   for (int t = threadIdx.x; t < K * K; t += blockDim.x) tcm[t] = tcm_g[t];
   __syncthreads();
@@ -182,7 +179,7 @@ __global__ void k_sank_median(const int32_t *nodes, int nchar, const int32_t *tc
 #pragma unroll
   for (int i = 0; i < K; ++i) { as[i] = a[i]; bs[i] = b[i]; }
   sank_char<K>(tcm, as, bs, cc, e, beta, minc, mina, minb);
-  const int64_t o = ((int64_t)(oi ? oi[c] : c) * nchar + ch) * K;
+  const int64_t o = ((int64_t)c * nchar + ch) * K;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
     out_s[o + i] = cc[i];
@@ -355,7 +352,7 @@ extern "C" int poyd_nonadd8_median_batch(const uint8_t *nodes, int64_t stride, i
   cudaStream_t st = (cudaStream_t)stream;
   ProfScope ps("fitch_median", st);
   k_fitch_median<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
-      nodes, stride, len, n, a_idx, b_idx, out, added_cost, nullptr);
+      nodes, stride, len, n, a_idx, b_idx, out, added_cost);
   FS_CK(cudaGetLastError());
   return POYD_OK;
 }
@@ -392,7 +389,7 @@ extern "C" int poyd_sank_median_batch(const int32_t *nodes, int32_t nchar, int32
   const int64_t total = (int64_t)n * nchar;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   ProfScope ps("sank_median", st);
-#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, out_s, out_e, out_beta, nullptr)
+#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, out_s, out_e, out_beta)
   switch (k) {
     SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
     SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)
@@ -450,30 +447,83 @@ extern "C" int poyd_sank_median_3_batch(const int32_t *nodes, const int32_t *fin
   return POYD_OK;
 }
 
-// Medians written into the node arrays' own rows out_idx[c] (the level
-// engine, csrc/levels.cu); same kernels and arguments as the entry points
-// above, checked by the caller.
-int poyd::launch_fitch_median_rows(uint8_t *nodes, int64_t stride, int32_t len, int32_t n,
-                                   const int32_t *a_idx, const int32_t *b_idx,
-                                   const int32_t *out_idx, int64_t *added, cudaStream_t st) {
-  if (n == 0) return POYD_OK;
-  ProfScope ps("fitch_median", st);
-  k_fitch_median<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
-      nodes, stride, len, n, a_idx, b_idx, nodes, added, out_idx);
-  FS_CK(cudaGetLastError());
-  return POYD_OK;
+namespace poyd {
+namespace {
+
+// One block per pair of a level (see LevelPost): the Fitch median
+// (k_fitch_median's arithmetic, its count summed over the block), the
+// Sankoff medians (k_sank_median's), and by thread 0 the DO median's place:
+// the fourth sequence of the pair's result slot.
+template <int K>
+__global__ void __launch_bounds__(128) k_level_post(LevelPost P) {
+  __shared__ int tcm[64];
+  __shared__ unsigned wsum[4];
+  const int i = blockIdx.x;
+  if (K > 0)
+    for (int t = threadIdx.x; t < K * K; t += blockDim.x) tcm[t] = P.tcm[t];
+  const int ia = P.a[i], ib = P.b[i], io = P.out[i];
+  unsigned cnt = 0;
+  if (P.fitch_len > 0) {
+    const uint4 *fa = (const uint4 *)(P.fitch + (int64_t)ia * P.stride);
+    const uint4 *fb = (const uint4 *)(P.fitch + (int64_t)ib * P.stride);
+    uint4 *r = (uint4 *)(P.fitch + (int64_t)io * P.stride);
+    const int nv = (P.fitch_len + 15) >> 4;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+      const uint4 x = fa[v], y = fb[v];
+      const int valid = P.fitch_len - v * 16;
+      uint4 o;
+      uint32_t in, z;
+      in = x.x & y.x; z = zbytes(in); o.x = in | (z & (x.x | y.x)); cnt += __popc(z & ~tailmask(valid, 0)) >> 3;
+      in = x.y & y.y; z = zbytes(in); o.y = in | (z & (x.y | y.y)); cnt += __popc(z & ~tailmask(valid, 1)) >> 3;
+      in = x.z & y.z; z = zbytes(in); o.z = in | (z & (x.z | y.z)); cnt += __popc(z & ~tailmask(valid, 2)) >> 3;
+      in = x.w & y.w; z = zbytes(in); o.w = in | (z & (x.w | y.w)); cnt += __popc(z & ~tailmask(valid, 3)) >> 3;
+      r[v] = o;
+    }
+  }
+  __syncthreads();  // tcm
+  if (K > 0) {
+    for (int ch = threadIdx.x; ch < P.nchar; ch += blockDim.x) {
+      const int32_t *sa = P.sank + ((int64_t)ia * P.nchar + ch) * K;
+      const int32_t *sb = P.sank + ((int64_t)ib * P.nchar + ch) * K;
+      int as[K > 0 ? K : 1], bs[K > 0 ? K : 1], cc[K > 0 ? K : 1], e[K > 0 ? K : 1],
+          beta[K > 0 ? K : 1], minc, mina, minb;
+#pragma unroll
+      for (int q = 0; q < K; ++q) { as[q] = sa[q]; bs[q] = sb[q]; }
+      sank_char<K>(tcm, as, bs, cc, e, beta, minc, mina, minb);
+      int32_t *so = P.sank + ((int64_t)io * P.nchar + ch) * K;
+#pragma unroll
+      for (int q = 0; q < K; ++q) so[q] = cc[q];
+    }
+  }
+  cnt = __reduce_add_sync(kFullF, cnt);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned fc = wsum[0] + wsum[1] + wsum[2] + wsum[3];
+    const int nm = P.out_len[2 * i + 1];
+    if (nm < 0) {
+      atomicOr(P.err, 1);
+      P.node_off[io] = P.slot_off[i];
+      P.node_len[io] = 0;
+    } else {
+      P.node_off[io] = P.slot_off[i] + 4 * slot_cap(P.a_len[i], P.b_len[i]) - nm;
+      P.node_len[io] = nm;
+    }
+    P.costs[2 * i] = P.cost[i];
+    P.costs[2 * i + 1] = P.fitch_len > 0 ? (int64_t)fc : 0;
+  }
 }
 
-int poyd::launch_sank_median_rows(int32_t *nodes, int32_t nchar, int32_t k, const int32_t *tcm,
-                                  int32_t n, const int32_t *a_idx, const int32_t *b_idx,
-                                  const int32_t *out_idx, cudaStream_t st) {
-  if (n == 0 || nchar == 0) return POYD_OK;
-  if (k < 2 || k > 8) return fail(POYD_EUNSUP, "Sankoff characters need 2..8 states");
-  const int64_t total = (int64_t)n * nchar;
-  const unsigned blocks = (unsigned)((total + 255) / 256);
-  ProfScope ps("sank_median", st);
-#define L(KV) k_sank_median<KV><<<blocks, 256, 0, st>>>(nodes, nchar, tcm, n, a_idx, b_idx, nodes, nullptr, nullptr, out_idx)
+}  // namespace
+
+int launch_level_post(const LevelPost &P, cudaStream_t st) {
+  if (P.n == 0) return POYD_OK;
+  const int k = P.nchar > 0 ? P.k : 0;
+  if (k != 0 && (k < 2 || k > 8)) return fail(POYD_EUNSUP, "Sankoff characters need 2..8 states");
+  ProfScope ps("level_post", st);
+#define L(KV) k_level_post<KV><<<(unsigned)P.n, 128, 0, st>>>(P)
   switch (k) {
+    case 0: L(0); break;
     SANK_DISPATCH(2, L) SANK_DISPATCH(3, L) SANK_DISPATCH(4, L) SANK_DISPATCH(5, L)
     SANK_DISPATCH(6, L) SANK_DISPATCH(7, L) SANK_DISPATCH(8, L)
   }
@@ -481,3 +531,5 @@ int poyd::launch_sank_median_rows(int32_t *nodes, int32_t nchar, int32_t k, cons
   FS_CK(cudaGetLastError());
   return POYD_OK;
 }
+
+}  // namespace poyd

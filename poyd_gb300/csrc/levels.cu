@@ -11,9 +11,9 @@
 //      places of the inputs) and lays the result slots out in the pool;
 //   2. the batched align_2 (plan, order, DP with fused traceback) writes
 //      every pair's four result sequences into its slot;
-//   3. the Fitch and Sankoff medians write the output nodes' own rows;
-//   4. k_lvl_place points every output node at its median (the fourth
-//      sequence of its slot) and records the costs.
+//   3. one launch (launch_level_post) writes the Fitch and Sankoff medians
+//      into the output nodes' own rows and points every output node at its
+//      median (the fourth sequence of its slot), recording the costs.
 // The host waits once per level (the align_2 plan read-back) and once at the
 // end, when the output nodes' places and the costs come back.
 #include <cuda_runtime.h>
@@ -82,29 +82,6 @@ __global__ void __launch_bounds__(kLvlThreads) k_lvl_gather(
     __syncthreads();
   }
   if (threadIdx.x == 0) *top = (base + 127) & ~(int64_t)127;
-}
-
-// Output node out[i] takes the median at the end of its slot; the costs of
-// pair i go to costs[2i] (DO) and costs[2i + 1] (Fitch).  A failed
-// traceback (negative length) sets *err and leaves the node empty.
-__global__ void k_lvl_place(int n, const int32_t *out, const int64_t *slot_off,
-                            const int32_t *a_len, const int32_t *b_len, const int32_t *out_len,
-                            const int32_t *cost, const int64_t *fitch_cost, int64_t *node_off,
-                            int32_t *node_len, int64_t *costs, int32_t *err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int nm = out_len[2 * i + 1];
-  const int v = out[i];
-  if (nm < 0) {
-    atomicOr(err, 1);
-    node_off[v] = slot_off[i];
-    node_len[v] = 0;
-  } else {
-    node_off[v] = slot_off[i] + 4 * slot_cap(a_len[i], b_len[i]) - nm;
-    node_len[v] = nm;
-  }
-  costs[2 * i] = cost[i];
-  costs[2 * i + 1] = fitch_cost ? fitch_cost[i] : 0;
 }
 
 // The output nodes' places, pair order: res[2i] = offset, res[2i+1] = length.
@@ -202,7 +179,7 @@ extern "C" int poyd_median_levels(const poyd_cm *cm, const poyd_node_store *stor
   // device node table (int64 offsets then int32 lengths) and the top
   unsigned char *nd = (unsigned char *)ws_buffer(w, WS_LVL_NODES,
                                                  (size_t)n_nodes * 12 + 2048);
-  const size_t per_pair = 3 * 4 + 2 * 8 + 2 * 4 + 8 + 2 * 4 + 4 + 8 + 2 * 8 + 2 * 8;
+  const size_t per_pair = 3 * 4 + 2 * 8 + 2 * 4 + 8 + 2 * 4 + 4 + 2 * 8 + 2 * 8;
   unsigned char *pp = (unsigned char *)ws_buffer(w, WS_LVL_PAIRS, (size_t)np * per_pair + 16 * 256);
   if (!nd || !pp) return fail(POYD_ENOMEM, "level engine workspace allocation failed");
   unsigned char *q = nd;
@@ -219,7 +196,6 @@ extern "C" int poyd_median_levels(const poyd_cm *cm, const poyd_node_store *stor
   int64_t *slot_off = carve<int64_t>(q, (size_t)np);
   int32_t *out_len = carve<int32_t>(q, 2 * (size_t)np);
   int32_t *cost = carve<int32_t>(q, (size_t)np);
-  int64_t *fcost = carve<int64_t>(q, (size_t)np);
   int64_t *d_costs = carve<int64_t>(q, 2 * (size_t)np);
   int64_t *d_res = carve<int64_t>(q, 2 * (size_t)np);
   const int32_t *da = d_ids, *db = d_ids + np, *dout = d_ids + 2 * np;
@@ -242,20 +218,16 @@ extern "C" int poyd_median_levels(const poyd_cm *cm, const poyd_node_store *stor
                                 cost + s, store->pool, slot_off + s, out_len + 2 * s, nullptr,
                                 POYD_FLAG_DOS_EMPTY, st);
     if (rc) return rc;
-    if (store->fitch_len > 0) {
-      rc = launch_fitch_median_rows(store->fitch, store->fitch_stride, store->fitch_len, n, da + s,
-                                    db + s, dout + s, fcost + s, st);
-      if (rc) return rc;
-    }
-    if (store->sank_nchar > 0) {
-      rc = launch_sank_median_rows(store->sank, store->sank_nchar, store->sank_k, store->sank_tcm,
-                                   n, da + s, db + s, dout + s, st);
-      if (rc) return rc;
-    }
-    k_lvl_place<<<(n + 127) / 128, 128, 0, st>>>(n, dout + s, slot_off + s, a_len + s, b_len + s,
-                                                  out_len + 2 * s, cost + s,
-                                                  store->fitch_len > 0 ? fcost + s : nullptr,
-                                                  d_off, d_len, d_costs + 2 * s, d_err);
+    LevelPost LP;
+    LP.n = n; LP.a = da + s; LP.b = db + s; LP.out = dout + s;
+    LP.fitch = store->fitch; LP.stride = store->fitch_stride; LP.fitch_len = store->fitch_len;
+    LP.sank = store->sank; LP.nchar = store->sank_nchar; LP.k = store->sank_k;
+    LP.tcm = store->sank_tcm;
+    LP.slot_off = slot_off + s; LP.a_len = a_len + s; LP.b_len = b_len + s;
+    LP.out_len = out_len + 2 * s; LP.cost = cost + s;
+    LP.node_off = d_off; LP.node_len = d_len; LP.costs = d_costs + 2 * s; LP.err = d_err;
+    rc = launch_level_post(LP, st);
+    if (rc) return rc;
     LV_CK(cudaGetLastError());
   }
   k_lvl_collect<<<(np + 127) / 128, 128, 0, st>>>(np, dout, d_off, d_len, d_res);

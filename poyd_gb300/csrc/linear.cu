@@ -798,6 +798,56 @@ __global__ void __launch_bounds__(128, 16) k_order_scatter(int n, const LinPlan 
   order[os->base[b] + atomicAdd(&os->hist[b], 1)] = id;
 }
 
+// Small batches (at most 1,024 pairs; every pair has its own warp, so the
+// longest-first order buys nothing): one block lays the direction matrices
+// out in id order, finds the widest band and zeroes the DP's counters, in
+// place of the bucketed order's three launches and two memsets.
+__global__ void __launch_bounds__(1024) k_order_small(int n, const LinPlan *plans,
+                                                      const int64_t *dm_words, int64_t *dm_off,
+                                                      LinOrderScratch *os, int *counter,
+                                                      int *batch_done, int nbatch) {
+  __shared__ unsigned long long part[32];
+  __shared__ int wmax[32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned long long w = t < n ? (unsigned long long)dm_words[t] : 0ull;
+  int wd = t < n ? plans[t].wd : 0;
+  unsigned long long incl = w;
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += x;
+  }
+  for (int d = 16; d > 0; d >>= 1) wd = max(wd, __shfl_xor_sync(0xffffffffu, wd, d));
+  if (lane == 31) part[warp] = incl;
+  if (lane == 0) wmax[warp] = wd;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long p = part[lane];
+    int m = wmax[lane];
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long x = __shfl_up_sync(0xffffffffu, p, d);
+      if (lane >= d) p += x;
+    }
+    for (int d = 16; d > 0; d >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, d));
+    part[lane] = p;  // inclusive over warps
+    if (lane == 0) wmax[0] = m;
+  }
+  __syncthreads();
+  if (t < n) dm_off[t] = (int64_t)((warp ? part[warp - 1] : 0ull) + incl - w);
+  if (t == 0) {
+    os->total = part[31];
+    os->maxwd = wmax[0];
+    *counter = 0;
+  }
+  if (batch_done)
+    for (int i = t; i < nbatch; i += blockDim.x) batch_done[i] = 0;
+}
+
+void launch_lin_order_small(int n, const LinPlan *plans, const int64_t *dm_words,
+                            int64_t *dm_off, LinOrderScratch *os, int *counter, int *batch_done,
+                            int nbatch, cudaStream_t st) {
+  k_order_small<<<1, 1024, 0, st>>>(n, plans, dm_words, dm_off, os, counter, batch_done, nbatch);
+}
+
 void launch_lin_order(int n, const LinPlan *plans, const int64_t *dm_words, int64_t *dm_off,
                       LinOrderScratch *os, int32_t *order, cudaStream_t st) {
   const int threads = 128;

@@ -90,6 +90,10 @@ struct LinOrderScratch {
 };
 void launch_lin_order(int n, const LinPlan *plans, const int64_t *dm_words, int64_t *dm_off,
                       LinOrderScratch *os, int32_t *order, cudaStream_t st);
+constexpr int kOrderSmall = 1024;  // batches up to this size use k_order_small
+void launch_lin_order_small(int n, const LinPlan *plans, const int64_t *dm_words,
+                            int64_t *dm_off, LinOrderScratch *os, int *counter, int *batch_done,
+                            int nbatch, cudaStream_t st);
 
 void launch_lin_plan(const LinPlanArgs &A, cudaStream_t st);
 int lin_dp_blocks(int mode);

@@ -105,13 +105,26 @@ struct ProfScope {
   ~ProfScope() { prof_end(tok, st); }
 };
 
-// Fitch / Sankoff medians of node pairs written into the node arrays' own
-// rows out_idx[c] (fitch_sankoff.cu), for the level engine.
-int launch_fitch_median_rows(uint8_t *nodes, int64_t stride, int32_t len, int32_t n,
-                             const int32_t *a_idx, const int32_t *b_idx, const int32_t *out_idx,
-                             int64_t *added, cudaStream_t st);
-int launch_sank_median_rows(int32_t *nodes, int32_t nchar, int32_t k, const int32_t *tcm,
-                            int32_t n, const int32_t *a_idx, const int32_t *b_idx,
-                            const int32_t *out_idx, cudaStream_t st);
+// The rest of one level of the level engine after its DO alignments
+// (fitch_sankoff.cu), in one launch: per pair, the Fitch and Sankoff medians
+// of the input nodes' rows into the output node's rows and the placement of
+// the DO median (the output node's place in the pool, the pair's costs).
+struct LevelPost {
+  int n;
+  const int32_t *a, *b, *out;     // node ids of the level's pairs
+  uint8_t *fitch;                 // Fitch rows (fitch_len 0: none)
+  int64_t stride;
+  int fitch_len;
+  int32_t *sank;                  // Sankoff rows (nchar 0: none)
+  int nchar, k;
+  const int32_t *tcm;
+  const int64_t *slot_off;        // the align_2 result slots
+  const int32_t *a_len, *b_len, *out_len, *cost;
+  int64_t *node_off;              // the device node table
+  int32_t *node_len;
+  int64_t *costs;                 // per pair: DO cost, Fitch cost
+  int32_t *err;                   // bit 0: a failed traceback
+};
+int launch_level_post(const LevelPost &P, cudaStream_t st);
 
 }  // namespace poyd

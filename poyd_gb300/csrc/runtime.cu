@@ -230,7 +230,23 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   // offsets on the device; one small read-back brings the plan's error bits,
   // the widest band and the direction-matrix size.
   int64_t *doff = dmw + n;
-  { ProfScope ps("lin_order", st); launch_lin_order(n, plans, dmw, doff, os, dord, st); }
+  // Batched align_2 with backtrack moves: the traceback runs inside the DP
+  // kernel, batch by batch as their fills complete.
+  const bool fuse = want_align && out && mode == kDpChoice;
+  const int nbatch = (int)(((int64_t)n + kLanes - 1) / kLanes);
+  int *batch_done = nullptr;
+  if (fuse) {
+    batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * (size_t)nbatch);
+    if (!batch_done) return fail(POYD_ENOMEM, "batch counter allocation failed");
+  }
+  // small batches take pairs in id order (the kernel also zeroes the DP's
+  // counters); the others the bucketed longest-first order
+  const bool small = n <= kOrderSmall && !ls;
+  {
+    ProfScope ps("lin_order", st);
+    if (small) launch_lin_order_small(n, plans, dmw, doff, os, counter, batch_done, nbatch, st);
+    else launch_lin_order(n, plans, dmw, doff, os, dord, st);
+  }
   CK(cudaGetLastError());
   struct {
     unsigned long long total;
@@ -340,14 +356,6 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
   const int64_t slab = maxwd + 64;
   int *scratch = (int *)ws_buffer(w, WS_SCRATCH, sizeof(int) * (size_t)slab * (size_t)blocks * warps);
   if (!scratch) return fail(POYD_ENOMEM, "scratch allocation failed");
-  // Batched align_2 with backtrack moves: the traceback runs inside the DP
-  // kernel, batch by batch as their fills complete.
-  const bool fuse = want_align && out && mode == kDpChoice;
-  int *batch_done = nullptr;
-  if (fuse) {
-    batch_done = (int *)ws_buffer(w, WS_BATCH, sizeof(int) * (((size_t)n + kLanes - 1) / kLanes));
-    if (!batch_done) return fail(POYD_ENOMEM, "batch counter allocation failed");
-  }
   std::vector<int64_t> off(host_waves ? (size_t)n : 0, 0);
   for (size_t v = 0; v + 1 < wave_at.size(); ++v) {
     const int32_t p0 = wave_at[v], p1 = wave_at[v + 1], m = p1 - p0;
@@ -359,14 +367,17 @@ static int linear_batch(Workspace *w, const poyd_cm *cm, int maxc, int32_t n, co
       }
       CK(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, st));
     }
-    CK(cudaMemsetAsync(counter, 0, 4, st));
-    if (fuse) CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * (((size_t)m + kLanes - 1) / kLanes), st));
+    const bool id_order = small && !host_waves;  // k_order_small zeroed the counters
+    if (!id_order) {
+      CK(cudaMemsetAsync(counter, 0, 4, st));
+      if (fuse) CK(cudaMemsetAsync(batch_done, 0, sizeof(int) * (((size_t)m + kLanes - 1) / kLanes), st));
+    }
     LinTbArgs TA;
     TA.n = m; TA.seq = seq; TA.plans = plans; TA.dm_off = doff; TA.dm = dm; TA.tables = tabs;
     TA.gap = cm->gap; TA.out = out; TA.out_off = out_off; TA.out_len = out_len;
-    TA.swaped = -1; TA.mode = mode; TA.order = dord + p0;
+    TA.swaped = -1; TA.mode = mode; TA.order = id_order ? nullptr : dord + p0;
     LinDpArgs DA;
-    DA.n = m; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = dord + p0;
+    DA.n = m; DA.seq = seq; DA.plans = plans; DA.dm_off = doff; DA.order = id_order ? nullptr : dord + p0;
     DA.tables = tabs; DA.gap = cm->gap; DA.counter = counter; DA.scratch = scratch;
     DA.slab = slab; DA.dm = dm; DA.cost = cost; DA.swaped = -1;
     DA.fuse_tb = fuse ? 1 : 0; DA.batch_done = batch_done; DA.tb = TA; DA.k = dp_constants();
