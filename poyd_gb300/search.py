@@ -1034,32 +1034,36 @@ def evaluate_trials(t: Tree, be, diag: Diagnosis, trials, detail=None) -> np.nda
             gp = lambda v, T=T: int(T.parent[v])
             gk = lambda v, T=T: T.kids[v].tolist()
             root_m = int(T.root)
-        dirty = set()
+        # the dirty nodes with their depths in the trial tree: each walk up
+        # from a start ends at the root or at a node already seen, whose
+        # depth fixes the depths along the walk
+        depth = {}
         for v in starts:
-            while v >= 0 and v not in dirty:
-                dirty.add(v)
+            chain = []
+            while v >= 0 and v not in depth:
+                chain.append(v)
                 v = gp(v)
-        h, tid = {}, {}
-
-        def height(v):
-            if v not in dirty:
-                return h_base[v]
-            if v not in h:
-                a, b = gk(v)
-                h[v] = 1 + max(height(a), height(b))
-            return h[v]
-
-        mc = {}   # min codes of the trial tree's dirty nodes
-        code = lambda c: mc[c] if c in dirty else mcb[c]
-        for v in sorted(dirty, key=height):
+            d = depth[v] if v >= 0 else -1
+            for x in reversed(chain):
+                d += 1
+                depth[x] = d
+        h, tid, mc = {}, {}, {}   # heights, scratch ids, min codes of dirty nodes
+        for v in sorted(depth, key=depth.__getitem__, reverse=True):  # children first
+            a, b = gk(v)
+            ha = h[a] if a in depth else h_base[a]
+            hb = h[b] if b in depth else h_base[b]
+            h[v] = 1 + (ha if ha > hb else hb)
+        for v in sorted(depth, key=h.__getitem__):
             tid[v] = tid_next
             tid_next += 1
             a, b = gk(v)
-            if code(a) > code(b):
-                a, b = b, a
-            mc[v] = code(a)
-            ref = lambda c: tid[c] if c in dirty else c
-            recs.setdefault(h[v], []).append((m, ref(a), ref(b), tid[v], v))
+            ca = mc[a] if a in depth else mcb[a]
+            cb = mc[b] if b in depth else mcb[b]
+            if ca > cb:
+                a, b, ca = b, a, cb
+            mc[v] = ca
+            recs.setdefault(h[v], []).append((m, tid[a] if a in depth else a,
+                                              tid[b] if b in depth else b, tid[v], v))
             old[m] += diag.do_cost[v] + diag.fitch_cost[v]
         roots.append(tid[root_m])
     be.ensure_nodes(tid_next)
