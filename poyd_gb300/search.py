@@ -624,24 +624,31 @@ class PassStats:
 
 
 def euler(t: Tree):
-    """Preorder entry / exit times: u is in subtree(v) iff tin[v] <= tin[u] < tout[v]."""
-    cap = len(t.parent)
-    tin = np.zeros(cap, np.int64)
-    tout = np.zeros(cap, np.int64)
+    """Preorder entry / exit times: u is in subtree(v) iff tin[v] <= tin[u] < tout[v]
+    (cached per tree state; do not modify the arrays)."""
+    return t._memo("euler", lambda: _euler(t))
+
+
+def _euler(t: Tree):
+    cap, n = len(t.parent), t.n
+    kids = t.kids.tolist()
+    tin = [0] * cap
+    tout = [0] * cap
     clock = 0
-    stack = [(t.root, 0)]
+    stack = [(int(t.root), 0)]
     while stack:
         v, state = stack.pop()
         if state == 0:
             tin[v] = clock
             clock += 1
             stack.append((v, 1))
-            if v >= t.n:
-                stack.append((int(t.kids[v][1]), 0))
-                stack.append((int(t.kids[v][0]), 0))
+            if v >= n:
+                a, b = kids[v]
+                stack.append((b, 0))
+                stack.append((a, 0))
         else:
             tout[v] = clock
-    return tin, tout
+    return np.array(tin, np.int64), np.array(tout, np.int64)
 
 
 def spr_candidates(t: Tree):
