@@ -459,9 +459,10 @@ struct AffState2 {
 
 // ENDS: the strip holds row 0 or a pair's last row.  Boundary cells (left
 // and right of the band) are handled under a per-step test of the lane's
-// bits: choosing between copies of the half block per half block (by a
-// warp vote) measured 40 % slower, and computing the masks on every step
-// 4 % slower.
+// bits.  Measured alternatives: computing the masks on every step, 4 %
+// slower; a second copy of the half block without them, chosen per half
+// block by a warp vote or by a per-strip mask, 35-50 % slower (both large
+// unrolled copies are then hot at once).
 template <bool BT, bool ENDS>
 __device__ __forceinline__ void aff2_half(AffState2 &S, const AffRow2 &R, const uint4 *clane,
                                           const uint4 *rin, uint4 *rout, int s0, uint32_t go4,
