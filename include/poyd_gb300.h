@@ -285,6 +285,60 @@ int poyd_algn_align_affine_3(const uint8_t *si, int32_t li, const uint8_t *sj,
                              int32_t *cost);
 
 /* ---------------------------------------------------------------------
+ * Three-sequence alignment of the Iterative (ThreeD) cost mode
+ * (sequence.ml:1075-1140, ukkCommon.c, ukk.checkp.c).  Sequences carry
+ * their leading gap; every other element must hold one of A, C, G, T
+ * (the lowest such bit is the character aligned, as powell_3D_align's
+ * copySequence does, ukkCommon.c:84-105).  The cost is Powell's optimum
+ * (alignmentCost, ukkCommon.c:345-391); among equally cheap alignments the
+ * GPU keeps, from the end, the lowest-numbered final state and at every
+ * column the lowest-numbered previous state (Powell's recursion can return
+ * another optimal one).  Each sequence is at most 4,096 elements; the
+ * choice cube needs 8 bytes per cell of la x lb x lc.
+ * ------------------------------------------------------------------- */
+/* powell_3D_align(sa, sb, sc, ra, rb, rc, mm, go, ge) (ukkCommon.c:111-143)
+ * with host buffers: the aligned rows, leading gap column first, are
+ * written right-aligned into ra/rb/rc of capacity cap (at least
+ * la + lb + lc - 2), their length to *len, the cost to *cost. */
+int poyd_powell_3D_align(const uint8_t *sa, int32_t la, const uint8_t *sb, int32_t lb,
+                         const uint8_t *sc, int32_t lc, uint8_t *ra, uint8_t *rb, uint8_t *rc,
+                         int32_t cap, int32_t *len, int32_t mm, int32_t go, int32_t ge,
+                         int32_t *cost);
+/* Cost_matrix.Three_D.median over a DNA combination matrix
+ * (Three_D.of_two_dim_comb, cost_matrix.ml:803-851) into a host table of
+ * 32,768 bytes indexed (i << 10) | (j << 5) | k. */
+int poyd_cm_median3(const poyd_cm *cm, uint8_t *tab);
+/* Batched align_3_powell (sequence.ml:1078-1087) with the median of
+ * align_3_powell_inter (sequence.ml:1103-1115) when median3 (a host table
+ * from poyd_cm_median3) is given.  Device arrays.  Triple i owns the slot
+ * out + out_off[i] of 4*cap_i bytes, cap_i = a_len + b_len + c_len rounded
+ * up to a multiple of 4, split in four right-aligned sequences: aligned a,
+ * aligned b, aligned c, median.  out_len[2i] = aligned length (with the
+ * leading gap column), out_len[2i+1] = median length (0 without median3).
+ * A triple with an element lacking A, C, G and T gets cost -1 and the call
+ * returns POYD_EINVAL after finishing the others. */
+int poyd_powell_3d_batch(int32_t n, const uint8_t *seq, const int64_t *a_off,
+                         const int32_t *a_len, const int64_t *b_off, const int32_t *b_len,
+                         const int64_t *c_off, const int32_t *c_len, int32_t mm, int32_t go,
+                         int32_t ge, const uint8_t *median3, int32_t *cost, uint8_t *out,
+                         const int64_t *out_off, int32_t *out_len, void *stream);
+/* Batched Sequence.Align.readjust_3d s1 s2 m cm cm3 p with first_gap true
+ * (sequence.ml:1117-1140): the early returns (equal lengths keep m; an
+ * empty child or parent gives the other sequence), otherwise the median of
+ * align_3_powell_inter (s1, s2, p) with mm = cost 1 2, go = the affine
+ * opening (0 for the linear model), ge = cost 1 16 and cm3 =
+ * Three_D.of_two_dim cm.  Slots as poyd_powell_3d_batch with c = p; the
+ * new median is the fourth sequence (out_len[2i] = 0 for an early return);
+ * cost[i] is the returned cost and changed[i] = (new median <> m). */
+int poyd_readjust_3d_batch(const poyd_cm *cm, int32_t n, const uint8_t *seq,
+                           const int64_t *s1_off, const int32_t *s1_len,
+                           const int64_t *s2_off, const int32_t *s2_len,
+                           const int64_t *m_off, const int32_t *m_len,
+                           const int64_t *p_off, const int32_t *p_len, int32_t *cost,
+                           uint8_t *out, const int64_t *out_off, int32_t *out_len,
+                           int32_t *changed, void *stream);
+
+/* ---------------------------------------------------------------------
  * Fitch non-additive characters, 8-bit state masks (NonaddCS8).
  * Batched over candidate pairs: row k of the result uses node rows
  * a_idx[k] and b_idx[k] of `nodes` (device, n_nodes x len bytes, row

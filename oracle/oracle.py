@@ -136,6 +136,13 @@ def lib():
         L.or_sank_elt_median_3.argtypes = [C.c_int, i64p, i64p, i64p, C.c_uint32, i64p, i64p,
                                            i64p, i64p, C.POINTER(C.c_uint32)]
         L.or_sank_elt_distance.restype = C.c_double
+        L.or_powell_3d.argtypes = [u8p, C.c_int, u8p, C.c_int, u8p, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, u8p, u8p, u8p, C.POINTER(C.c_int)]
+        L.or_powell_alignment_cost.argtypes = [u8p, u8p, u8p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.or_median3_table.argtypes = [C.POINTER(OrCM), u8p]
+        L.or_readjust_3d.argtypes = [u8p, C.c_int, u8p, C.c_int, u8p, C.c_int, u8p, C.c_int,
+                                     C.POINTER(OrCM), u8p, u8p, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -172,6 +179,8 @@ def ref():
             getattr(R, "ref_nonadd%d_distance" % w).argtypes = [C.c_void_p] * 2 + [C.c_int]
             getattr(R, "ref_nonadd%d_distance" % w).restype = C.c_long
             getattr(R, "ref_nonadd%d_median_3" % w).argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p]
+        R.ref_powell_3d.argtypes = [u8p, C.c_int, u8p, C.c_int, u8p, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, u8p, u8p, u8p, C.POINTER(C.c_int)]
         _ref = R
     return _ref
 
@@ -310,6 +319,52 @@ def closest(parent, mine, m, dos_empty: bool = True):
     if n < 0:
         raise ValueError("closest: a column of `mine` has no states")
     return out[:n].copy()
+
+
+def powell_3d(a, b, c, mm, go, ge, reference=False):
+    """powell_3D_align (ukkCommon.c:111-143) on three sequences with their
+    leading gap: (cost, aligned a, aligned b, aligned c).  reference=True
+    runs the compiled reference instead of the restatement."""
+    a, b, c = _u8(a), _u8(b), _u8(c)
+    cap = len(a) + len(b) + len(c)
+    oa, ob, oc = (np.zeros(cap, np.uint8) for _ in range(3))
+    n = C.c_int()
+    f = ref().ref_powell_3d if reference else lib().or_powell_3d
+    cost = f(_ptr(a), len(a), _ptr(b), len(b), _ptr(c), len(c), mm, go, ge, _ptr(oa), _ptr(ob),
+             _ptr(oc), C.byref(n))
+    if cost < 0:
+        raise ValueError("powell_3d: an element holds none of A, C, G, T")
+    k = n.value
+    return cost, oa[:k].copy(), ob[:k].copy(), oc[:k].copy()
+
+
+def powell_alignment_cost(a, b, c, mm, go, ge):
+    """The least alignmentCost (ukkCommon.c:345-391) of aligned rows."""
+    a, b, c = _u8(a), _u8(b), _u8(c)
+    return lib().or_powell_alignment_cost(_ptr(a), _ptr(b), _ptr(c), len(a), mm, go, ge)
+
+
+def median3_table(m):
+    """Cost_matrix.Three_D.of_two_dim_comb medians, indexed (i<<10)|(j<<5)|k."""
+    t = np.zeros(32768, np.uint8)
+    lib().or_median3_table(C.byref(m), _ptr(t))
+    return t
+
+
+def readjust_3d(s1, s2, cur, p, m, tab3=None):
+    """Sequence.Align.readjust_3d s1 s2 cur cm cm3 p: (cost, new median,
+    changed)."""
+    s1, s2, cur, p = _u8(s1), _u8(s2), _u8(cur), _u8(p)
+    if tab3 is None:
+        tab3 = median3_table(m)
+    res = np.zeros(len(s1) + len(s2) + len(p) + len(cur) + 1, np.uint8)
+    lr, ch = C.c_int(), C.c_int()
+    cost = lib().or_readjust_3d(_ptr(s1), len(s1), _ptr(s2), len(s2), _ptr(cur), len(cur),
+                                _ptr(p), len(p), C.byref(m), _ptr(tab3), _ptr(res), C.byref(lr),
+                                C.byref(ch))
+    if cost < 0:
+        raise ValueError("readjust_3d: an element holds none of A, C, G, T")
+    return cost, res[:lr.value].copy(), bool(ch.value)
 
 
 def nonadd_median(a, b):

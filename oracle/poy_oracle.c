@@ -1149,3 +1149,270 @@ void or_candidate_scores(const uint8_t *seq, const int64_t *off, const int32_t *
         out[t] = s;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Three-sequence alignment of the Iterative (ThreeD) mode:                  */
+/* Sequence.Align.readjust_3d (sequence.ml:1117-1140) over                   */
+/* align_3_powell_inter (sequence.ml:1089-1115) and powell_3D_align          */
+/* (ukkCommon.c:111-143, ukk.checkp.c).                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Powell's column states (ukkCommon.c setup, lines 206-262): one of match
+ * (M), delete (D) or insert (I) per sequence, at least one M and at most
+ * one I; code x0 + 3 x1 + 9 x2 with M 0, D 1, I 2, numbered in increasing
+ * code order (16 states, MMM first).  A state without I advances its M
+ * sequences; a state with I advances only the I sequence. */
+typedef struct {
+    int n;
+    int code[OR_P3_STATES];
+    int adv[OR_P3_STATES];   /* bit i: sequence i consumes a character */
+    int gapm[OR_P3_STATES];  /* bit i: sequence i is in D or I */
+    int ins[OR_P3_STATES];
+    int ndel[OR_P3_STATES];
+    int trans[OR_P3_STATES][OR_P3_STATES]; /* opening cost from s to t */
+} p3_states;
+
+static void p3_setup(p3_states *S, int go) {
+    int code, s, t, i;
+    S->n = 0;
+    for (code = 0; code < 27; code++) {
+        int x[3] = {code % 3, (code / 3) % 3, (code / 9) % 3};
+        int nm = 0, ni = 0, nd = 0, adv = 0, gm = 0;
+        for (i = 0; i < 3; i++) {
+            nm += x[i] == 0; nd += x[i] == 1; ni += x[i] == 2;
+            if (x[i] != 0) gm |= 1 << i;
+        }
+        if (nm == 0 || ni > 1) continue;
+        for (i = 0; i < 3; i++)
+            if (ni ? x[i] == 2 : x[i] == 0) adv |= 1 << i;
+        S->code[S->n] = code; S->adv[S->n] = adv; S->gapm[S->n] = gm;
+        S->ins[S->n] = ni; S->ndel[S->n] = nd;
+        S->n++;
+    }
+    /* transition cost (ukkCommon.c:263-290): go for every sequence that
+     * is in D or I in the new state and was not in that same state */
+    for (s = 0; s < S->n; s++)
+        for (t = 0; t < S->n; t++) {
+            int c = 0;
+            for (i = 0; i < 3; i++) {
+                int xs = (S->code[s] / (i == 0 ? 1 : i == 1 ? 3 : 9)) % 3;
+                int xt = (S->code[t] / (i == 0 ? 1 : i == 1 ? 3 : 9)) % 3;
+                if (xt != 0 && xt != xs) c += go;
+            }
+            S->trans[s][t] = c;
+        }
+}
+
+/* Column cost of state t over the characters its M (or I) sequences
+ * consume (alignmentCost, ukkCommon.c:345-391): ge for an insert column;
+ * otherwise ge per D plus mm per mismatch among the matched characters
+ * (three matched: 0 all equal, 1 two equal, 2 all different). */
+static int p3_col(const p3_states *S, int t, int mm, int ge, const int *ch) {
+    int v[3], n = 0, i;
+    if (S->ins[t]) return ge;
+    for (i = 0; i < 3; i++) if (S->adv[t] >> i & 1) v[n++] = ch[i];
+    {
+        int c = ge * S->ndel[t];
+        if (n == 2) c += (v[0] != v[1]) ? mm : 0;
+        if (n == 3) {
+            if (v[0] == v[1] && v[1] == v[2]) ;
+            else if (v[0] == v[1] || v[0] == v[2] || v[1] == v[2]) c += mm;
+            else c += 2 * mm;
+        }
+        return c;
+    }
+}
+
+/* The character Powell's code aligns for a sequence element
+ * (copySequence, ukkCommon.c:84-105): the lowest of the A, C, G, T bits;
+ * -1 for an element with none (the reference fails). */
+static int p3_base(int x) {
+    if (x & 1) return 1;
+    if (x & 2) return 2;
+    if (x & 4) return 4;
+    if (x & 8) return 8;
+    return -1;
+}
+
+#define P3_INF (1 << 29)
+
+int or_powell_3d(const uint8_t *a, int la, const uint8_t *b, int lb, const uint8_t *c, int lc,
+                 int mm, int go, int ge, uint8_t *oa, uint8_t *ob, uint8_t *oc, int *olen) {
+    /* The optimum of Powell's cost model by plain dynamic programming over
+     * the (la x lb x lc) cube and the 16 states, instead of Powell's
+     * furthest-reaching recursion: cell (i, j, k) holds, per state, the
+     * least cost of aligning a[1..i], b[1..j], c[1..k] with that state in
+     * the last column; the start (0, 0, 0) is MMM at cost 0 (the state
+     * before the first column, ukkCommon.c:351 and ukk.checkp.c:99-107).
+     * The cost equals powell_3D_align's; among equally cheap alignments
+     * this one keeps, from the end, the lowest-numbered final state and at
+     * every column the lowest-numbered previous state. */
+    p3_states S;
+    int na = la - 1, nb = lb - 1, nc = lc - 1, i, j, k, t, s;
+    int64_t plane = (int64_t)lb * lc;
+    int *V0, *V1;
+    uint64_t *P;
+    int best = P3_INF, bt = 0, cost;
+    uint8_t *A = (uint8_t *)malloc((size_t)la + 1), *B = (uint8_t *)malloc((size_t)lb + 1),
+            *C = (uint8_t *)malloc((size_t)lc + 1);
+    if (la < 1 || lb < 1 || lc < 1) { free(A); free(B); free(C); return -1; }
+    for (i = 1; i < la; i++) if ((A[i] = (uint8_t)p3_base(a[i])) == 0xff) { free(A); free(B); free(C); return -1; }
+    for (i = 1; i < lb; i++) if ((B[i] = (uint8_t)p3_base(b[i])) == 0xff) { free(A); free(B); free(C); return -1; }
+    for (i = 1; i < lc; i++) if ((C[i] = (uint8_t)p3_base(c[i])) == 0xff) { free(A); free(B); free(C); return -1; }
+    p3_setup(&S, go);
+    V0 = (int *)malloc(sizeof(int) * (size_t)plane * OR_P3_STATES);
+    V1 = (int *)malloc(sizeof(int) * (size_t)plane * OR_P3_STATES);
+    P = (uint64_t *)calloc((size_t)plane * la, sizeof(uint64_t));
+    for (i = 0; i <= na; i++) {
+        int *cur = (i & 1) ? V1 : V0, *prv = (i & 1) ? V0 : V1;
+        for (j = 0; j <= nb; j++)
+            for (k = 0; k <= nc; k++) {
+                int *v = cur + ((int64_t)j * lc + k) * OR_P3_STATES;
+                uint64_t pw = 0;
+                for (t = 0; t < S.n; t++) {
+                    int di = S.adv[t] & 1, dj = S.adv[t] >> 1 & 1, dk = S.adv[t] >> 2 & 1;
+                    const int *u;
+                    int ch[3], col, bv = P3_INF, bs = 0;
+                    v[t] = P3_INF;
+                    if (i == 0 && j == 0 && k == 0) { if (t == 0) v[t] = 0; continue; }
+                    if (i < di || j < dj || k < dk) continue;
+                    u = (di ? prv : cur) + ((int64_t)(j - dj) * lc + (k - dk)) * OR_P3_STATES;
+                    ch[0] = A[i]; ch[1] = B[j]; ch[2] = C[k];
+                    col = p3_col(&S, t, mm, ge, ch);
+                    for (s = 0; s < S.n; s++) {
+                        if (u[s] >= P3_INF) continue;
+                        if (u[s] + S.trans[s][t] < bv) { bv = u[s] + S.trans[s][t]; bs = s; }
+                    }
+                    if (bv < P3_INF) { v[t] = bv + col; pw |= (uint64_t)bs << (4 * t); }
+                }
+                P[(int64_t)i * plane + (int64_t)j * lc + k] = pw;
+            }
+    }
+    {
+        const int *v = ((na & 1) ? V1 : V0) + ((int64_t)nb * lc + nc) * OR_P3_STATES;
+        for (t = 0; t < S.n; t++) if (v[t] < best) { best = v[t]; bt = t; }
+    }
+    cost = best;
+    /* traceback, writing the columns right-aligned then moving them left */
+    {
+        int cap = na + nb + nc + 1, n = 0;
+        i = na; j = nb; k = nc; t = bt;
+        while (i || j || k) {
+            int di = S.adv[t] & 1, dj = S.adv[t] >> 1 & 1, dk = S.adv[t] >> 2 & 1;
+            int s2 = (int)(P[(int64_t)i * plane + (int64_t)j * lc + k] >> (4 * t) & 15);
+            n++;
+            oa[cap - n] = di ? A[i] : 16;
+            ob[cap - n] = dj ? B[j] : 16;
+            oc[cap - n] = dk ? C[k] : 16;
+            i -= di; j -= dj; k -= dk; t = s2;
+        }
+        n++;
+        oa[cap - n] = ob[cap - n] = oc[cap - n] = 16;  /* the leading gap */
+        memmove(oa, oa + cap - n, (size_t)n);
+        memmove(ob, ob + cap - n, (size_t)n);
+        memmove(oc, oc + cap - n, (size_t)n);
+        *olen = n;
+    }
+    free(V0); free(V1); free(P); free(A); free(B); free(C);
+    return cost;
+}
+
+int or_powell_alignment_cost(const uint8_t *oa, const uint8_t *ob, const uint8_t *oc, int n,
+                             int mm, int go, int ge) {
+    /* alignmentCost (ukkCommon.c:345-391) of an alignment whose columns
+     * carry no states: each column takes the cheapest state that
+     * consumes exactly its non-gap rows, given the previous column's
+     * state (the all-gap leading column is skipped).  Exhaustive over
+     * state sequences by dynamic programming on the column index. */
+    p3_states S;
+    int cur[OR_P3_STATES], nxt[OR_P3_STATES], x, t, s, best = P3_INF;
+    p3_setup(&S, go);
+    for (t = 0; t < S.n; t++) cur[t] = t == 0 ? 0 : P3_INF;
+    for (x = 1; x < n; x++) {
+        int adv = (oa[x] != 16) | (ob[x] != 16) << 1 | (oc[x] != 16) << 2;
+        int ch[3] = {oa[x], ob[x], oc[x]};
+        for (t = 0; t < S.n; t++) {
+            nxt[t] = P3_INF;
+            if (S.adv[t] != adv) continue;
+            for (s = 0; s < S.n; s++)
+                if (cur[s] < P3_INF && cur[s] + S.trans[s][t] < nxt[t]) nxt[t] = cur[s] + S.trans[s][t];
+            if (nxt[t] < P3_INF) nxt[t] += p3_col(&S, t, mm, ge, ch);
+        }
+        memcpy(cur, nxt, sizeof(cur));
+    }
+    for (t = 0; t < S.n; t++) if (cur[t] < best) best = cur[t];
+    return best;
+}
+
+void or_median3_table(const or_cm *m, uint8_t *tab) {
+    /* Cost_matrix.Three_D.of_two_dim_comb (cost_matrix.ml:803-851): the
+     * median of (i, j, k) is the lowest single state l minimising
+     * cost[l][i] + cost[l][j] + cost[l][k]; the gap state takes part only
+     * for metric matrices or when at least two of i, j, k hold the gap.
+     * The reference seeds each entry with OCaml's max_int, which fits a C
+     * int on a 32-bit OCaml; on a 64-bit one it becomes -1 and the table
+     * keeps no median at all.  This follows the 32-bit reading.  Indexed
+     * (i << 10) | (j << 5) | k. */
+    int i, j, k, l;
+    memset(tab, 0, 32768);
+    for (i = 1; i < 32; i++)
+        for (j = 1; j < 32; j++)
+            for (k = 1; k < 32; k++) {
+                int64_t best = INT64_MAX;
+                int med = 0;
+                for (l = 0; l < m->lcm; l++) {
+                    int inter = 1 << l;
+                    int shared = ((i & inter) != 0) + ((j & inter) != 0) + ((k & inter) != 0);
+                    int64_t c;
+                    if (m->is_metric || shared >= 2 || inter != m->gap)
+                        c = (int64_t)m->cost[(inter << 5) + i] + m->cost[(inter << 5) + j] +
+                            m->cost[(inter << 5) + k];
+                    else
+                        c = INT64_MAX;
+                    if (c < best) { best = c; med = inter; }
+                    else if (c == best) med |= inter;
+                }
+                tab[(i << 10) | (j << 5) | k] = (uint8_t)(med & -med);
+            }
+}
+
+int or_readjust_3d(const uint8_t *s1, int l1, const uint8_t *s2, int l2, const uint8_t *cm_,
+                   int lm, const uint8_t *p, int lp, const or_cm *m, const uint8_t *tab3,
+                   uint8_t *res, int *lres, int *changed) {
+    /* Sequence.Align.readjust_3d with first_gap = true
+     * (sequence.ml:1117-1140): the early returns, then
+     * align_3_powell_inter (sequence.ml:1089-1115) with mm = cost 1 2,
+     * go = the affine opening (0 for the linear model) and ge = cost 1 16;
+     * the median keeps the non-gap column medians behind one leading gap.
+     * cm_ is the node's current median m.  Returns the cost, or -1 where
+     * the reference fails (an element without A, C, G or T). */
+    int gap = m->gap, cost, n, x, q;
+    const uint8_t *keep = NULL;
+    int lkeep = 0;
+    if (l1 == l2 && lm == lp && l1 == lm) { keep = cm_; lkeep = lm; cost = 0; }
+    else if (is_empty(s1, l1, gap) && !is_empty(s2, l2, gap)) { keep = s2; lkeep = l2; cost = 0; }
+    else if (is_empty(s2, l2, gap) && !is_empty(s1, l1, gap)) { keep = s1; lkeep = l1; cost = 0; }
+    else if (is_empty(p, lp, gap)) { keep = p; lkeep = lp; cost = 0; }
+    if (keep) {
+        memcpy(res, keep, (size_t)lkeep);
+        *lres = lkeep;
+    } else {
+        int cap = l1 + l2 + lp;
+        uint8_t *oa = (uint8_t *)malloc((size_t)cap), *ob = (uint8_t *)malloc((size_t)cap),
+                *oc = (uint8_t *)malloc((size_t)cap);
+        int mmc = m->cost[(1 << 5) + 2], ge = m->cost[(1 << 5) + 16];
+        int go = m->cost_model == 1 ? m->gap_open : 0;
+        cost = or_powell_3d(s1, l1, s2, l2, p, lp, mmc, go, ge, oa, ob, oc, &n);
+        if (cost < 0) { free(oa); free(ob); free(oc); return -1; }
+        q = 0;
+        res[q++] = (uint8_t)gap;
+        for (x = 0; x < n; x++) {
+            int md = tab3[(oa[x] << 10) | (ob[x] << 5) | oc[x]];
+            if (md != gap) res[q++] = (uint8_t)md;
+        }
+        *lres = q;
+        free(oa); free(ob); free(oc);
+    }
+    *changed = (*lres != lm) || memcmp(res, cm_, (size_t)lm) != 0;
+    return cost;
+}

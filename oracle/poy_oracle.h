@@ -199,6 +199,29 @@ void or_sank_elt_median_3(int k, const int64_t *tcm, const int64_t *a_s, const i
 double or_sank_elt_distance(int k, const int64_t *tcm, const int64_t *a_s,
                             const int64_t *b_s);
 
+
+/* ---- Three-sequence alignment of the Iterative (ThreeD) mode ---- */
+#define OR_P3_STATES 16
+/* powell_3D_align (ukkCommon.c:111-143): optimal cost of aligning three
+ * sequences (each with its leading gap) under Powell's state model with
+ * mismatch mm, gap opening go and extension ge.  Writes the aligned rows
+ * (characters reduced to one base, 16 for gaps, leading gap first) to
+ * oa/ob/oc (capacity la + lb + lc) and their length to *olen.  Returns -1
+ * for an element with none of A, C, G, T. */
+int or_powell_3d(const uint8_t *a, int la, const uint8_t *b, int lb, const uint8_t *c, int lc,
+                 int mm, int go, int ge, uint8_t *oa, uint8_t *ob, uint8_t *oc, int *olen);
+/* The least alignmentCost (ukkCommon.c:345-391) of a given alignment. */
+int or_powell_alignment_cost(const uint8_t *oa, const uint8_t *ob, const uint8_t *oc, int n,
+                             int mm, int go, int ge);
+/* Cost_matrix.Three_D median table from a 2-D matrix (cost_matrix.ml:803-851),
+ * 32768 bytes indexed (i << 10) | (j << 5) | k. */
+void or_median3_table(const or_cm *m, uint8_t *tab);
+/* Sequence.Align.readjust_3d (sequence.ml:1117-1140): new median of a node
+ * from its children s1, s2, its current median cm_ and its parent p. */
+int or_readjust_3d(const uint8_t *s1, int l1, const uint8_t *s2, int l2, const uint8_t *cm_,
+                   int lm, const uint8_t *p, int lp, const or_cm *m, const uint8_t *tab3,
+                   uint8_t *res, int *lres, int *changed);
+
 #ifdef __cplusplus
 }
 #endif

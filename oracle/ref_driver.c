@@ -282,3 +282,22 @@ void ref_nonadd##W##_median_3(const void *A, const void *N, const void *D1,     
 }
 REF_NONADD_WIDE(16, 2)
 REF_NONADD_WIDE(32, 4)
+
+/* powell_3D_align (ukkCommon.c:111-143) through its OCaml external: three
+ * sequences with their leading gap, the aligned rows prepended into seqs
+ * of capacity la + lb + lc (align_3_powell, sequence.ml:1078-1087). */
+value powell_3D_align(value sa, value sb, value sc, value ra, value rb, value rc,
+                      value mm, value go, value ge);
+int ref_powell_3d(const uint8_t *a, int la, const uint8_t *b, int lb, const uint8_t *c, int lc,
+                  int mm, int go, int ge, uint8_t *oa, uint8_t *ob, uint8_t *oc, int *olen) {
+    int cap = la + lb + lc;
+    value va = make_seq(la, a, la), vb = make_seq(lb, b, lb), vc = make_seq(lc, c, lc);
+    value pa = make_seq(cap, NULL, 0), pb = make_seq(cap, NULL, 0), pc = make_seq(cap, NULL, 0);
+    int r = Int_val(powell_3D_align(va, vb, vc, pa, pb, pc, Val_int(mm), Val_int(go), Val_int(ge)));
+    *olen = seq_out(pa, oa);
+    seq_out(pb, ob);
+    seq_out(pc, oc);
+    free((void *)va); free((void *)vb); free((void *)vc);
+    free((void *)pa); free((void *)pb); free((void *)pc);
+    return r;
+}

@@ -87,7 +87,7 @@ void *ws_buffer(Workspace *w, int slot, size_t bytes);
 enum WsSlot {
   WS_TABLES = 0, WS_PLANS, WS_DMWORDS, WS_WD, WS_ORDER, WS_DM, WS_SCRATCH,
   WS_COUNTER, WS_CELLS, WS_AFF, WS_ERR, WS_SEQ, WS_META, WS_OUT, WS_BATCH, WS_ORDSCR,
-  WS_LVL_NODES, WS_LVL_PAIRS, WS_NSLOTS
+  WS_LVL_NODES, WS_LVL_PAIRS, WS_P3_RING, WS_P3_DIR, WS_P3_META, WS_P3_IO, WS_NSLOTS
 };
 
 int upload_tables(const poyd_cm *cm, DevTables **dev, void *stream);

@@ -71,7 +71,8 @@ EXPORTED = (
     "poyd_algn_backtrack_2d", "poyd_algn_cost_affine_3", "poyd_algn_median_2_no_gaps",
     "poyd_algn_median_2_with_gaps", "poyd_algn_simple_2", "poyd_algn_verify_2",
     "poyd_algn_worst_2", "poyd_align_2_batch", "poyd_align_2_host", "poyd_ancestor_2_batch",
-    "poyd_closest_batch", "poyd_cm_dna", "poyd_cm_of_matrix5", "poyd_colsum_bf16",
+    "poyd_closest_batch", "poyd_cm_dna", "poyd_cm_median3", "poyd_cm_of_matrix5",
+    "poyd_colsum_bf16",
     "poyd_cost_2_batch", "poyd_cost_2_batch_noalloc", "poyd_gemm_bf16", "poyd_int32_peak",
     "poyd_int_pipe_rate", "poyd_last_error", "poyd_launch_count", "poyd_matrix_create",
     "poyd_matrix_free", "poyd_median_2_no_gaps_batch", "poyd_median_2_with_gaps_batch",
@@ -80,8 +81,9 @@ EXPORTED = (
     "poyd_nonadd16_median_3_batch", "poyd_nonadd16_median_batch",
     "poyd_nonadd32_distance_batch", "poyd_nonadd32_median_3_batch",
     "poyd_nonadd32_median_batch", "poyd_nonadd8_distance_batch", "poyd_nonadd8_median_3_batch",
-    "poyd_nonadd8_median_batch", "poyd_pack_alignments", "poyd_profile_enable",
-    "poyd_profile_read", "poyd_relu_grad_bf16", "poyd_sank_distance_batch",
+    "poyd_nonadd8_median_batch", "poyd_pack_alignments", "poyd_powell_3D_align",
+    "poyd_powell_3d_batch", "poyd_profile_enable", "poyd_profile_read", "poyd_readjust_3d_batch",
+    "poyd_relu_grad_bf16", "poyd_sank_distance_batch",
     "poyd_sank_median_3_batch", "poyd_sank_median_batch", "poyd_to_bf16", "poyd_verify_2_batch", "poyd_version",
     "poyd_worst_2_batch",
 )
@@ -130,6 +132,12 @@ SIGNATURES = [
     ("poyd_algn_verify_2", C.c_int, [_vp, _vp, _i32, _cmp, _vp]),
     ("poyd_closest_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _i32, _vp]),
+    ("poyd_cm_median3", C.c_int, [_cmp, _vp]),
+    ("poyd_powell_3D_align", C.c_int, [_vp, _i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _i32, _vp,
+                                       _i32, _i32, _i32, _vp]),
+    ("poyd_powell_3d_batch", C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,
+                                       _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("poyd_readjust_3d_batch", C.c_int, [_cmp, _i32] + [_vp] * 14 + [_vp]),
     ("poyd_int32_peak", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("poyd_int_pipe_rate", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]

@@ -153,3 +153,24 @@ def pair_batch_fast(seed: int, n_pairs: int, lmin: int = 100, lmax: int = 5000,
     sizes[0::2], sizes[1::2] = a_len, b_len
     starts = np.cumsum(sizes) - sizes
     return [seq, starts[0::2].copy(), a_len, starts[1::2].copy(), b_len]
+
+
+def triple_batch(seed: int, n: int, lmin: int = 50, lmax: int = 300,
+                 sub=(0.05, 0.20), indel=(0.01, 0.04), ambig: float = 0.02):
+    """Triples (child 1, child 2, parent) of a three-way alignment: three
+    descendants of one random ancestor of length U[lmin, lmax], each with
+    its own substitutions and indels, plus IUPAC ambiguity masks.  Returns a
+    list of 3-tuples of uint8 arrays with the leading gap."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        anc = random_dna(rng, int(rng.integers(lmin, lmax + 1)))
+        t = []
+        for _k in range(3):
+            s = mutate(rng, anc, float(rng.uniform(*sub)), float(rng.uniform(*indel)))
+            if ambig > 0 and len(s):
+                m = rng.random(len(s)) < ambig
+                s[m] = AMBIG[rng.integers(0, len(AMBIG), size=int(m.sum()))]
+            t.append(with_gap(s))
+        out.append(tuple(t))
+    return out

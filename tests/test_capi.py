@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "poyd_gb300.h")
 def declared_symbols():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(poyd_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(poyd_[A-Za-z0-9_]+)\s*\(", src)))
 
 
 @pytest.fixture(scope="module")
