@@ -65,13 +65,17 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="launch the default variant instead of the autotuner's choice")
     p.add_argument("--no-extras", action="store_true",
-                   help="headline only: skip the affine, SPR, learned and serving keys")
+                   help="headline only: skip the affine, SPR, learned, readjust_3d and serving keys")
     p.add_argument("--workload", default="align",
-                   choices=["align", "spr", "tbr", "learned", "serving", "kernels"],
+                   choices=["align", "spr", "tbr", "learned", "serving", "kernels", "three"],
                    help="align (default, the headline line) or one of the other configs")
     p.add_argument("--train-trees", type=int, default=2)
     p.add_argument("--max-passes", type=int, default=8)
     p.add_argument("--serve-s", type=float, default=10.0)
+    p.add_argument("--triples", type=int, default=1216,
+                   help="three: node triples per step (readjust_3d)")
+    p.add_argument("--tri-len", type=int, nargs=2, default=[100, 300],
+                   help="three: ancestor length range of the triples")
     return p.parse_args()
 
 
@@ -289,7 +293,8 @@ def run_ours(args):
     if rank == 0 and world == 1 and args.workload == "align" and not args.no_extras:
         # The other configurations, on a bounded budget, as keys of the same
         # line: the affine variant of the same pairs, one SPR pass's
-        # candidate scoring, the learned vs plain search and the serving loop.
+        # candidate scoring, the learned vs plain search, the Iterative
+        # (ThreeD) node readjustments and the serving loop.
         extras = argparse.Namespace(**vars(args))
         extras.cpu_sample_s = min(args.cpu_sample_s, 6.0)
         extras.serve_s = min(args.serve_s, 8.0)
@@ -312,6 +317,10 @@ def run_ours(args):
         # search's exact cost
         line["learned_speedup"] = lrn.get("speedup") if lrn.get("reached_same_cost") else None
         line["learned"] = lrn
+        tri = argparse.Namespace(**vars(extras))
+        tri.steps, tri.warmup = min(args.steps, 5), 1
+        line["readjust_3d"] = _guard(lambda: run_three(tri))
+        failed |= bool(line["readjust_3d"].get("parity", {}).get("mismatches"))
         srv = _guard(lambda: run_serving(extras))
         line["serving"] = {"req_s": srv.get("value"), "p50_ms": srv.get("p50_ms"),
                            "p99_ms": srv.get("p99_ms"), **srv}
@@ -717,6 +726,109 @@ def run_serving(args):
            "jobs": st["n"], "sample_identical_alone": bool(ok)})
 
 
+def run_three(args):
+    """Iterative (ThreeD) mode: ``Sequence.Align.readjust_3d`` for a batch of
+    node triples (two children, the current median, the parent) descended
+    from seeded ancestors of --tri-len bp with 5-20 % substitutions and
+    1-4 % indels per sequence, DNA sub 1 / indel 2 (Powell's mm 1, go 0,
+    ge 2).  A step is one batched readjust of every triple.  Device-resident
+    value (triples/s, cube cells/s), the end-to-end run from pinned host
+    buffers (uploads, the call, the download of every result), parity with
+    the oracle on the smallest triples and the oracle's CPU rate on a
+    sample."""
+    import torch
+    from oracle import oracle as O
+    from poyd_gb300 import align, native, synth, three
+    torch.cuda.set_device(0)
+    T = synth.triple_batch(args.seed, args.triples, args.tri_len[0], args.tri_len[1])
+    items = [(a, b, a.copy(), p) for a, b, p in T]  # current median: the first child
+    cm = align.CostMatrix.dna(1, 2)
+    seq, offs, lens = three.TripleBatch.pack_host(items)
+    host = [torch.from_numpy(x).pin_memory() for x in [seq] + offs + lens]
+    batch = three.TripleBatch(host[0].cuda(), [x.cuda() for x in host[1:5]],
+                              [x.cuda() for x in host[5:9]])
+    cells = float(sum(len(a) * len(b) * len(p) for a, b, _, p in items))
+    native.lib().poyd_profile_enable(1)
+    native.profile_read(clear=True)
+    for _ in range(max(args.warmup, 1)):
+        r = three.readjust_3d(batch, cm)
+    torch.cuda.synchronize()
+    native.profile_read(clear=True)
+    launches0 = native.lib().poyd_launch_count()
+    steps = max(args.steps, 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        r = three.readjust_3d(batch, cm)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    kern_ms = native.profile_read("p3", clear=True)[0] / steps
+    launches = (native.lib().poyd_launch_count() - launches0) / steps
+    # end to end: pinned host inputs -> device, readjust, every result back
+    e2e_ms, h2d, d2h = [], 0, 0
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev = [x.to("cuda", non_blocking=True) for x in host]
+        b2 = three.TripleBatch(dev[0], dev[1:5], dev[5:9])
+        r2 = three.readjust_3d(b2, cm)
+        outs = [r2.out.to("cpu"), r2.out_len.to("cpu"), r2.cost.to("cpu"), r2.changed.to("cpu")]
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        h2d = sum(x.numel() * x.element_size() for x in host)
+        d2h = sum(x.numel() * x.element_size() for x in outs)
+    e2e = float(np.median(e2e_ms))
+    # parity: the smallest triples against the oracle (cost, median, changed)
+    res = r.to_host()
+    order = np.argsort([len(a) * len(b) * len(p) for a, b, _, p in items])[:6]
+    m = O.cm_dna(1, 2, -1)
+    tab = O.median3_table(m)
+    bad = 0
+    for i in order:
+        c, med, ch = O.readjust_3d(*items[i], m, tab)
+        bad += (c, ch) != (res[i]["cost"], res[i]["changed"]) or not np.array_equal(med, res[i]["median"])
+    # the oracle's rate on a sample of median-sized triples, all host threads
+    threads = os.cpu_count() or 1
+    mid = np.argsort([len(a) * len(b) * len(p) for a, b, _, p in items])
+    pick = mid[len(mid) // 2 - threads // 2:len(mid) // 2 - threads // 2 + threads]
+
+    def work(i):
+        O.readjust_3d(*items[i], m, tab)
+    ths = [threading.Thread(target=work, args=(int(i),)) for i in pick]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    cdt = time.perf_counter() - t0
+    ccells = float(sum(len(items[i][0]) * len(items[i][1]) * len(items[i][3]) for i in pick))
+    pairs_per_cell = 256  # (previous, next) state pairs: one fused add-min each
+    peak = native.int32_peak()
+    del r, r2, outs, batch
+    native.check(native.lib().poyd_workspace_release())  # the choice cubes: tens of GB
+    return {
+        "workload": "Iterative (ThreeD) readjust_3d: %d node triples, ancestors %d-%d bp, "
+                    "DNA sub 1 / indel 2" % (args.triples, args.tri_len[0], args.tri_len[1]),
+        "metric": "node readjustments per second", "value": args.triples / (ms * 1e-3),
+        "unit": "triples/s", "ms_per_step": ms, "steps": steps, "warmup": args.warmup,
+        "cube_cells_per_step": cells, "gcells_s": cells / (ms * 1e-3) / 1e9,
+        "kernel_ms_per_step": kern_ms, "gpu_launches": launches, "dtype": "int32",
+        "data": "synthetic (seeded)",
+        "roofline": {"bound": "int32", "achieved": cells * pairs_per_cell * 2 / (kern_ms * 1e-3) / 1e12
+                     if kern_ms else None, "peak": peak / 1e3, "unit": "Tops/s",
+                     "frac": cells * pairs_per_cell * 2 / (kern_ms * 1e-3) / 1e9 / peak
+                     if kern_ms else None,
+                     "ops_per_cell": "256 add-min (2 ops each) of 16 x 16 state pairs"},
+        "e2e": {"value": args.triples / (e2e * 1e-3), "unit": "triples/s", "ms_per_step": e2e,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "parity": {"checked": len(order), "mismatches": int(bad), "against": "oracle (or_readjust_3d)"},
+        "cpu_baseline": {"value": len(pick) / cdt, "unit": "triples/s", "cores": len(pick),
+                         "kind": "port", "gcells_s": ccells / cdt / 1e9,
+                         "sample": "%d median-sized triples of the batch, one per thread" % len(pick)},
+    }
+
+
 def run_kernels(args):
     """The other kernels on their own: Fitch and Sankoff distance / median
     over node arrays larger than L2 (HBM-bound: achieved GB/s of the bytes
@@ -854,6 +966,8 @@ def main():
         _emit(run_serving(args))
     elif args.workload == "kernels":
         _emit(run_kernels(args))
+    elif args.workload == "three":
+        _emit(run_three(args))
     else:
         run_ours(args)
 

@@ -66,6 +66,12 @@ typedef struct poyd_cm {
 
 const char *poyd_last_error(void);
 int poyd_version(void);
+/* Frees the device scratch the library keeps between calls (grow-only, per
+ * device and stream; the three-sequence choice cubes can reach tens of GB)
+ * for the current device.  No call of the library may be in flight on that
+ * device.  No reference counterpart (the reference frees its matrices with
+ * the OCaml custom block). */
+int poyd_workspace_release(void);
 
 /* Replaces Cost_matrix.Two_D.of_transformations_and_gaps true 5 sub indel 31
  * (cost_matrix.ml:645-656) followed, for gap_open >= 0, by

@@ -59,6 +59,27 @@ Workspace *workspace(cudaStream_t st) {
   return w;
 }
 
+// Frees every cached buffer of the current device's workspaces (the grow-
+// only scratch of all entry points); the next call allocates again.
+extern "C" int poyd_workspace_release(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaGetDevice");
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize");
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  for (auto &kv : g_ws) {
+    if (kv.first.first != dev) continue;
+    Workspace *w = kv.second;
+    for (int k = 0; k < WS_NSLOTS; ++k) {
+      if (w->ptr[k]) cudaFree(w->ptr[k]);
+      w->ptr[k] = nullptr;
+      w->size[k] = 0;
+    }
+    w->have_cm = false;
+  }
+  return POYD_OK;
+}
+
 void *ws_buffer(Workspace *w, int slot, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (w->size[slot] >= bytes) return w->ptr[slot];

@@ -84,6 +84,10 @@ __host__ __device__ constexpr P3States p3_states() {
   return S;
 }
 
+// The same tables for indices known only at run time (traceback, table
+// setup): constant memory rather than a local copy.
+__constant__ P3States c_p3 = p3_states();
+
 struct P3Args {
   int n, mode;            // mode 1: readjust_3d's early returns and changed flags
   const uint8_t *seq;
@@ -173,6 +177,81 @@ __device__ __forceinline__ uint64_t p3_cell(const P3Args &A, int32_t *ring, int6
   return word;
 }
 
+// The same cell with two values per 32-bit word, for batches whose costs
+// stay small: x16 values in 16-bit halves of a uint16 ring, each value
+// carrying its own state number in the low 4 bits, so that a value loaded
+// as a previous state already holds its rank, and one __viaddmin_u16x2
+// tries two previous states.  Infinity is 0xC000; every value is clamped
+// to it and every addend stays below 0x4000, so no half wraps.  A value
+// that reaches the clamp is not exact; a triple whose optimum reaches it is
+// redone by the 32-bit cell (the cells of an optimal path never exceed the
+// optimum, so a smaller optimum is exact).  Neighbours outside the cube
+// are read from a constant infinite cell, so the 14 loads of a cell issue
+// before any of its arithmetic.
+constexpr unsigned kP3Inf2 = 0xC000C000u;
+template <bool GO0>
+__device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16_t *dst,
+                                              const unsigned *gg, const uint4 ca,
+                                              const uint4 cb) {
+  constexpr P3States S = p3_states();
+  uint4 u[7][2];
+#pragma unroll
+  for (int d = 0; d < 7; ++d) {
+    const uint4 *p = reinterpret_cast<const uint4 *>(src[d]);
+    u[d][0] = p[0];
+    u[d][1] = p[1];
+  }
+  unsigned best[kP3States];
+#pragma unroll
+  for (int t = 0; t < kP3States; ++t) best[t] = kP3Inf2;
+#pragma unroll
+  for (int d = 1; d < 8; ++d) {
+    const unsigned w[8] = {u[d - 1][0].x, u[d - 1][0].y, u[d - 1][0].z, u[d - 1][0].w,
+                           u[d - 1][1].x, u[d - 1][1].y, u[d - 1][1].z, u[d - 1][1].w};
+#pragma unroll
+    for (int t = 0; t < kP3States; ++t) {
+      if (S.adv[t] != d) continue;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        best[t] = GO0 ? __vminu2(w[q], best[t])
+                      : __viaddmin_u16x2(w[q], gg[4 * S.ngo[2 * q][t] + S.ngo[2 * q + 1][t]],
+                                         best[t]);
+    }
+  }
+  const unsigned col2[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+  uint64_t word = 0;
+  unsigned v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {  // states 2k (low half) and 2k + 1 (high half)
+    const unsigned lo = __byte_perm(best[2 * k], best[2 * k + 1], 0x5410);
+    const unsigned hi = __byte_perm(best[2 * k], best[2 * k + 1], 0x7632);
+    const unsigned m = __vminu2(lo, hi);
+    const unsigned own = (unsigned)(2 * k) | (unsigned)(2 * k + 1) << 16;
+    v[k] = __vminu2((m & 0xFFF0FFF0u) + col2[k], kP3Inf2 + own);
+    word |= (uint64_t)(m & 15u) << (8 * k) | (uint64_t)(m >> 16 & 15u) << (8 * k + 4);
+  }
+  uint4 *o = reinterpret_cast<uint4 *>(dst);
+  o[0] = make_uint4(v[0], v[1], v[2], v[3]);
+  o[1] = make_uint4(v[4], v[5], v[6], v[7]);
+  return word;
+}
+
+// Column costs of the packed cell (x16, each state's own number added):
+// state pairs (2k, 2k + 1) for the characters x0, x1, x2 (0: none) of a
+// cell; an entry whose state needs a missing character is never used.
+__device__ __forceinline__ unsigned p3_col2(int k, int x0, int x1, int x2, int mm16, int ge16) {
+  const P3States &S = c_p3;
+  unsigned r = 0;
+  for (int h = 0; h < 2; ++h) {
+    const int t = 2 * k + h, d = S.adv[t];
+    const int ch = ((d & 1) ? x0 : 0) | ((d & 2) ? x1 : 0) | ((d & 4) ? x2 : 0);
+    const int col = S.ins[t] ? ge16 : mm16 * max(__popc(ch) - 1, 0) + S.ndel[t] * ge16;
+    r |= (unsigned)(col + t) << (16 * h);
+  }
+  return r;
+}
+
+template <bool PACKED, bool GO0>
 __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Args A) {
   constexpr P3States S = p3_states();
   extern __shared__ uint8_t p3_sm[];
@@ -184,6 +263,24 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
   // x16 costs: g16[k] = k gap openings, g16[4] = one extension
   const int g16[5] = {0, 16 * A.go, 32 * A.go, 48 * A.go, 16 * A.ge};
   int32_t *ring = A.ring + (int64_t)blockIdx.x * A.ring_stride;
+  // packed: [infinite cell | ring]; the column-cost table after the
+  // sequences in shared memory, 8 words per (x0, x1, x2), each 0..4
+  uint16_t *const infc = reinterpret_cast<uint16_t *>(ring);
+  uint16_t *const ring16 = infc + kP3States;
+  uint4 *const ctab = reinterpret_cast<uint4 *>(p3_sm + 3 * A.smax);
+  unsigned gg[16];  // packed opening costs of two previous states
+#pragma unroll
+  for (int k = 0; k < 16; ++k) gg[k] = (unsigned)g16[k >> 2] | (unsigned)g16[k & 3] << 16;
+  if (PACKED) {
+    if (tid < 2) reinterpret_cast<uint4 *>(infc)[tid] = make_uint4(kP3Inf2, kP3Inf2, kP3Inf2, kP3Inf2);
+    for (int e = tid; e < 125 * 8; e += kP3Threads) {
+      const int cmb = e >> 3, k = e & 7;
+      const int i0 = cmb / 25, i1 = cmb / 5 % 5, i2 = cmb % 5;
+      reinterpret_cast<unsigned *>(ctab)[e] =
+          p3_col2(k, i0 ? 1 << (i0 - 1) : 0, i1 ? 1 << (i1 - 1) : 0, i2 ? 1 << (i2 - 1) : 0,
+                  16 * A.mm, g16[4]);
+    }
+  }
   uint64_t *dir = A.dir + (int64_t)blockIdx.x * A.dir_stride;
 
   for (;;) {
@@ -265,13 +362,44 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
       for (int a = a_lo + warp; a <= a_hi; a += kWarps) {  // a warp per row
         const int s = h - a, blo = max(0, s - nc), bhi = min(nb, s);
         const int64_t drow = (int64_t)a * bcs + p3_soff(s, nb, nc) - blo;
+        if (PACKED && h > 0) {
+          // row bases (uint16 units) of the 7 neighbours and of the cell
+          int rb[7];
+#pragma unroll
+          for (int d = 1; d < 8; ++d) {
+            const int da = d & 1, db = d >> 1 & 1, dc = d >> 2 & 1;
+            rb[d - 1] = (((h - da - db - dc) & 3) * (int)pl + (a - da) * (nb + 1) - db) * kP3States;
+          }
+          const int ob = ((h & 3) * (int)pl + a * (nb + 1)) * kP3States;
+          const int i0 = a ? __ffs(sq[0][a]) : 0;
+          for (int b = blo + lane; b <= bhi; b += 32) {
+            const int c = s - b, b16 = b * kP3States;
+            const uint16_t *src[7];
+#pragma unroll
+            for (int d = 1; d < 8; ++d) {
+              const bool ok = (a >= (d & 1)) && (b >= (d >> 1 & 1)) && (c >= (d >> 2 & 1));
+              src[d - 1] = ok ? ring16 + rb[d - 1] + b16 : infc;
+            }
+            const int cmb = (i0 * 5 + (b ? __ffs(sq[1][b]) : 0)) * 5 + (c ? __ffs(sq[2][c]) : 0);
+            dir[drow + b] = p3_cell16<GO0>(src, ring16 + ob + b16, gg, ctab[2 * cmb],
+                                           ctab[2 * cmb + 1]);
+          }
+          continue;
+        }
         for (int b = blo + lane; b <= bhi; b += 32) {
           const int c = s - b;
           uint64_t word = 0;
           if (h == 0) {  // the start: MMM at cost 0
-            int4 *r = reinterpret_cast<int4 *>(ring);
-            r[0] = make_int4(0, kP3Inf, kP3Inf, kP3Inf);
-            for (int q = 1; q < 4; ++q) r[q] = make_int4(kP3Inf, kP3Inf, kP3Inf, kP3Inf);
+            if (PACKED) {
+              uint4 *r = reinterpret_cast<uint4 *>(ring16);
+              // every value carries its own state number
+              r[0] = make_uint4(0xC0010000u, 0xC003C002u, 0xC005C004u, 0xC007C006u);
+              r[1] = make_uint4(0xC009C008u, 0xC00BC00Au, 0xC00DC00Cu, 0xC00FC00Eu);
+            } else {
+              int4 *r = reinterpret_cast<int4 *>(ring);
+              r[0] = make_int4(0, kP3Inf, kP3Inf, kP3Inf);
+              for (int q = 1; q < 4; ++q) r[q] = make_int4(kP3Inf, kP3Inf, kP3Inf, kP3Inf);
+            }
           } else {
             // alignmentCost's mismatches (ukkCommon.c:381-389), x16, by the
             // sequences a column consumes: mm per extra distinct character
@@ -292,17 +420,23 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
     }
 
     if (tid == 0) {
-      const int32_t *fin = ring + ((int64_t)(H & 3) * pl + (int64_t)na * (nb + 1) + nb) * kP3States;
-      int best = kP3Inf, st = 0;
-      for (int s = 0; s < kP3States; ++s)
-        if (fin[s] < best) best = fin[s], st = s;
+      const int64_t fo = ((int64_t)(H & 3) * pl + (int64_t)na * (nb + 1) + nb) * kP3States;
+      const int inf = PACKED ? 0xC000 : kP3Inf;
+      int best = inf, st = 0;
+      for (int s = 0; s < kP3States; ++s) {
+        const int f = PACKED ? (int)(ring16[fo + s] & 0xFFF0u) : ring[fo + s];
+        if (f < best) best = f, st = s;
+      }
+      if (PACKED && best >= inf) {  // the optimum reached the clamp: redo in 32 bits
+        if (tid == 0) atomicOr(A.err, 4);
+      }
       int a = na, b = nb, c = nc, n = 0, nm = 0;
-      bool okw = best < kP3Inf;
+      bool okw = best < inf;
       while (okw && (a | b | c)) {
         const int s = b + c;
         const uint64_t wd = dir[(int64_t)a * bcs + p3_soff(s, nb, nc) + (b - max(0, s - nc))];
         const int prev = (int)(wd >> (4 * st) & 15);
-        const int ad = S.adv[st];
+        const int ad = c_p3.adv[st];
         if ((ad & 1) > a || (ad >> 1 & 1) > b || (ad >> 2 & 1) > c) {
           okw = false;  // cannot happen for a finite optimum; kept as a guard
           break;
@@ -324,7 +458,7 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
       o[cap - n] = o[2 * cap - n] = o[3 * cap - n] = 16;
       if (A.has_med) o[4 * cap - ++nm] = (uint8_t)A.gap;
       if (!okw) {
-        atomicOr(A.err, 2);
+        if (!PACKED) atomicOr(A.err, 2);
         n = nm = -1;
       }
       A.cost[i] = okw ? best >> 4 : -1;
@@ -438,22 +572,34 @@ static int p3_run(int mode, int32_t n, const uint8_t *seq, const int64_t *const 
               median3 ? median3[(st5[x] << 10) | (st5[y] << 5) | st5[z]] : (uint8_t)gap;
   }
   A.smax = smax;
-  const size_t smem = 3 * (size_t)smax;
-  if (smem > 48 * 1024)
-    CK3(cudaFuncSetAttribute(k_p3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  {
-    ProfScope ps("p3", st);
-    k_p3<<<(unsigned)blocks, kP3Threads, smem, st>>>(A);
+  const size_t smem = 3 * (size_t)smax + 125 * 8 * sizeof(unsigned);
+  // 16-bit halves while every addend of a half stays below 0x4000
+  // (openings, column costs); a triple whose optimum reaches the clamp
+  // sets err bit 4 and the batch is redone in 32 bits
+  const char *pk = getenv("POYD_P3_PACKED");
+  bool packed = !(pk && pk[0] == '0') && 48LL * go + 15 < 0x4000 &&
+                16LL * (2LL * mm + 3LL * ge) < 0x4000;
+  for (;;) {
+    auto kern = packed ? (go == 0 ? k_p3<true, true> : k_p3<true, false>) : k_p3<false, false>;
+    if (smem > 48 * 1024)
+      CK3(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    {
+      ProfScope ps("p3", st);
+      kern<<<(unsigned)blocks, kP3Threads, smem, st>>>(A);
+    }
+    CK3(cudaGetLastError());
+    int32_t herr = 0;
+    CK3(cudaMemcpyAsync(&herr, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK3(cudaStreamSynchronize(st));
+    if (herr & 1)
+      return fail(POYD_EINVAL, "an element holds none of A, C, G, T (powell_3D_align fails, "
+                               "ukkCommon.c:101): its triple has cost -1");
+    if (herr & 2) return fail(POYD_ERANGE, "three-sequence traceback left the cube");
+    if (!(herr & 4)) return POYD_OK;
+    packed = false;  // some optimum reached the 16-bit clamp
+    const int32_t zero2[2] = {0, 0};
+    CK3(cudaMemcpyAsync(A.counter, zero2, sizeof(zero2), cudaMemcpyHostToDevice, st));
   }
-  CK3(cudaGetLastError());
-  int32_t herr = 0;
-  CK3(cudaMemcpyAsync(&herr, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  CK3(cudaStreamSynchronize(st));
-  if (herr & 1)
-    return fail(POYD_EINVAL, "an element holds none of A, C, G, T (powell_3D_align fails, "
-                             "ukkCommon.c:101): its triple has cost -1");
-  if (herr & 2) return fail(POYD_ERANGE, "three-sequence traceback left the cube");
-  return POYD_OK;
 }
 
 // Cost_matrix.Three_D.of_two_dim_comb (cost_matrix.ml:803-851): the median

@@ -85,7 +85,7 @@ EXPORTED = (
     "poyd_powell_3d_batch", "poyd_profile_enable", "poyd_profile_read", "poyd_readjust_3d_batch",
     "poyd_relu_grad_bf16", "poyd_sank_distance_batch",
     "poyd_sank_median_3_batch", "poyd_sank_median_batch", "poyd_to_bf16", "poyd_verify_2_batch", "poyd_version",
-    "poyd_worst_2_batch",
+    "poyd_workspace_release", "poyd_worst_2_batch",
 )
 
 # (name, restype, argtypes) of the entry points the Python mirror calls
@@ -133,6 +133,7 @@ SIGNATURES = [
     ("poyd_closest_batch", C.c_int, [_cmp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _i32, _vp]),
     ("poyd_cm_median3", C.c_int, [_cmp, _vp]),
+    ("poyd_workspace_release", C.c_int, []),
     ("poyd_powell_3D_align", C.c_int, [_vp, _i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _i32, _vp,
                                        _i32, _i32, _i32, _vp]),
     ("poyd_powell_3d_batch", C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32,

@@ -103,3 +103,39 @@ def test_long_triples_properties():
             assert len(col) == len(s) - 1
     same = three.align_3_powell(three.TripleBatch.from_host([(T[0][0],) * 3]), 1, 2, 1).to_host()
     assert same[0]["cost"] == 0
+
+
+def test_packed_and_32_bit_kernels_agree(monkeypatch):
+    # the 16-bit kernel (default) and the 32-bit one give the same rows
+    T = synth.triple_batch(12, 24, lmin=0, lmax=90)
+    b = three.TripleBatch.from_host(T)
+    packed = three.align_3_powell(b, 1, 2, 1).to_host()
+    monkeypatch.setenv("POYD_P3_PACKED", "0")
+    wide = three.align_3_powell(b, 1, 2, 1).to_host()
+    for x, y in zip(packed, wide):
+        assert x["cost"] == y["cost"]
+        for k in "abc":
+            assert np.array_equal(x[k], y[k])
+
+
+def test_optimum_above_the_16_bit_range_is_redone_in_32_bits():
+    # mm = ge = 100: the optima exceed 3,072, the 16-bit kernel's range
+    T = synth.triple_batch(8, 5, lmin=30, lmax=40, sub=(0.3, 0.5), indel=(0.05, 0.1))
+    T.append(synth.triple_batch(9, 1, lmin=3, lmax=5)[0])
+    res = three.align_3_powell(three.TripleBatch.from_host(T), 100, 0, 100).to_host()
+    assert max(r["cost"] for r in res) > 3072
+    for t, r in zip(T, res):
+        c, *rows = O.powell_3d(*t, 100, 0, 100)
+        assert c == r["cost"]
+        for x, k in zip(rows, "abc"):
+            assert np.array_equal(x, r[k])
+
+
+def test_workspace_release_then_reuse():
+    T = synth.triple_batch(14, 4, lmin=10, lmax=40)
+    b = three.TripleBatch.from_host(T)
+    first = three.align_3_powell(b, 1, 2, 1).to_host()
+    native.check(native.lib().poyd_workspace_release())
+    again = three.align_3_powell(b, 1, 2, 1).to_host()
+    assert [r["cost"] for r in first] == [r["cost"] for r in again]
+    assert all(np.array_equal(x["a"], y["a"]) for x, y in zip(first, again))
