@@ -740,6 +740,9 @@ def run_three(args):
     from oracle import oracle as O
     from poyd_gb300 import align, native, synth, three
     torch.cuda.set_device(0)
+    # the choice cubes want free memory: drop what earlier workloads cached
+    torch.cuda.empty_cache()
+    native.check(native.lib().poyd_workspace_release())
     T = synth.triple_batch(args.seed, args.triples, args.tri_len[0], args.tri_len[1])
     items = [(a, b, a.copy(), p) for a, b, p in T]  # current median: the first child
     cm = align.CostMatrix.dna(1, 2)

@@ -523,8 +523,8 @@ static int p3_run(int mode, int32_t n, const uint8_t *seq, const int64_t *const 
   CK3(cudaMemGetInfo(&fr, &tot));
   const int64_t per_block = ring_max * 4 + dir_max * 8;
   // the choice cubes dominate: one per resident block, sized for the
-  // largest triple; by default at most half the free memory, 96 GiB
-  int64_t budget = std::min<int64_t>((int64_t)(fr / 2), 96LL << 30);
+  // largest triple; by default at most 60 % of the free memory, 120 GiB
+  int64_t budget = std::min<int64_t>((int64_t)(fr * 0.6), 120LL << 30);
   if (const char *e = getenv("POYD_P3_BUDGET_MB")) budget = std::max<int64_t>(1, atoll(e)) << 20;
   int64_t blocks = std::min<int64_t>({(int64_t)n, 3LL * sms, std::max<int64_t>(1, budget / per_block)});
 
