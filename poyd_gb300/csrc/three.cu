@@ -189,6 +189,9 @@ __device__ __forceinline__ uint64_t p3_cell(const P3Args &A, int32_t *ring, int6
 // are read from a constant infinite cell, so the 14 loads of a cell issue
 // before any of its arithmetic.
 constexpr unsigned kP3Inf2 = 0xC000C000u;
+// min per half (measured: the fused add-min with a zero addend in its
+// place executes 365 instructions per cell instead of 331)
+__device__ __forceinline__ unsigned p3_min2(unsigned a, unsigned b) { return __vminu2(a, b); }
 template <bool GO0>
 __device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16_t *dst,
                                               const unsigned *gg, const uint4 ca,
@@ -213,7 +216,7 @@ __device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16
       if (S.adv[t] != d) continue;
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        best[t] = GO0 ? __vminu2(w[q], best[t])
+        best[t] = GO0 ? p3_min2(w[q], best[t])
                       : __viaddmin_u16x2(w[q], gg[4 * S.ngo[2 * q][t] + S.ngo[2 * q + 1][t]],
                                          best[t]);
     }
@@ -225,9 +228,9 @@ __device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16
   for (int k = 0; k < 8; ++k) {  // states 2k (low half) and 2k + 1 (high half)
     const unsigned lo = __byte_perm(best[2 * k], best[2 * k + 1], 0x5410);
     const unsigned hi = __byte_perm(best[2 * k], best[2 * k + 1], 0x7632);
-    const unsigned m = __vminu2(lo, hi);
+    const unsigned m = p3_min2(lo, hi);
     const unsigned own = (unsigned)(2 * k) | (unsigned)(2 * k + 1) << 16;
-    v[k] = __vminu2((m & 0xFFF0FFF0u) + col2[k], kP3Inf2 + own);
+    v[k] = p3_min2((m & 0xFFF0FFF0u) + col2[k], kP3Inf2 + own);
     word |= (uint64_t)(m & 15u) << (8 * k) | (uint64_t)(m >> 16 & 15u) << (8 * k + 4);
   }
   uint4 *o = reinterpret_cast<uint4 *>(dst);
