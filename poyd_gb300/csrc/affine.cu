@@ -421,10 +421,10 @@ struct AffSmem2 {
 __device__ __forceinline__ uint32_t am2(uint32_t a, uint32_t b) {
   return __viaddmin_u16x2(a, b, kInfA2);  // saturating add, both halves
 }
-// min / max per half as the fused add-min / add-max with a zero addend (one
-// instruction each; the plain SIMD min and max are not)
-__device__ __forceinline__ uint32_t mn2(uint32_t a, uint32_t b) { return __viaddmin_u16x2(a, 0u, b); }
-__device__ __forceinline__ uint32_t mx2(uint32_t a, uint32_t b) { return __viaddmax_u16x2(a, 0u, b); }
+// min / max per half (measured: the plain SIMD forms run the 65,536-pair DP
+// in 46.7-47.1 ms, the fused add-min / add-max with a zero addend in 48.8)
+__device__ __forceinline__ uint32_t mn2(uint32_t a, uint32_t b) { return __vminu2(a, b); }
+__device__ __forceinline__ uint32_t mx2(uint32_t a, uint32_t b) { return __vmaxu2(a, b); }
 // selects b where m is all ones, else a (m: 0 / 0xFFFF per half)
 __device__ __forceinline__ uint32_t sel2(uint32_t a, uint32_t b, uint32_t m) {
   return (a & ~m) | (b & m);
