@@ -367,6 +367,77 @@ def readjust_3d(s1, s2, cur, p, m, tab3=None):
     return cost, res[:lr.value].copy(), bool(ch.value)
 
 
+def select_one(s, m):
+    """Sequence.select_one (sequence.ml:1143-1156): every element becomes its
+    lowest state (combination alphabets; list_of_bits, cost_matrix.ml:206-217,
+    sorted ascending)."""
+    s = _u8(s)
+    if not m.combinations:
+        return s.copy()
+    if np.any(s == 0):
+        raise ValueError("select_one: an element with no states")
+    return (s & ((-s.astype(np.int16)) & 0xFF).astype(np.uint8)).astype(np.uint8)
+
+
+def algn_median(s1, s2, m):
+    """The `algn` of Sequence.readjust / DOS.readjust (sequence.ml:1168-1178,
+    seqCS.ml:684-698) before select_one: (cost, median); linear: align_2 then
+    median_2 (algn_CAML_median_2_no_gaps); affine: align_affine_3's median."""
+    if m.cost_model == 1:
+        c, med, _mwg, _ri, _rj = align_affine_3(s1, s2, m)
+        return c, med
+    c, ra, rb = align_2(s1, s2, m)
+    return c, median_2(ra, rb, m)
+
+
+def seq_readjust(a, b, parent, m):
+    """Sequence.readjust a b m cm parent, ApproxD mode (sequence.ml:1166-1195):
+    the three pairwise medians, each aligned with the third sequence; the
+    cheapest centre's median made closest to the third (Align.closest,
+    sequence.ml:967-1033).  Returns (cost, sequence)."""
+    c = parent
+    cab, ab = algn_median(a, b, m)
+    cbc, bc = algn_median(b, c, m)
+    cac, ac = algn_median(a, c, m)
+    cabc = algn_median(ab, c, m)[0] + cab
+    cbca = algn_median(bc, a, m)[0] + cbc
+    cacb = algn_median(ac, b, m)[0] + cac
+    if cabc <= cbca:
+        if cabc <= cacb:
+            return cabc, closest(c, ab, m, dos_empty=False)
+        return cacb, closest(b, ac, m, dos_empty=False)
+    if cbca < cacb:
+        return cbca, closest(a, bc, m, dos_empty=False)
+    return cacb, closest(b, ac, m, dos_empty=False)
+
+
+def dos_readjust(mode, ch1, ch2, parent, mine, m, tab3=None):
+    """DOS.readjust (seqCS.ml:680-722) of one DO character: mode "three"
+    (Iterative ThreeD: Sequence.Align.readjust_3d) or "approx" (ApproxD:
+    Sequence.readjust), with the rules for empty neighbours.  Returns
+    (changed, new sequence, cost); changed is `0 <> compare res mine`."""
+    ch1, ch2, parent, mine = _u8(ch1), _u8(ch2), _u8(parent), _u8(mine)
+    gap = m.gap
+    e1, e2, ep = (bool(np.all(x == gap)) for x in (ch1, ch2, parent))
+    if not (e1 or e2 or ep):
+        if mode == "three":
+            cost, res, _ = readjust_3d(ch1, ch2, mine, parent, m, tab3)
+        else:
+            cost, res = seq_readjust(ch1, ch2, parent, m)
+    elif e1 and e2:
+        cost, res = 0, ch1.copy()
+    elif e1 and ep:
+        cost, res = 0, ch1.copy()
+    elif e2 and ep:
+        cost, res = 0, ch2.copy()
+    else:
+        x, y = (ch1, ch2) if ep else (ch1, parent) if e2 else (ch2, parent)
+        cost, med = algn_median(x, y, m)
+        res = select_one(med, m)
+    changed = not (len(res) == len(mine) and np.array_equal(res, mine))
+    return changed, res, int(cost)
+
+
 def nonadd_median(a, b):
     a, b = _u8(a), _u8(b)
     r = np.zeros(len(a), np.uint8)

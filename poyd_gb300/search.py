@@ -549,6 +549,29 @@ class GpuBackend:
         o, l = int(self.off[v]), int(self.len[v])
         return self.pool[o:o + l].cpu().numpy()
 
+    def put_seqs(self, out, seqs):
+        """Host sequences into the pool as nodes out_i (one upload)."""
+        out = np.asarray(out, np.int64)
+        lens = np.array([len(x) for x in seqs], np.int64)
+        if not len(out):
+            return
+        dst = self._reserve(int(lens.sum()))
+        self.pool[dst:dst + int(lens.sum())] = torch.from_numpy(
+            np.concatenate([np.asarray(x, np.uint8) for x in seqs])).to(self.dev)
+        self.off[out] = dst + np.cumsum(lens) - lens
+        self.len[out] = lens.astype(np.int32)
+
+    def readjust(self, ch1, ch2, par, mine, out, mode: str = "three"):
+        """``DOS.readjust`` (seqCS.ml:680-722) of nodes mine_i from their
+        neighbours (ch1_i, ch2_i, par_i), the Iterative mode's ThreeD or
+        ApproxD, into nodes out_i; returns (changed, costs)."""
+        from . import iterative
+        items = [(self.node_seq(int(a)), self.node_seq(int(b)), self.node_seq(int(c)),
+                  self.node_seq(int(m))) for a, b, c, m in zip(ch1, ch2, par, mine)]
+        res = iterative.dos_readjust(items, self.cm, mode)
+        self.put_seqs(out, [r[1] for r in res])
+        return (np.array([r[0] for r in res], bool), np.array([r[2] for r in res], np.int64))
+
     def node_fitch(self, v: int) -> np.ndarray:
         return self.fitch[v, :self.nf].cpu().numpy()
 
@@ -1345,6 +1368,15 @@ def _assign_final_states(be, D: _AllDir, k: int, a: int, b: int, n: int) -> dict
 def _assign_single_cost(be, D: _AllDir, k: int, a: int, b: int) -> int:
     """assign_single from root edge k = (a, b) and check_cost, one
     backend's characters."""
+    single, _ = _assign_singles(be, D, k, a, b)
+    ea = np.array([single[x] for x, _ in D.edges], np.int64)
+    eb = np.array([single[y] for _, y in D.edges], np.int64)
+    return int(be.do_distances(ea, eb).sum()) + int(D.other[k])
+
+
+def _assign_singles(be, D: _AllDir, k: int, a: int, b: int):
+    """assign_single (allDirChar.ml:288-404) from root edge k = (a, b):
+    {vertex: node id of its single sequence} and the next free node id."""
     nxt = D.next_id
     be.ensure_nodes(nxt + 1 + len(D.adj))
     root = nxt
@@ -1363,6 +1395,147 @@ def _assign_single_cost(be, D: _AllDir, k: int, a: int, b: int) -> int:
             single[c] = int(o)
             nf.extend((x, c, int(o)) for x in D.adj[c] if x != p)
         front = nf
-    ea = np.array([single[x] for x, _ in D.edges], np.int64)
-    eb = np.array([single[y] for _, y in D.edges], np.int64)
-    return int(be.do_distances(ea, eb).sum()) + int(D.other[k])
+    return single, nxt
+
+
+@dataclass
+class AdjustResult:
+    cost: int           # check_cost of the accepted tree (DO edge distances + non-DO root cost)
+    initial_cost: int   # the same before adjusting (final_cost's)
+    passes: int         # accepted passes
+    changes: int        # vertex readjustments that changed a sequence, accepted passes
+    calls: int          # batched readjust calls (one per level and pass)
+    seqs: dict = field(default_factory=dict)   # vertex -> adjusted DO sequence
+
+
+def adjust_order(tree: Tree, adj: dict):
+    """The interior vertices of the unrooted tree in post-order (children
+    before parents) with their neighbours (ch1, ch2, parent) in the
+    reference's positional order (``Tree.Interior (_, a, b, c)`` ->
+    ``adjust_node a b c``, allDirChar.ml:532-545): the neighbour towards
+    the handle first, then the two others.  The tree's root is dropped and
+    its first child plays the handle, with the root's second child as the
+    neighbour in front of it (visited as its last child)."""
+    n = tree.n
+    r = int(tree.root)
+    top, other = (int(x) for x in tree.kids[r])
+    up = {}
+    for v in adj:
+        if v == top:
+            up[v] = other
+        elif int(tree.parent[v]) == r:
+            up[v] = top
+        else:
+            up[v] = int(tree.parent[v])
+    # post-order from the handle: its own children, then the other side of
+    # the root edge, then the handle
+    order = []
+    stack = [(top, False)]
+    while stack:
+        v, done = stack.pop()
+        if done:
+            if v >= n:
+                order.append(v)
+            continue
+        stack.append((v, True))
+        kids = [x for x in adj[v] if x != up[v]] + ([other] if v == top else [])
+        for x in reversed(kids):
+            stack.append((x, False))
+    nbrs = {v: (up[v],) + tuple(x for x in adj[v] if x != up[v]) for v in order}
+    return order, nbrs
+
+
+def adjust_levels(order, adj):
+    """Batches of the sequential order that keep its results: a vertex
+    reads its neighbours' sequences, so of two adjacent vertices the one
+    earlier in the order must run first (it reads the later one's old
+    sequence, the later one reads its new one).  Level = 1 + the highest
+    level of an earlier adjacent vertex; vertices of a level are pairwise
+    non-adjacent."""
+    pos = {v: i for i, v in enumerate(order)}
+    lvl = {}
+    for v in order:
+        lvl[v] = 1 + max([lvl[u] for u in adj[v] if u in pos and pos[u] < pos[v]], default=-1)
+    out = [[] for _ in range(1 + max(lvl.values(), default=-1))]
+    for v in order:
+        out[lvl[v]].append(v)
+    return out
+
+
+def adjust_tree(tree: Tree, be, mode: str = "three", max_count: int | None = None,
+                batched: bool = True) -> AdjustResult:
+    """``AllDirChar.adjust_tree`` (allDirChar.ml:488-668) of the Iterative
+    cost modes for the DO characters of one backend, after the default
+    diagnosis (``pick_best_root`` and ``assign_single``, see
+    :func:`final_cost`): passes over the interior vertices in post-order,
+    each vertex's sequence re-estimated from its three neighbours' current
+    ones by ``DOS.readjust`` (mode "three": ``readjust_3d``; "approx":
+    ``Sequence.readjust``).  A pass visits the vertices marked by the
+    previous one (the first visits all); a changed vertex marks its three
+    neighbours.  A pass is kept while something changed and the tree cost
+    (``check_cost``: ``DOS.distance`` over every edge plus the rooting's
+    non-DO cost) went down, at most `max_count` passes; otherwise the tree
+    before it is returned.  The root recomputation of ``adjust_handle``
+    leaves this cost unchanged for the DO part and is not done.
+
+    With `batched`, the vertices of a pass run in the batches of
+    :func:`adjust_levels` (the same results as one at a time)."""
+    D = _all_directions(tree, be)
+    if D is None:
+        return AdjustResult(0, 0, 0, 0, 0)
+    tot = D.do_cost + D.other
+    k = int(np.argmin(tot))
+    u, v = D.edges[k]
+    if tree.parent[v] == u:
+        a, b = u, v
+    elif tree.parent[u] == v:
+        a, b = v, u
+    else:
+        a, b = (int(x) for x in tree.kids[tree.root])
+    single, nxt = _assign_singles(be, D, k, a, b)
+    ea = np.array([x for x, _ in D.edges], np.int64)
+    eb = np.array([y for _, y in D.edges], np.int64)
+    other = int(D.other[k])
+
+    def cost_of(cur):
+        return int(be.do_distances(np.array([cur[x] for x in ea]),
+                                   np.array([cur[y] for y in eb])).sum()) + other
+
+    order, nbrs = adjust_order(tree, D.adj)
+    groups = adjust_levels(order, D.adj) if batched else [[x] for x in order]
+    cur = dict(single)
+    prev = cost_of(cur)
+    initial = prev
+    affected = set(cur)
+    count = max_count if max_count is not None else 1 << 30
+    passes = changes = calls = 0
+    while count > 0:
+        new = dict(cur)
+        marked, n_changed = set(), 0
+        for g in groups:
+            g = [x for x in g if x in affected]
+            if not g:
+                continue
+            be.ensure_nodes(nxt + len(g))
+            out = np.arange(nxt, nxt + len(g), dtype=np.int64)
+            nxt += len(g)
+            ch, _ = be.readjust([new[nbrs[x][0]] for x in g], [new[nbrs[x][1]] for x in g],
+                                [new[nbrs[x][2]] for x in g], [new[x] for x in g], out, mode)
+            calls += 1
+            for x, o, c in zip(g, out, ch):
+                if c:
+                    new[x] = int(o)
+                    marked.update(nbrs[x])
+                    n_changed += 1
+        if not n_changed:
+            break
+        c = cost_of(new)
+        if c >= prev:
+            break
+        cur, prev, affected = new, c, marked
+        passes += 1
+        changes += n_changed
+        count -= 1
+    seqs = {x: np.asarray(be.node_seq(cur[x]), np.uint8).copy() for x in order}
+    be.release_nodes(2 * tree.n)
+    return AdjustResult(prev, initial, passes, changes, calls, seqs)

@@ -76,6 +76,17 @@ class OracleBackend:
                 out.append(O.cost_2(s1, s2, self.om, max(abs(len(s1) - len(s2)), 8)))
         return np.array(out, np.int64)
 
+    def readjust(self, ch1, ch2, par, mine, out, mode="three"):
+        ch, cs = [], []
+        tab = O.median3_table(self.om) if mode == "three" else None
+        for a, b, c, m_, o in zip(ch1, ch2, par, mine, out):
+            changed, res, cost = O.dos_readjust(mode, self.seq[int(a)], self.seq[int(b)],
+                                                self.seq[int(c)], self.seq[int(m_)], self.om, tab)
+            self.seq[int(o)] = res
+            ch.append(changed)
+            cs.append(cost)
+        return np.array(ch, bool), np.array(cs, np.int64)
+
     def sank_costs(self, vs):
         return np.array([self.sank_cost(v) for v in vs], np.int64)
 
