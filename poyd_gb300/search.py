@@ -565,12 +565,34 @@ class GpuBackend:
         """``DOS.readjust`` (seqCS.ml:680-722) of nodes mine_i from their
         neighbours (ch1_i, ch2_i, par_i), the Iterative mode's ThreeD or
         ApproxD, into nodes out_i; returns (changed, costs)."""
-        from . import iterative
-        items = [(self.node_seq(int(a)), self.node_seq(int(b)), self.node_seq(int(c)),
-                  self.node_seq(int(m))) for a, b, c, m in zip(ch1, ch2, par, mine)]
-        res = iterative.dos_readjust(items, self.cm, mode)
-        self.put_seqs(out, [r[1] for r in res])
-        return (np.array([r[0] for r in res], bool), np.array([r[2] for r in res], np.int64))
+        from . import iterative, three
+        ch1, ch2, par, mine, out = (np.asarray(x, np.int64) for x in (ch1, ch2, par, mine, out))
+        n = len(out)
+        changed = np.zeros(n, bool)
+        costs = np.zeros(n, np.int64)
+        host = np.arange(n)
+        if mode == "three" and n:
+            # no empty neighbour: readjust_3d on the pool's own bytes, the
+            # medians moved back into the pool on the device
+            emp = self._empty(np.concatenate([ch1, ch2, par])).reshape(3, n).any(axis=0)
+            dev = np.flatnonzero(~emp)
+            host = np.flatnonzero(emp)
+            if len(dev):
+                t = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x, dt)).to(self.dev)
+                ids = (ch1[dev], ch2[dev], mine[dev], par[dev])
+                batch = three.TripleBatch(self.pool, [t(self.off[x], np.int64) for x in ids],
+                                          [t(self.len[x], np.int32) for x in ids])
+                r = three.readjust_3d(batch, self.cm)
+                c, ch = self._store(r, out[dev], r.changed.to(torch.int64))
+                costs[dev], changed[dev] = c, ch.astype(bool)
+        if len(host):
+            items = [(self.node_seq(int(ch1[i])), self.node_seq(int(ch2[i])),
+                      self.node_seq(int(par[i])), self.node_seq(int(mine[i]))) for i in host]
+            res = iterative.dos_readjust(items, self.cm, mode)
+            self.put_seqs(out[host], [x[1] for x in res])
+            changed[host] = [x[0] for x in res]
+            costs[host] = [x[2] for x in res]
+        return changed, costs
 
     def node_fitch(self, v: int) -> np.ndarray:
         return self.fitch[v, :self.nf].cpu().numpy()
