@@ -493,9 +493,10 @@ static int p3_run(int mode, int32_t n, const uint8_t *seq, const int64_t *const 
   if (mm <= 0 || go < 0 || ge <= 0)
     return fail(POYD_EINVAL, "powell_3D_align needs mm > 0, go >= 0, ge > 0 (ukkCommon.c:130)");
   const int nq = mode == 1 ? 4 : 3;
+  for (int q = 0; q < nq; ++q)
+    if (!off[q] || !len[q]) return fail(POYD_EINVAL, "three-sequence batch: null argument");
   std::vector<int32_t> hl[4];
   for (int q = 0; q < nq; ++q) {
-    if (!off[q] || !len[q]) return fail(POYD_EINVAL, "three-sequence batch: null argument");
     hl[q].resize(n);
     CK3(cudaMemcpyAsync(hl[q].data(), len[q], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
   }

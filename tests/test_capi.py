@@ -235,3 +235,38 @@ def test_autotune_table_without_a_gpu(lib):
     lin = _dna(lib)
     assert L.poyd_autotune_batch(C.byref(lin), 1, 0, None, None, None, None, None, 0, None,
                                  None, None, None, 0, 1, C.byref(res), None) == -1
+
+
+@pytest.mark.parametrize("model", [(1, 2, -1), (1, 1, -1), (2, 1, 3)])
+def test_median3_table_matches_oracle(lib, model):
+    """poyd_cm_median3 (host code: Three_D.of_two_dim_comb) equals the
+    oracle's table for metric DNA matrices."""
+    sub, indel, go = model
+    cm = native.PoydCM()
+    native.check(lib.poyd_cm_dna(C.byref(cm), sub, indel, go))
+    tab = np.zeros(32768, np.uint8)
+    native.check(lib.poyd_cm_median3(C.byref(cm), tab.ctypes.data))
+    assert np.array_equal(tab, O.median3_table(O.cm_dna(sub, indel, go)))
+
+
+def test_three_sequence_argument_checks_without_a_gpu(lib):
+    """The three-sequence entry points refuse bad arguments before any CUDA
+    call: a negative count, Powell's parameter rule (ukkCommon.c:130), null
+    arrays, a null cost matrix."""
+    L = C.CDLL(native.LIB_PATH)
+    L.poyd_last_error.restype = C.c_char_p
+    vp = C.c_void_p
+    L.poyd_powell_3d_batch.argtypes = [C.c_int32] + [vp] * 7 + [C.c_int32] * 3 + [vp] * 5 + [vp]
+    L.poyd_readjust_3d_batch.argtypes = [vp, C.c_int32] + [vp] * 15
+    d = np.zeros(64, np.uint8)
+    p = d.ctypes.data
+    assert L.poyd_powell_3d_batch(-1, p, p, p, p, p, p, p, 1, 0, 2, None, p, p, p, p, None) == -1
+    assert L.poyd_powell_3d_batch(0, p, p, p, p, p, p, p, 1, 0, 2, None, p, p, p, p, None) == 0
+    assert L.poyd_powell_3d_batch(1, p, p, p, p, p, p, p, 0, 0, 2, None, p, p, p, p, None) == -1
+    assert b"mm > 0" in L.poyd_last_error()
+    assert L.poyd_powell_3d_batch(1, p, p, p, p, p, None, p, 1, 0, 2, None, p, p, p, p, None) == -1
+    assert L.poyd_readjust_3d_batch(None, 1, *([p] * 14), None) == -1
+    cm = native.PoydCM()
+    native.check(lib.poyd_cm_of_matrix5(C.byref(cm), (C.c_int32 * 25)(*([1] * 25)), -1))
+    cm.combinations = 0
+    assert L.poyd_readjust_3d_batch(C.byref(cm), 1, *([p] * 14), None) == -5
