@@ -28,6 +28,8 @@
 // Among equally cheap alignments the walk keeps the lowest-numbered final
 // state and at every column the lowest-numbered previous state; Powell's
 // recursion may return another of the optimal alignments.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -194,7 +196,7 @@ constexpr unsigned kP3Inf2 = 0xC000C000u;
 // 16-way minimum among the next states of a step when go = 0 let the
 // loads interleave with the arithmetic again and ran 1.5x slower)
 __device__ __forceinline__ unsigned p3_min2(unsigned a, unsigned b) { return __vminu2(a, b); }
-template <bool GO0>
+template <bool GO0, bool CL>
 __device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16_t *dst,
                                               const unsigned *gg, const uint4 ca,
                                               const uint4 cb) {
@@ -203,8 +205,9 @@ __device__ __forceinline__ uint64_t p3_cell16(const uint16_t *const *src, uint16
 #pragma unroll
   for (int d = 0; d < 7; ++d) {
     const uint4 *p = reinterpret_cast<const uint4 *>(src[d]);
-    u[d][0] = p[0];
-    u[d][1] = p[1];
+    // a cluster's blocks write each other's neighbours: read them from L2
+    u[d][0] = CL ? __ldcg(p) : p[0];
+    u[d][1] = CL ? __ldcg(p + 1) : p[1];
   }
   unsigned best[kP3States];
 #pragma unroll
@@ -256,18 +259,32 @@ __device__ __forceinline__ unsigned p3_col2(int k, int x0, int x1, int x2, int m
   return r;
 }
 
-template <bool PACKED, bool GO0>
+// CL: a thread-block cluster per triple (small batches): the rows of a
+// hyperplane are spread over the cluster's blocks and a cluster barrier
+// ends each hyperplane; block 0 of the cluster takes the jobs, writes the
+// early-return outputs and walks the choices back.  Every branch depends
+// only on data all blocks read alike, so all blocks reach every barrier.
+template <bool PACKED, bool GO0, bool CL>
 __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Args A) {
+  namespace cg = cooperative_groups;
   constexpr P3States S = p3_states();
   extern __shared__ uint8_t p3_sm[];
   __shared__ int s_job;
+  const int rank = CL ? (int)cg::this_cluster().block_rank() : 0;
+  const int csz = CL ? (int)cg::this_cluster().num_blocks() : 1;
+  const bool lead = rank == 0;
+  auto bar = [&]() {
+    if (CL) cg::this_cluster().sync();
+    else __syncthreads();
+  };
   const uint8_t *sq[3] = {p3_sm, p3_sm + A.smax, p3_sm + 2 * A.smax};
   uint8_t *sqw[3] = {p3_sm, p3_sm + A.smax, p3_sm + 2 * A.smax};
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int kWarps = kP3Threads / 32;
   // x16 costs: g16[k] = k gap openings, g16[4] = one extension
   const int g16[5] = {0, 16 * A.go, 32 * A.go, 48 * A.go, 16 * A.ge};
-  int32_t *ring = A.ring + (int64_t)blockIdx.x * A.ring_stride;
+  const int64_t slot = CL ? blockIdx.x / csz : blockIdx.x;  // the block's (cluster's) scratch
+  int32_t *ring = A.ring + slot * A.ring_stride;
   // packed: [infinite cell | ring]; the column-cost table after the
   // sequences in shared memory, 8 words per (x0, x1, x2), each 0..4
   uint16_t *const infc = reinterpret_cast<uint16_t *>(ring);
@@ -277,7 +294,8 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
 #pragma unroll
   for (int k = 0; k < 16; ++k) gg[k] = (unsigned)g16[k >> 2] | (unsigned)g16[k & 3] << 16;
   if (PACKED) {
-    if (tid < 2) reinterpret_cast<uint4 *>(infc)[tid] = make_uint4(kP3Inf2, kP3Inf2, kP3Inf2, kP3Inf2);
+    if (lead && tid < 2)
+      reinterpret_cast<uint4 *>(infc)[tid] = make_uint4(kP3Inf2, kP3Inf2, kP3Inf2, kP3Inf2);
     for (int e = tid; e < 125 * 8; e += kP3Threads) {
       const int cmb = e >> 3, k = e & 7;
       const int i0 = cmb / 25, i1 = cmb / 5 % 5, i2 = cmb % 5;
@@ -286,12 +304,13 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
                   16 * A.mm, g16[4]);
     }
   }
-  uint64_t *dir = A.dir + (int64_t)blockIdx.x * A.dir_stride;
+  uint64_t *dir = A.dir + slot * A.dir_stride;
 
   for (;;) {
-    if (tid == 0) s_job = atomicAdd(A.counter, 1);
-    __syncthreads();
-    const int job = s_job;
+    if (lead && tid == 0) s_job = atomicAdd(A.counter, 1);
+    bar();
+    const int job = CL ? *cg::this_cluster().map_shared_rank(&s_job, 0) : s_job;
+    if (CL) cg::this_cluster().sync();  // every block has read block 0's s_job
     if (job >= A.n) break;
     const int i = A.order[job];
     const int la = A.len[0][i], lb = A.len[1][i], lc = A.len[2][i];
@@ -322,17 +341,17 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
         const int lk = keep == 1 ? lm : keep == 2 ? lb : keep == 3 ? la : lc;
         bool diff = lk != lm;
         for (int x = tid; x < lk; x += kP3Threads) {
-          o[4 * cap - lk + x] = k[x];
+          if (lead) o[4 * cap - lk + x] = k[x];
           if (lk == lm) diff |= k[x] != m[x];
         }
         diff = __syncthreads_or(diff);
-        if (tid == 0) {
+        if (lead && tid == 0) {
           A.cost[i] = 0;
           A.out_len[2 * i] = 0;
           A.out_len[2 * i + 1] = lk;
           A.changed[i] = diff ? 1 : 0;
         }
-        __syncthreads();
+        bar();
         continue;
       }
     }
@@ -348,14 +367,14 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
       }
     }
     if (__syncthreads_or(bad)) {
-      if (tid == 0) {
+      if (lead && tid == 0) {
         A.cost[i] = -1;
         A.out_len[2 * i] = -1;
         A.out_len[2 * i + 1] = -1;
         if (A.mode == 1) A.changed[i] = 0;
         atomicOr(A.err, 1);
       }
-      __syncthreads();
+      bar();
       continue;
     }
 
@@ -364,7 +383,7 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
     const int64_t bcs = (int64_t)(nb + 1) * (nc + 1); // choice-cube i-slice
     for (int h = 0; h <= H; ++h) {
       const int a_lo = max(0, h - nb - nc), a_hi = min(na, h);
-      for (int a = a_lo + warp; a <= a_hi; a += kWarps) {  // a warp per row
+      for (int a = a_lo + rank * kWarps + warp; a <= a_hi; a += kWarps * csz) {  // a warp per row
         const int s = h - a, blo = max(0, s - nc), bhi = min(nb, s);
         const int64_t drow = (int64_t)a * bcs + p3_soff(s, nb, nc) - blo;
         if (PACKED && h > 0) {
@@ -386,7 +405,7 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
               src[d - 1] = ok ? ring16 + rb[d - 1] + b16 : infc;
             }
             const int cmb = (i0 * 5 + (b ? __ffs(sq[1][b]) : 0)) * 5 + (c ? __ffs(sq[2][c]) : 0);
-            dir[drow + b] = p3_cell16<GO0>(src, ring16 + ob + b16, gg, ctab[2 * cmb],
+            dir[drow + b] = p3_cell16<GO0, CL>(src, ring16 + ob + b16, gg, ctab[2 * cmb],
                                            ctab[2 * cmb + 1]);
           }
           continue;
@@ -421,15 +440,15 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
           dir[drow + b] = word;
         }
       }
-      __syncthreads();
+      bar();
     }
 
-    if (tid == 0) {
+    if (lead && tid == 0) {
       const int64_t fo = ((int64_t)(H & 3) * pl + (int64_t)na * (nb + 1) + nb) * kP3States;
       const int inf = PACKED ? 0xC000 : kP3Inf;
       int best = inf, st = 0;
       for (int s = 0; s < kP3States; ++s) {
-        const int f = PACKED ? (int)(ring16[fo + s] & 0xFFF0u) : ring[fo + s];
+        const int f = PACKED ? (int)(__ldcg(ring16 + fo + s) & 0xFFF0u) : __ldcg(ring + fo + s);
         if (f < best) best = f, st = s;
       }
       if (PACKED && best >= inf) {  // the optimum reached the clamp: redo in 32 bits
@@ -439,7 +458,8 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
       bool okw = best < inf;
       while (okw && (a | b | c)) {
         const int s = b + c;
-        const uint64_t wd = dir[(int64_t)a * bcs + p3_soff(s, nb, nc) + (b - max(0, s - nc))];
+        const uint64_t wd =
+            __ldcg(dir + (int64_t)a * bcs + p3_soff(s, nb, nc) + (b - max(0, s - nc)));
         const int prev = (int)(wd >> (4 * st) & 15);
         const int ad = c_p3.adv[st];
         if ((ad & 1) > a || (ad >> 1 & 1) > b || (ad >> 2 & 1) > c) {
@@ -477,7 +497,7 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
         A.changed[i] = diff ? 1 : 0;
       }
     }
-    __syncthreads();
+    bar();
   }
 }
 
@@ -585,11 +605,48 @@ static int p3_run(int mode, int32_t n, const uint8_t *seq, const int64_t *const 
   const char *pk = getenv("POYD_P3_PACKED");
   bool packed = !(pk && pk[0] == '0') && 48LL * go + 15 < 0x4000 &&
                 16LL * (2LL * mm + 3LL * ge) < 0x4000;
+  // small batches: a cluster of up to 8 blocks per triple, so that the
+  // batch still covers the SMs (POYD_P3_CLUSTER=0: one block per triple)
+  int csize = 1;
+  {
+    const char *ce = getenv("POYD_P3_CLUSTER");
+    const int64_t want = 3LL * sms / std::max<int64_t>(blocks, 1);
+    if (!(ce && ce[0] == '0'))
+      while (csize < 8 && 2 * csize <= want) csize *= 2;
+  }
   for (;;) {
-    auto kern = packed ? (go == 0 ? k_p3<true, true> : k_p3<true, false>) : k_p3<false, false>;
-    if (smem > 48 * 1024)
-      CK3(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    {
+    auto kern = packed ? (go == 0 ? k_p3<true, true, false> : k_p3<true, false, false>)
+                       : k_p3<false, false, false>;
+    auto kcl = go == 0 ? k_p3<true, true, true> : k_p3<true, false, true>;
+    bool launched = false;
+    if (packed && csize > 1) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)csize;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)(blocks * csize));
+      cfg.blockDim = dim3(kP3Threads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = st;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      if (smem > 48 * 1024)
+        CK3(cudaFuncSetAttribute(kcl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int ncl = 0;
+      if (cudaOccupancyMaxActiveClusters(&ncl, kcl, &cfg) == cudaSuccess && ncl > 0) {
+        ProfScope ps("p3", st);
+        CK3(cudaLaunchKernelEx(&cfg, kcl, A));
+        launched = true;
+      } else {
+        cudaGetLastError();
+        csize = 1;
+      }
+    }
+    if (!launched) {
+      if (smem > 48 * 1024)
+        CK3(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       ProfScope ps("p3", st);
       kern<<<(unsigned)blocks, kP3Threads, smem, st>>>(A);
     }

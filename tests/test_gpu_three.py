@@ -139,3 +139,21 @@ def test_workspace_release_then_reuse():
     again = three.align_3_powell(b, 1, 2, 1).to_host()
     assert [r["cost"] for r in first] == [r["cost"] for r in again]
     assert all(np.array_equal(x["a"], y["a"]) for x, y in zip(first, again))
+
+
+def test_cluster_and_single_block_kernels_agree(monkeypatch):
+    # a small batch runs a thread-block cluster per triple; the one-block
+    # kernel (large batches) must give the same rows
+    for go in (0, 2):
+        T = synth.triple_batch(13 + go, 6, lmin=60, lmax=140)
+        b = three.TripleBatch.from_host(T)
+        monkeypatch.delenv("POYD_P3_CLUSTER", raising=False)
+        cl = three.align_3_powell(b, 1, go, 1).to_host()
+        monkeypatch.setenv("POYD_P3_CLUSTER", "0")
+        one = three.align_3_powell(b, 1, go, 1).to_host()
+        for t, x, y in zip(T, cl, one):
+            assert x["cost"] == y["cost"]
+            for k in "abc":
+                assert np.array_equal(x[k], y[k])
+        c, *rows = O.powell_3d(*T[0], 1, go, 1)
+        assert c == cl[0]["cost"] and all(np.array_equal(r, cl[0][k]) for r, k in zip(rows, "abc"))
