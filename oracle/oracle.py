@@ -4,11 +4,12 @@ Two libraries live here:
 
 * ``_build/liboracle.so`` -- the plain-C restatement of the reference's
   scoring path (``poy_oracle.c``), built by ``build_oracle.sh``;
-* ``_ref/libporef.so`` -- the reference's own ``algn.c`` / ``nonaddCSc.c``
-  compiled from source by ``build_ref.sh`` where the sources are available.
+* ``_ref/libporef.so`` -- the reference's own ``algn.c``, ``ukkCommon.c`` /
+  ``ukk.checkp.c`` and ``nonaddCSc.c`` compiled from source by
+  ``build_ref.sh`` where the sources are available.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU arms use this
-module, and only as the checker.
+module, and only to check or time against the CUDA path.
 """
 from __future__ import annotations
 

@@ -1,7 +1,8 @@
 /*
  * CPU oracle for the POY direct-optimization scoring path (restatement).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, never shipped.
+ * TEST INFRASTRUCTURE ONLY: results the CUDA path is checked against, never
+ * shipped.
  * See poy_oracle.h for the parity pin.  File:line citations are relative to
  * the reference project's src/ directory.
  */

@@ -3,11 +3,13 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
  * algorithms, used by tests/, __graft_entry__.smoke() and the cpu_baseline /
- * reference arm of bench.py as the checker.  Nothing in the poyd_gb300 package
+ * reference arm of bench.py to check and time the CUDA path.  Nothing in the
+ * poyd_gb300 package
  * links, imports or calls it.
  *
  * Parity pin: the restatement is checked against the reference's own C
- * kernels (algn.c, nonaddCSc.c) compiled from source by oracle/build_ref.sh
+ * kernels (algn.c, nonaddCSc.c, ukkCommon.c / ukk.checkp.c) compiled from
+ * source by oracle/build_ref.sh
  * into oracle/_ref/, and against golden vectors in tests/golden/ produced by
  * that compiled reference (tests/golden/make_golden.py).
  *
