@@ -4,8 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
  * algorithms, used by tests/, __graft_entry__.smoke() and the cpu_baseline /
  * reference arm of bench.py to check and time the CUDA path.  Nothing in the
- * poyd_gb300 package
- * links, imports or calls it.
+ * poyd_gb300 package links, imports or calls it.
  *
  * Parity pin: the restatement is checked against the reference's own C
  * kernels (algn.c, nonaddCSc.c, ukkCommon.c / ukk.checkp.c) compiled from
