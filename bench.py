@@ -67,7 +67,8 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="headline only: skip the affine, SPR, learned, readjust_3d and serving keys")
     p.add_argument("--workload", default="align",
-                   choices=["align", "spr", "tbr", "learned", "serving", "kernels", "three"],
+                   choices=["align", "spr", "tbr", "learned", "serving", "kernels", "three",
+                            "adjust"],
                    help="align (default, the headline line) or one of the other configs")
     p.add_argument("--train-trees", type=int, default=2)
     p.add_argument("--max-passes", type=int, default=8)
@@ -832,6 +833,49 @@ def run_three(args):
     }
 
 
+def run_adjust(args):
+    """Iterative cost modes end to end: ``AllDirChar.adjust_tree`` after the
+    default diagnosis of a seeded random tree (100 taxa x 500 bp, JC 0.1 per
+    site per branch, indels 0.02; DNA sub 1 / indel 2), ThreeD and ApproxD,
+    on the GPU backend; the same driver over the CPU oracle on a 20-taxon x
+    120 bp tree gives the CPU time and the parity check."""
+    import torch
+    from oracle import oracle as O
+    from poyd_gb300 import align, learned, search, simulate
+    from tests.oracle_backend import OracleBackend  # the CPU leg only
+    torch.cuda.set_device(0)
+    out = {"workload": "Iterative modes: adjust_tree, 100 taxa x 500 bp (GPU), 20 x 120 (parity)",
+           "metric": "seconds per adjustment", "unit": "s", "higher_is_better": False,
+           "data": "synthetic (seeded)", "modes": {}}
+    big = simulate.simulate(3, 100, 500, 0, 0, sub_per_branch=0.1, indel_rate=0.02)
+    small = simulate.simulate(4, 20, 120, 0, 0, sub_per_branch=0.1, indel_rate=0.02)
+    tb, ts = learned.random_tree(100, 9), learned.random_tree(20, 9)
+    for mode in ("three", "approx"):
+        be = search.GpuBackend(big, align.CostMatrix.default())
+        search.adjust_tree(tb, be, mode, max_count=1)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = search.adjust_tree(tb, be, mode)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        g = search.adjust_tree(ts, search.GpuBackend(small, align.CostMatrix.default()), mode)
+        torch.cuda.synchronize()
+        gdt = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        o = search.adjust_tree(ts, OracleBackend(small, O.cm_dna(1, 2, -1)), mode)
+        cdt = time.perf_counter() - t1
+        same = (g.cost, g.passes, g.changes) == (o.cost, o.passes, o.changes) and \
+            all(np.array_equal(g.seqs[v], o.seqs[v]) for v in o.seqs)
+        out["modes"][mode] = {
+            "seconds": dt, "cost_before": r.initial_cost, "cost_after": r.cost,
+            "passes": r.passes, "changes": r.changes, "batched_calls": r.calls,
+            "parity_20_taxa": {"identical": bool(same), "cost": g.cost, "gpu_seconds": gdt},
+            "cpu_baseline_20_taxa": {"seconds": cdt, "cores": 1, "kind": "port"}}
+    out["value"] = out["modes"]["three"]["seconds"]
+    return out
+
+
 def run_kernels(args):
     """The other kernels on their own: Fitch and Sankoff distance / median
     over node arrays larger than L2 (HBM-bound: achieved GB/s of the bytes
@@ -971,6 +1015,8 @@ def main():
         _emit(run_kernels(args))
     elif args.workload == "three":
         _emit(run_three(args))
+    elif args.workload == "adjust":
+        _emit(run_adjust(args))
     else:
         run_ours(args)
 
