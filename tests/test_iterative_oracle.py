@@ -29,3 +29,13 @@ def test_empty_neighbour_rules():
     # unchanged median: changed is False
     ch, res, _ = O.dos_readjust("three", a, a, a, a, m)
     assert not ch and res.tolist() == a.tolist()
+
+
+def test_host_select_one_matches_oracle():
+    # the GPU module's select_one (host numpy) against the oracle's
+    from poyd_gb300 import iterative
+    m = O.cm_dna(1, 2, -1)
+    rng = np.random.default_rng(2)
+    s = rng.integers(1, 32, size=200).astype(np.uint8)
+    s[0] = 16
+    assert np.array_equal(iterative.select_one(s, None), O.select_one(s, m))
