@@ -131,9 +131,8 @@ __device__ __forceinline__ int p3_ix(int x) { return __ffs(x) - 1; }  // 1 2 4 8
 
 // One cell (a, b, c) of hyperplane h: its 16 values (x16, into the ring)
 // and its 64-bit choice word (returned).
-__device__ __forceinline__ uint64_t p3_cell(const P3Args &A, int32_t *ring, int64_t pl, int nb,
-                                            int h, int a, int b, int c, const uint8_t *const *sq,
-                                            const int *g16, const int *col16) {
+__device__ __forceinline__ uint64_t p3_cell(int32_t *ring, int64_t pl, int nb, int h, int a,
+                                            int b, int c, const int *g16, const int *col16) {
   constexpr P3States S = p3_states();
   int best[kP3States];
 #pragma unroll
@@ -435,7 +434,7 @@ __global__ void __launch_bounds__(kP3Threads) k_p3(const __grid_constant__ P3Arg
               const int ch = ((d & 1) ? x0 : 0) | ((d & 2) ? x1 : 0) | ((d & 4) ? x2 : 0);
               col16[d] = 16 * A.mm * (__popc(ch) - 1);
             }
-            word = p3_cell(A, ring, pl, nb, h, a, b, c, sq, g16, col16);
+            word = p3_cell(ring, pl, nb, h, a, b, c, g16, col16);
           }
           dir[drow + b] = word;
         }
