@@ -270,3 +270,23 @@ def test_three_sequence_argument_checks_without_a_gpu(lib):
     native.check(lib.poyd_cm_of_matrix5(C.byref(cm), (C.c_int32 * 25)(*([1] * 25)), -1))
     cm.combinations = 0
     assert L.poyd_readjust_3d_batch(C.byref(cm), 1, *([p] * 14), None) == -5
+
+
+def test_median3_table_non_metric_matches_oracle(lib):
+    """poyd_cm_median3 over arbitrary 5x5 matrices (the non-metric ones
+    take the gap into a median only where two of the three states hold
+    it) equals the oracle's Three_D.of_two_dim_comb."""
+    rng = np.random.default_rng(8)
+    for t in range(8):
+        mat = rng.integers(0, 6, size=(5, 5)).astype(np.int32)
+        if t % 2 == 0:
+            mat = np.minimum(mat, mat.T)
+            np.fill_diagonal(mat, 0)
+        m = native.PoydCM()
+        assert lib.poyd_cm_of_matrix5(C.byref(m), mat.ctypes.data, -1) == 0
+        o = O.OrCM()
+        O.lib().or_cm_of_matrix5(C.byref(o), mat.ctypes.data_as(O.i32p), -1)
+        assert m.is_metric == o.is_metric
+        tab = np.zeros(32768, np.uint8)
+        native.check(lib.poyd_cm_median3(C.byref(m), tab.ctypes.data))
+        assert np.array_equal(tab, O.median3_table(o)), t
