@@ -10,18 +10,20 @@
 // optimum is searched.  Here each triple is one dynamic program over the
 // full (la x lb x lc) cube and the 16 states, swept by hyperplanes
 // h = i + j + k (a cell depends only on the three hyperplanes before it):
-//   * one block per triple, persistent over a largest-first queue; a warp
-//     takes a row (fixed i) of the hyperplane, a lane one cell of it;
+//   * one block per triple (a cluster of 2-8 blocks for small batches),
+//     persistent over a largest-first queue; a warp takes a row (fixed i)
+//     of the hyperplane, a lane one cell of it;
 //   * a thread computes all 16 states of its cell: every state reads one
 //     neighbour cell (the one its column consumes from), so a cell loads 7
-//     neighbours of 16 values; values are stored x16 with the previous
-//     state in the low 4 bits, so that one fused add-min per (previous,
-//     next) state pair keeps the least cost and, on ties, the
-//     lowest-numbered previous state;
+//     neighbours of 16 values; values are stored x16 with a state number
+//     in the low 4 bits, so that one add-min per (previous, next) state
+//     pair keeps the least cost and, on ties, the lowest-numbered previous
+//     state; by default two states per 32-bit word (16-bit halves), the
+//     32-bit values as the fallback for large costs;
 //   * the last four hyperplanes' values in a ring in global memory
-//     ([h & 3][i][j][state], int32); the 16 choices of a cell (4 bits
-//     each) in one 64-bit word of a per-triple cube laid out [i][j + k][j]
-//     so that a hyperplane's cells of one i are contiguous;
+//     ([h & 3][i][j][state]); the 16 choices of a cell (4 bits each) in
+//     one 64-bit word of a per-triple cube laid out [i][j + k][j] so that
+//     a hyperplane's cells of one i are contiguous;
 //   * then one thread walks the choices back and writes the three aligned
 //     rows and the column medians (Cost_matrix.Three_D.median) right-aligned
 //     into the triple's slot.
