@@ -65,10 +65,10 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="launch the default variant instead of the autotuner's choice")
     p.add_argument("--no-extras", action="store_true",
-                   help="headline only: skip the affine, SPR, learned, readjust_3d and serving keys")
+                   help="headline only: skip the affine, SPR, learned, config0, readjust_3d and serving keys")
     p.add_argument("--workload", default="align",
                    choices=["align", "spr", "tbr", "learned", "serving", "kernels", "three",
-                            "adjust"],
+                            "adjust", "config0"],
                    help="align (default, the headline line) or one of the other configs")
     p.add_argument("--train-trees", type=int, default=2)
     p.add_argument("--max-passes", type=int, default=8)
@@ -318,6 +318,10 @@ def run_ours(args):
         # search's exact cost
         line["learned_speedup"] = lrn.get("speedup") if lrn.get("reached_same_cost") else None
         line["learned"] = lrn
+        c0 = _guard(lambda: run_config0(extras))
+        line["config0_s"] = c0.get("value")
+        line["config0"] = c0
+        failed |= c0.get("parity", {}).get("identical_tree_costs_and_medians") is False
         tri = argparse.Namespace(**vars(extras))
         tri.steps, tri.warmup = min(args.steps, 5), 1
         line["readjust_3d"] = _guard(lambda: run_three(tri))
@@ -833,6 +837,44 @@ def run_three(args):
     }
 
 
+def run_config0(args):
+    """Config 0: a Wagner build plus one SPR pass on 20 taxa x ~300 bp
+    (seeded Yule tree, JC 0.05 per site per branch, indels 0.01 per site;
+    DNA sub 1 / indel 2), wall time of the whole search on the GPU backend
+    and on the oracle backend (the CPU restatement, one core), and parity:
+    the same tree, the same costs and every per-node median."""
+    import torch
+    from oracle import oracle as O
+    from poyd_gb300 import align, search, simulate
+    from tests.oracle_backend import OracleBackend  # the CPU leg only
+    torch.cuda.set_device(0)
+    data = simulate.simulate(args.seed, 20, 300)
+
+    def run(be):
+        t0 = time.perf_counter()
+        t, d = search.wagner(data.n_taxa, be)
+        st = search.spr_pass(t, be, max_moves=16)
+        if hasattr(be, "pool"):
+            torch.cuda.synchronize()
+        return time.perf_counter() - t0, t, d, st
+
+    run(search.GpuBackend(data, align.CostMatrix.default()))  # warm-up
+    g = search.GpuBackend(data, align.CostMatrix.default())
+    gdt, tg, dg, sg = run(g)
+    o = OracleBackend(data, O.cm_dna(1, 2, -1))
+    odt, to, do, so = run(o)
+    same = tg.newick() == to.newick() and (dg.total, sg.cost_after) == (do.total, so.cost_after) \
+        and all(np.array_equal(g.node_seq(v), o.node_seq(v)) for v in tg.nodes())
+    return {"workload": "config 0: Wagner build + one SPR pass, 20 taxa x ~300 bp",
+            "metric": "seconds per search", "value": gdt, "unit": "s", "higher_is_better": False,
+            "data": "synthetic (seeded)", "wagner_cost": int(dg.total),
+            "spr": {"cost_before": sg.cost_before, "cost_after": sg.cost_after,
+                    "moves_accepted": sg.moves_accepted},
+            "parity": {"identical_tree_costs_and_medians": bool(same)},
+            "cpu_baseline": {"value": odt, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": "the same search on the oracle backend"}}
+
+
 def run_adjust(args):
     """Iterative cost modes end to end: ``AllDirChar.adjust_tree`` after the
     default diagnosis of a seeded random tree (100 taxa x 500 bp, JC 0.1 per
@@ -1017,6 +1059,8 @@ def main():
         _emit(run_three(args))
     elif args.workload == "adjust":
         _emit(run_adjust(args))
+    elif args.workload == "config0":
+        _emit(run_config0(args))
     else:
         run_ours(args)
 
